@@ -1,0 +1,209 @@
+/*
+ * gbba.h - C ABI of the GB300 bundle-adjustment engine.
+ *
+ * This is the drop-in boundary that replaces the ceres::Problem / ceres::Solve
+ * block of the reference's bundle-adjustment call sites:
+ *   - IncrementalReconstructionEngine::BundleAdjustment
+ *       libs/sfm/src/sfm_incremental_engine.cpp:1395-1473 (problem build,
+ *       options, Solve) and :1476 (IsSolutionUsable + write-back);
+ *   - GlobalReconstructionEngine::bundleAdjustment_t_Xi / _Rt_Xi
+ *       libs/sfm/src/sfm_global_engine.cpp:1546-1594, 1756-1802;
+ *   - the two-view refinement, libs/sfm/src/sfm_global_engine.cpp:1142-1174.
+ * The flat parameter layout is the one of the reference containers
+ * BA_Problem_data_camMotionAndIntrinsic<6,K> / BAProblemData<N>
+ * (libs/sfm/include/mvg/sfm/problem_data_container.h:16-121): extrinsics as
+ * [angle-axis(3), t(3)] per camera, intrinsics as one block per group, points
+ * as [X,Y,Z], observations as (x,y) pairs with per-observation indices.
+ *
+ * Conventions (the reference's, libs/sfm + ceres 1.10):
+ *   - the caller owns every array; refinement is in place;
+ *   - no exceptions and no abort: every entry point returns a gbba_status and
+ *     fills a summary that mirrors ceres::Solver::Summary;
+ *   - cost = 1/2 * sum_i rho(|r_i|^2) (ceres residual_block.cc:160-166);
+ *   - a handle is not thread safe: use one handle per host thread.
+ * No C++ types cross this boundary.
+ */
+#ifndef GBBA_H_
+#define GBBA_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBBA_ABI_VERSION 1
+
+typedef enum gbba_status {
+  GBBA_SUCCESS = 0,
+  GBBA_ERROR_INVALID_ARGUMENT = 1, /* bad sizes, index out of range, NULL array */
+  GBBA_ERROR_CUDA = 2,             /* a CUDA runtime call failed */
+  GBBA_ERROR_OUT_OF_MEMORY = 3,    /* device allocation failed (nothing aborted) */
+  GBBA_ERROR_NUMERICAL = 4,        /* non-finite cost at the initial point */
+  GBBA_ERROR_NOT_SUPPORTED = 5,
+  GBBA_ERROR_TOO_LARGE = 6,        /* problem exceeds a documented limit */
+  GBBA_ERROR_NO_DEVICE = 7,
+  GBBA_ERROR_TIMEOUT = 8           /* a bounded device-side wait gave up */
+} gbba_status;
+
+/* Camera models.  Residual r = predicted - observed, with
+ *   p = R(w) X + t      (ceres::AngleAxisRotatePoint, rotation.h:566-625)
+ *   x = p0/p2, y = p1/p2
+ * PINHOLE_F : pred = f*(x,y)            k = 1 [f]; observations pre-centred by
+ *             the principal point (pinhole_ceres_functor.h:24-54,
+ *             sfm_bundle_adjustment_helper_tonly.h:11-76).
+ * RADIAL_K3 : pred = pp + f*(x,y)*(1+k1 r2+k2 r4+k3 r6)      k = 6
+ *             [f,ppx,ppy,k1,k2,k3] (pinhole_brown_rt_ceres_functor.h:60-107,
+ *             brown_pinhole_camera.h:15-41).
+ * BROWN_T2  : RADIAL_K3 plus the tangential terms the reference has only as a
+ *             commented-out formula (brown_pinhole_camera.h:35-36):
+ *             xd += 2 t1 x y + t2 (r2 + 2x^2), yd += 2 t2 x y + t1 (r2 + 2y^2)
+ *             k = 8 [f,ppx,ppy,k1,k2,k3,t1,t2]. */
+typedef enum gbba_camera_model {
+  GBBA_PINHOLE_F = 0,
+  GBBA_RADIAL_K3 = 1,
+  GBBA_BROWN_T2 = 2
+} gbba_camera_model;
+
+typedef enum gbba_loss {
+  GBBA_LOSS_SQUARED = 0, /* ceres TrivialLoss / NULL loss */
+  GBBA_LOSS_HUBER = 1    /* ceres::HuberLoss(a): rho(s) = s if s <= a^2, else 2a sqrt(s) - a^2 */
+} gbba_loss;
+
+typedef enum gbba_linear_solver {
+  GBBA_SOLVER_AUTO = 0,            /* dense Schur up to options.dense_schur_max_size, else iterative */
+  GBBA_SOLVER_DENSE_SCHUR = 1,     /* dense Cholesky of the reduced camera system S */
+  GBBA_SOLVER_ITERATIVE_SCHUR = 2  /* block-Jacobi PCG on S */
+} gbba_linear_solver;
+
+typedef enum gbba_precision {
+  GBBA_PRECISION_FP64 = 0,  /* every kernel in FP64: the plain GPU path */
+  GBBA_PRECISION_MIXED = 1  /* FP32 Jacobians / Schur build / factor, FP64 cost and refinement */
+} gbba_precision;
+
+typedef enum gbba_memory {
+  GBBA_MEMORY_HOST = 0,   /* arrays are host pointers; copies are done by the call */
+  GBBA_MEMORY_DEVICE = 1  /* arrays are device pointers on the handle's device */
+} gbba_memory;
+
+/* Same values as ceres::TerminationType (include/ceres/types.h:324-344). */
+typedef enum gbba_termination {
+  GBBA_CONVERGENCE = 0,
+  GBBA_NO_CONVERGENCE = 1,
+  GBBA_FAILURE = 2
+} gbba_termination;
+
+typedef struct gbba_problem {
+  int32_t camera_model;          /* gbba_camera_model */
+  int32_t memory;                /* gbba_memory of every array below */
+  int64_t num_cameras;           /* extrinsic blocks */
+  int64_t num_intrinsics;        /* intrinsic groups */
+  int64_t num_points;
+  int64_t num_observations;
+  double* extrinsics;            /* [num_cameras][6]  angle-axis, t   (in/out) */
+  double* intrinsics;            /* [num_intrinsics][k]               (in/out) */
+  double* points;                /* [num_points][3]                   (in/out) */
+  const double* observations;    /* [num_observations][2] pixels */
+  const uint32_t* camera_index;     /* [num_observations] */
+  const uint32_t* intrinsic_index;  /* [num_observations] */
+  const uint32_t* point_index;      /* [num_observations] */
+  const uint8_t* camera_constant;    /* [num_cameras] 1 = SetParameterBlockConstant, or NULL */
+  const uint8_t* intrinsic_constant; /* [num_intrinsics] or NULL */
+  uint32_t extrinsic_fixed_mask; /* bit j: coordinate j of every extrinsic block held
+                                    (rotation-only-fixed translation refinement, :1438) */
+  uint32_t intrinsic_fixed_mask; /* bit j: coordinate j of every intrinsic block held
+                                    (ceres::SubsetParameterization, :1396-1409) */
+} gbba_problem;
+
+typedef struct gbba_options {
+  /* ceres::Solver::Options names and defaults (include/ceres/solver.h:81-129) */
+  int32_t max_num_iterations;             /* 50 */
+  int32_t max_num_consecutive_invalid_steps; /* 5 */
+  double function_tolerance;              /* 1e-6 */
+  double gradient_tolerance;              /* 1e-10 */
+  double parameter_tolerance;             /* 1e-8 */
+  double initial_trust_region_radius;     /* 1e4 */
+  double max_trust_region_radius;         /* 1e16 */
+  double min_trust_region_radius;         /* 1e-32 */
+  double min_relative_decrease;           /* 1e-3 */
+  double min_lm_diagonal;                 /* 1e-6 */
+  double max_lm_diagonal;                 /* 1e32 */
+  int32_t jacobi_scaling;                 /* 1 */
+  int32_t loss_type;                      /* gbba_loss */
+  double loss_scale;                      /* Huber a (pixels) */
+  int32_t linear_solver;                  /* gbba_linear_solver */
+  int32_t precision;                      /* gbba_precision */
+  int32_t max_linear_solver_iterations;   /* 500 (PCG) */
+  int32_t dense_schur_max_size;           /* AUTO switches to PCG above this S size: 16384 */
+  double eta;                             /* 0.1: PCG forcing sequence (ceres q-tolerance) */
+  int32_t refinement_interval;            /* mixed PCG: FP64 residual recompute every k steps: 8 */
+  int32_t use_cuda_graphs;                /* 1: capture the per-iteration launch sequence */
+  void* stream;                           /* cudaStream_t, or NULL for the handle's stream */
+} gbba_options;
+
+typedef struct gbba_summary {
+  double initial_cost;
+  double final_cost;
+  int32_t num_iterations;          /* LM iterations run (successful + unsuccessful) */
+  int32_t num_successful_steps;
+  int32_t num_unsuccessful_steps;
+  int32_t termination_type;        /* gbba_termination */
+  int32_t usable;                  /* ceres Summary::IsSolutionUsable() */
+  int32_t linear_solver_iterations;/* total PCG iterations (0 for dense) */
+  int64_t reduced_system_size;     /* rows of S */
+  double total_time_s;
+  double jacobian_time_s;          /* Schur build (residual + Jacobian + elimination) */
+  double linear_solver_time_s;     /* factorisation / PCG + back-substitution */
+  double residual_time_s;          /* cost evaluations of candidate steps */
+} gbba_summary;
+
+typedef struct gbba_handle gbba_handle;
+
+/* Create a handle bound to CUDA device `device`.  It owns a stream and a
+ * workspace that is grown on demand and reused across solves. */
+gbba_status gbba_create(int device, gbba_handle** out);
+void gbba_destroy(gbba_handle* handle);
+void gbba_default_options(gbba_options* options);
+const char* gbba_status_string(gbba_status status);
+int gbba_abi_version(void);
+/* Number of CUDA kernel launches issued through this handle so far. */
+int64_t gbba_launch_count(const gbba_handle* handle);
+
+/* Refine extrinsics, intrinsics and points in place: the replacement of
+ * ceres::Solve with SPARSE_SCHUR/DENSE_SCHUR on the reference problems.
+ * Parameters are written back only when the solution is usable. */
+gbba_status gbba_solve(gbba_handle* handle, const gbba_problem* problem,
+                       const gbba_options* options, gbba_summary* summary);
+
+/* Solve `num_problems` independent problems (local-BA windows) in one call.
+ * Each problem is solved with the same options; summaries[i] belongs to
+ * problems[i].  All problems must use the same camera model and memory. */
+gbba_status gbba_solve_batched(gbba_handle* handle, const gbba_problem* problems,
+                               int32_t num_problems, const gbba_options* options,
+                               gbba_summary* summaries);
+
+/* Differentiation contract, forward half: residuals r = pred - obs (not
+ * robustified, [num_observations][2], may be NULL) and the robustified cost
+ * 1/2 sum rho(|r|^2) (may be NULL).  Replaces ceres::Problem::Evaluate's
+ * residual output (include/ceres/problem.h:392-468). */
+gbba_status gbba_project_forward(gbba_handle* handle, const gbba_problem* problem,
+                                 int32_t loss_type, double loss_scale,
+                                 double* residuals, double* cost);
+
+/* Differentiation contract, backward half: per-observation Jacobian blocks of
+ * the robustified residual (ceres Corrector applied, corrector.cc:118-155),
+ * row-major per block: jac_extrinsic [N_o][2][6], jac_intrinsic [N_o][2][k],
+ * jac_point [N_o][2][3]; and the gradient J^T r of the robustified problem
+ * laid out as [extrinsics | intrinsics | points] (same layout as the
+ * parameters).  Any output may be NULL.  The projection is recomputed, no
+ * intermediate of the forward call is stored. */
+gbba_status gbba_project_backward(gbba_handle* handle, const gbba_problem* problem,
+                                  int32_t loss_type, double loss_scale,
+                                  double* jac_extrinsic, double* jac_intrinsic,
+                                  double* jac_point, double* gradient);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBBA_H_ */

@@ -1,0 +1,182 @@
+"""Python access to the CPU oracle (liboracle.so, built from gbba_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU baseline, never by the product package.
+"""
+import ctypes as C
+import importlib
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
+_lib = None
+
+
+def _abi():
+    return importlib.import_module("3dreconstruction_gb300.abi")
+
+
+def build():
+    subprocess.run(["make", "-C", HERE, "liboracle.so"], check=True, stdout=subprocess.DEVNULL)
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        abi = _abi()
+        lib = C.CDLL(LIB)
+        vp = C.c_void_p
+        lib.oracle_ba_solve.argtypes = [C.POINTER(abi.GbbaProblem), C.POINTER(abi.GbbaOptions),
+                                        C.POINTER(abi.GbbaSummary), vp, C.c_int, C.c_int]
+        lib.oracle_ba_solve.restype = C.c_int
+        lib.oracle_ba_evaluate.argtypes = [C.POINTER(abi.GbbaProblem), C.c_int, C.c_double, vp, vp, vp, vp, vp, vp]
+        lib.oracle_ba_evaluate.restype = C.c_int
+        lib.oracle_tri_dlt2.argtypes = [C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp]
+        lib.oracle_tri_nview.argtypes = [C.c_int, vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp]
+        lib.oracle_tri_linear_gn.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int, vp, vp, vp]
+        _lib = lib
+    return _lib
+
+
+def ba_solve(scene, options, num_threads=0, max_costs=1024):
+    """Solve a scene with the oracle; returns (summary dict, params dict, iteration costs)."""
+    abi = _abi()
+    lib = load()
+    hp = abi.HostProblem(scene)
+    p = hp.struct()
+    s = abi.GbbaSummary()
+    costs = np.zeros(max_costs)
+    st = lib.oracle_ba_solve(C.byref(p), C.byref(options), C.byref(s), costs.ctypes.data, max_costs, num_threads)
+    n = s.num_iterations + 1
+    return st, s.as_dict(), hp.params(), costs[:min(n, max_costs)]
+
+
+def ba_evaluate(scene, loss_type=0, loss_scale=1.0):
+    abi = _abi()
+    lib = load()
+    hp = abi.HostProblem(scene)
+    p = hp.struct()
+    k = abi.MODEL_K[hp.model]
+    no, nc, ni, npt = p.num_observations, p.num_cameras, p.num_intrinsics, p.num_points
+    cost = np.zeros(1)
+    res = np.zeros((no, 2))
+    je = np.zeros((no, 2, 6))
+    ji = np.zeros((no, 2, k))
+    jp = np.zeros((no, 2, 3))
+    g = np.zeros(6 * nc + k * ni + 3 * npt)
+    lib.oracle_ba_evaluate(C.byref(p), loss_type, loss_scale, cost.ctypes.data, res.ctypes.data,
+                           je.ctypes.data, ji.ctypes.data, jp.ctypes.data, g.ctypes.data)
+    return {"cost": cost[0], "residuals": res, "jac_extrinsic": je, "jac_intrinsic": ji,
+            "jac_point": jp, "gradient": g}
+
+
+def tri_dlt2(P1, P2, x1, x2, shared=False):
+    lib = load()
+    n = len(x1)
+    P1 = np.ascontiguousarray(P1, np.float64)
+    P2 = np.ascontiguousarray(P2, np.float64)
+    x1 = np.ascontiguousarray(x1, np.float64)
+    x2 = np.ascontiguousarray(x2, np.float64)
+    Xh = np.zeros((n, 4))
+    Xe = np.zeros((n, 3))
+    lib.oracle_tri_dlt2(n, P1.ctypes.data, P2.ctypes.data, 0 if shared else 12, x1.ctypes.data,
+                        x2.ctypes.data, Xh.ctypes.data, Xe.ctypes.data)
+    return Xh, Xe
+
+
+def tri_nview(method, P, offsets, cam, xy):
+    lib = load()
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 12)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    cam = np.ascontiguousarray(cam, np.uint32)
+    xy = np.ascontiguousarray(xy, np.float64)
+    n = len(offsets) - 1
+    X = np.zeros((n, 3 if method == 2 else 4))
+    err = np.zeros(n)
+    lib.oracle_tri_nview(method, P.ctypes.data, len(P), offsets.ctypes.data, cam.ctypes.data,
+                         xy.ctypes.data, n, X.ctypes.data, err.ctypes.data)
+    return X, err
+
+
+def tri_linear_gn(P, offsets, cam, xy, gn_steps=1):
+    lib = load()
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 12)
+    offsets = np.ascontiguousarray(offsets, np.int64)
+    cam = np.ascontiguousarray(cam, np.uint32)
+    xy = np.ascontiguousarray(xy, np.float64)
+    n = len(offsets) - 1
+    X = np.zeros((n, 3))
+    st = np.zeros(n, np.uint8)
+    md = np.zeros(n)
+    lib.oracle_tri_linear_gn(P.ctypes.data, offsets.ctypes.data, cam.ctypes.data, xy.ctypes.data, n,
+                             gn_steps, X.ctypes.data, st.ctypes.data, md.ctypes.data)
+    return X, st, md
+
+
+# ------------------------------------------------------------ reference harness
+def write_kv(path, items):
+    with open(path, "w") as f:
+        for name, v in items.items():
+            a = np.asarray(v, dtype=np.float64).ravel()
+            f.write(f"{name} {a.size}\n")
+            f.write(" ".join(repr(float(x)) for x in a))
+            f.write("\n")
+
+
+def read_kv(path):
+    out = {}
+    with open(path) as f:
+        toks = f.read().split()
+    i = 0
+    while i < len(toks):
+        name, n = toks[i], int(toks[i + 1])
+        out[name] = np.array([float(t) for t in toks[i + 2:i + 2 + n]])
+        i += 2 + n
+    return out
+
+
+def ref_available():
+    return os.path.exists(REF_HARNESS)
+
+
+def ref_run(mode, items, tmpdir, extra_args=()):
+    """Run the reference harness (compiled from the reference sources)."""
+    inp = os.path.join(tmpdir, f"{mode}_in.txt")
+    out = os.path.join(tmpdir, f"{mode}_out.txt")
+    if items is not None:
+        write_kv(inp, items)
+        args = [REF_HARNESS, mode, inp, out]
+    else:
+        args = [REF_HARNESS, mode, *map(str, extra_args), out]
+    r = subprocess.run(args, capture_output=True, text=True)
+    if r.returncode not in (0, 1):
+        raise RuntimeError(f"ref_harness {mode} failed: {r.stderr[-2000:]}")
+    return read_kv(out)
+
+
+def scene_to_kv(scene, options, layout=0, linear_solver=0, num_threads=1):
+    """BA problem + options in the harness's input format."""
+    model = int(scene["model"])
+    d = {
+        "model": model, "layout": layout,
+        "loss": options.loss_type, "loss_scale": options.loss_scale,
+        "extrinsics": scene["extrinsics"], "intrinsics": scene["intrinsics"], "points": scene["points"],
+        "observations": scene["observations"], "camera_index": scene["camera_index"],
+        "intrinsic_index": scene["intrinsic_index"], "point_index": scene["point_index"],
+        "intrinsic_fixed_mask": scene.get("intrinsic_fixed_mask", 0),
+        "extrinsic_fixed_mask": scene.get("extrinsic_fixed_mask", 0),
+        "linear_solver": linear_solver, "max_num_iterations": options.max_num_iterations,
+        "function_tolerance": options.function_tolerance, "gradient_tolerance": options.gradient_tolerance,
+        "parameter_tolerance": options.parameter_tolerance, "num_threads": num_threads,
+    }
+    if scene.get("camera_constant") is not None:
+        d["camera_constant"] = scene["camera_constant"]
+    if scene.get("intrinsic_constant") is not None:
+        d["intrinsic_constant"] = scene["intrinsic_constant"]
+    return d
