@@ -1,0 +1,107 @@
+// Host-side internals shared by the translation units of libgbba: the handle,
+// its device workspace, error plumbing and launch accounting.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/gbba.h"
+#include "../../include/gbtri.h"
+
+namespace gbba {
+
+// Error type carried across internal C++ calls; converted to gbba_status at
+// the C boundary (no exception crosses it).
+struct Error {
+  gbba_status status;
+  std::string what;
+};
+
+#define GBBA_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      throw ::gbba::Error{e_ == cudaErrorMemoryAllocation ? GBBA_ERROR_OUT_OF_MEMORY      \
+                                                          : GBBA_ERROR_CUDA,              \
+                          std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+    }                                                                                     \
+  } while (0)
+
+#define GBBA_REQUIRE(cond, st, msg)                    \
+  do {                                                 \
+    if (!(cond)) throw ::gbba::Error{(st), (msg)};     \
+  } while (0)
+
+// A device arena: one growable allocation carved by a bump pointer.  Solves
+// reuse it across calls, so the steady state makes no cudaMalloc.
+struct Arena {
+  char* base = nullptr;
+  size_t capacity = 0;
+  size_t used = 0;
+  size_t high_water = 0;
+  void reset() { used = 0; }
+  void reserve(size_t bytes) {
+    if (bytes <= capacity) return;
+    if (base) cudaFree(base);
+    base = nullptr;
+    capacity = 0;
+    GBBA_CUDA(cudaMalloc(&base, bytes));
+    capacity = bytes;
+  }
+  template <typename T>
+  T* take(size_t count) {
+    const size_t bytes = ((count * sizeof(T)) + 255) & ~size_t(255);
+    GBBA_REQUIRE(used + bytes <= capacity, GBBA_ERROR_OUT_OF_MEMORY, "workspace overflow");
+    T* p = reinterpret_cast<T*>(base + used);
+    used += bytes;
+    if (used > high_water) high_water = used;
+    return p;
+  }
+  void release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+    capacity = used = 0;
+  }
+};
+
+// Size planner: the same sequence of take() calls run against a counter so
+// that the arena can be reserved once before the real carve.
+struct Planner {
+  size_t used = 0;
+  template <typename T>
+  T* take(size_t count) {
+    used += ((count * sizeof(T)) + 255) & ~size_t(255);
+    return nullptr;
+  }
+};
+
+}  // namespace gbba
+
+struct gbba_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  gbba::Arena arena;
+  // small pinned host buffer for per-iteration scalars
+  double* pinned = nullptr;
+  int64_t launches = 0;
+  int sm_count = 0;
+  cudaStream_t active = nullptr;  // stream of the current call
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
+namespace gbba {
+
+inline void count_launch(gbba_handle* h, int n = 1) { h->launches += n; }
+
+inline void check_launch(gbba_handle* h) {
+  count_launch(h);
+  GBBA_CUDA(cudaGetLastError());
+}
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace gbba

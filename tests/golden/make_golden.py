@@ -1,0 +1,137 @@
+"""Generate the golden fixtures of tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_harness -- the reference's own code (its ceres
+functors + vendored ceres 1.10 / CXSparse / Eigen, and libs/multiview
+triangulation) compiled from the reference sources by `make -C oracle ref` --
+on small seeded inputs and stores inputs and outputs as .npz files.  Needs the
+reference sources, so it runs in the development container only; the
+fixtures it writes are committed and travel with the tests.
+
+    python tests/golden/make_golden.py
+"""
+import importlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402
+
+abi = importlib.import_module("3dreconstruction_gb300.abi")
+scenes = importlib.import_module("3dreconstruction_gb300.scenes")
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(OUT, name), **{k: np.asarray(v) for k, v in arrays.items()})
+    print("wrote", name)
+
+
+def tri_ring(tmp, nviews, npoints):
+    """The scenes of the reference's triangulation unit tests
+    (libs/multiview/src/triangulation_unittest.cpp:12,
+    triangulation_nview_unittest.cpp:9) with the reference outputs."""
+    r = oracle.ref_run("tri-ring", None, tmp, extra_args=(nviews, npoints))
+    save(f"tri_ring_{nviews}x{npoints}.npz", **r)
+
+
+def tri_noisy(tmp):
+    tr = scenes.track_scene(num_cameras=24, num_tracks=300, seed=21, max_len=12)
+    r = oracle.ref_run("tri", {"P": tr["P"], "track_offsets": tr["track_offsets"],
+                               "camera_index": tr["camera_index"], "xy": tr["xy"]}, tmp)
+    save("tri_noisy.npz", P=tr["P"], track_offsets=tr["track_offsets"], camera_index=tr["camera_index"],
+         xy=tr["xy"], **r)
+
+
+def scene_arrays(sc):
+    keys = ("extrinsics", "intrinsics", "points", "observations", "camera_index", "intrinsic_index", "point_index")
+    out = {k: sc[k] for k in keys}
+    out["model"] = sc["model"]
+    out["camera_constant"] = sc.get("camera_constant") if sc.get("camera_constant") is not None else np.zeros(len(sc["extrinsics"]), np.uint8)
+    out["intrinsic_constant"] = sc.get("intrinsic_constant") if sc.get("intrinsic_constant") is not None else np.zeros(len(sc["intrinsics"]), np.uint8)
+    out["intrinsic_fixed_mask"] = sc.get("intrinsic_fixed_mask", 0)
+    out["extrinsic_fixed_mask"] = sc.get("extrinsic_fixed_mask", 0)
+    return out
+
+
+def ba_case(tmp, name, sc, layout=0, **opt):
+    o = scenes.ba_options_for(sc, **opt)
+    r = oracle.ref_run("ba", oracle.scene_to_kv(sc, o, layout=layout, linear_solver=0), tmp)
+    save(f"ba_{name}.npz", layout=layout, loss=o.loss_type, loss_scale=o.loss_scale,
+         max_num_iterations=o.max_num_iterations, **scene_arrays(sc),
+         **{"ref_" + k: v for k, v in r.items()})
+
+
+def eval_case(tmp, name, sc, loss=0, a=1.0):
+    o = scenes.ba_options_for(sc, loss_type=loss, loss_scale=a)
+    r = oracle.ref_run("eval", oracle.scene_to_kv(sc, o), tmp)
+    save(f"eval_{name}.npz", loss=loss, loss_scale=a, **scene_arrays(sc), **{"ref_" + k: v for k, v in r.items()})
+
+
+def unit_test_scene(tmp):
+    """The reference's BA unit test (libs/sfm/src/bundle_adjustment_unittest.cpp:
+    19-122): NRealisticCamerasRing(3,6), [R t f] blocks, observations centred by
+    the principal point (500,500) and shifted by its integer-division "noise"
+    rand()/RAND_MAX - 0.5 = -0.5, squared loss."""
+    r = oracle.ref_run("tri-ring", None, tmp, extra_args=(3, 6))
+    P = r["P"].reshape(3, 3, 4)
+    R = r["R"].reshape(3, 3, 3)
+    t = r["t"].reshape(3, 3)
+    X = r["X_gt"].reshape(6, 3)
+    xy = r["xy"].reshape(-1, 2)
+    cam = r["camera_index"].astype(np.uint32)
+    pt = np.repeat(np.arange(6), 3).astype(np.uint32)
+    obs = xy - 500.0 - 0.5
+    ext = np.concatenate([scenes.rotation_to_angle_axis(R), t], 1)
+    sc = {"model": abi.PINHOLE_F, "extrinsics": ext, "intrinsics": np.full((3, 1), 1000.0), "points": X,
+          "observations": obs, "camera_index": cam, "intrinsic_index": cam.copy(), "point_index": pt}
+    return sc, P
+
+
+def main():
+    if not oracle.ref_available():
+        raise SystemExit("oracle/_ref/ref_harness missing: run `make -C oracle ref` first")
+    tmp = tempfile.mkdtemp()
+    tri_ring(tmp, 2, 12)
+    tri_ring(tmp, 5, 6)
+    tri_noisy(tmp)
+
+    # BA problems, each solved by ceres SPARSE_SCHUR/CX_SPARSE with the
+    # reference functor of the layout.  The per-camera-intrinsics scenes keep a
+    # scale gauge free (only camera 0 is held, as in the incremental engine),
+    # so they are run to convergence: two correct LM implementations then agree
+    # on the final cost, not on every rounding of the trajectory.
+    sc = scenes.ring_scene(num_cameras=16, num_points=300, seed=31)
+    ba_case(tmp, "ring_k3_const", sc, max_num_iterations=20)
+    sc = scenes.ring_scene(num_cameras=10, num_points=200, seed=32)
+    sc["intrinsic_constant"][:] = 0
+    sc["intrinsic_fixed_mask"] = 0b111110  # the incremental engine's !refine subset (:1396-1409)
+    ba_case(tmp, "ring_k3_focal_huber", sc, max_num_iterations=20, loss_type=abi.LOSS_HUBER, loss_scale=4.0)
+    sc = scenes.medium_scene(num_cameras=12, num_points=300, seed=33)
+    ba_case(tmp, "k3_percam_huber", sc, max_num_iterations=100)
+    sc = scenes.medium_scene(num_cameras=8, num_points=200, seed=34, model=abi.BROWN_T2)
+    ba_case(tmp, "t2_percam_huber", sc, max_num_iterations=100)
+    sc = scenes.ring_scene(num_cameras=8, num_points=150, seed=35, model=abi.PINHOLE_F)
+    sc["intrinsic_constant"][:] = 0
+    ba_case(tmp, "pinhole_f_split", sc, max_num_iterations=20)
+    sc = scenes.ring_scene(num_cameras=8, num_points=150, seed=36, model=abi.PINHOLE_F)
+    sc["extrinsic_fixed_mask"] = 0b000111  # rotation held: translation-only refinement (:1438)
+    ba_case(tmp, "t_only", sc, layout=2, max_num_iterations=20, loss_type=abi.LOSS_HUBER, loss_scale=16.0)
+    sc = scenes.ring_scene(num_cameras=8, num_points=150, seed=37, model=abi.PINHOLE_F)
+    ba_case(tmp, "rt_only", sc, layout=3, max_num_iterations=20, loss_type=abi.LOSS_HUBER, loss_scale=4.0)
+    sc, _ = unit_test_scene(tmp)
+    ba_case(tmp, "unit_test_rtf7", sc, layout=1, max_num_iterations=50)
+
+    # Problem::Evaluate at the initial point (Jacobian pins)
+    eval_case(tmp, "k3", scenes.medium_scene(num_cameras=4, num_points=15, seed=41), loss=abi.LOSS_HUBER, a=4.0)
+    eval_case(tmp, "t2", scenes.medium_scene(num_cameras=4, num_points=15, seed=42, model=abi.BROWN_T2))
+    sc = scenes.ring_scene(num_cameras=4, num_points=15, seed=43, model=abi.PINHOLE_F)
+    sc["extrinsics"][1, :3] = [1e-9, -2e-9, 5e-10]  # small-angle branch of AngleAxisRotatePoint
+    eval_case(tmp, "pinhole_f", sc)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+"""GPU triangulation through the C ABI against the reference's golden outputs
+and the oracle.  Tolerances: FP64 paths 1e-9 (relative to the coordinate
+scale; homogeneous vectors compared up to their unspecified sign); the FP32
+production path against its FP64 twin in the oracle: 2e-4 absolute on points
+in [-3,3]^3 (FP32 normal equations), status codes exact."""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from test_oracle_golden import same_up_to_sign
+
+pytestmark = pytest.mark.gpu
+
+
+def dlt2(handle, abi, P1, P2, x1, x2, shared=False):
+    n = len(x1)
+    Xh = np.zeros((n, 4))
+    Xe = np.zeros((n, 3))
+    P1 = np.ascontiguousarray(P1, np.float64)
+    P2 = np.ascontiguousarray(P2, np.float64)
+    x1 = np.ascontiguousarray(x1, np.float64)
+    x2 = np.ascontiguousarray(x2, np.float64)
+    handle.check(handle.lib.gbtri_dlt2_batched(handle.h, n, P1.ctypes.data, P2.ctypes.data, 0 if shared else 12,
+                                               x1.ctypes.data, x2.ctypes.data, Xh.ctypes.data, Xe.ctypes.data,
+                                               abi.MEMORY_HOST), "dlt2")
+    return Xh, Xe
+
+
+def nview(handle, abi, method, P, off, cam, xy):
+    nt = len(off) - 1
+    X = np.zeros((nt, 3 if method == abi.TRI_ITERATIVE else 4))
+    err = np.zeros(nt)
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 12)
+    off = np.ascontiguousarray(off, np.int64)
+    cam = np.ascontiguousarray(cam, np.uint32)
+    xy = np.ascontiguousarray(xy, np.float64)
+    st = handle.lib.gbtri_nview_batched(handle.h, method, P.ctypes.data, len(P), off.ctypes.data, cam.ctypes.data,
+                                        xy.ctypes.data, nt, X.ctypes.data, err.ctypes.data, abi.MEMORY_HOST)
+    return st, X, err
+
+
+@pytest.mark.parametrize("case", ["tri_ring_2x12.npz", "tri_ring_5x6.npz", "tri_noisy.npz"])
+def test_fp64_triangulation_matches_reference(case, handle, abi):
+    g = load_golden(case)
+    P = g["P"].reshape(-1, 12)
+    off = g["track_offsets"].astype(np.int64)
+    cam = g["camera_index"].astype(np.uint32)
+    xy = g["xy"].reshape(-1, 2)
+    nt = len(off) - 1
+    f = off[:-1]
+    Xh, Xe = dlt2(handle, abi, P[cam[f]], P[cam[f + 1]], xy[f], xy[f + 1])
+    assert same_up_to_sign(Xh, g["dlt_h"].reshape(nt, 4), 1e-9)
+    np.testing.assert_allclose(Xe, g["dlt_e"].reshape(nt, 3), rtol=1e-9, atol=1e-9)
+    for method, key in ((abi.TRI_NVIEW, "nview_h"), (abi.TRI_NVIEW_ALGEBRAIC, "algebraic_h")):
+        st, X, _ = nview(handle, abi, method, P, off, cam, xy)
+        assert st == 0
+        assert same_up_to_sign(X, g[key].reshape(nt, 4), 1e-9), key
+    st, X, err = nview(handle, abi, abi.TRI_ITERATIVE, P, off, cam, xy)
+    assert st == 0
+    np.testing.assert_allclose(X, g["iterative_e"].reshape(nt, 3), rtol=1e-10, atol=1e-10)
+    np.testing.assert_allclose(err, g["iterative_error"], rtol=1e-6, atol=1e-9)
+
+
+def test_reference_unit_test_assertions_on_gpu(handle, abi):
+    """triangulation_unittest.cpp:21 (L-inf < 1e-8) with a shared P pair, and
+    triangulation_nview_unittest.cpp:32/62 (reprojection < 1e-9)."""
+    g = load_golden("tri_ring_2x12.npz")
+    P = g["P"].reshape(-1, 12)
+    xy = g["xy"].reshape(-1, 2)
+    _, Xe = dlt2(handle, abi, P[0], P[1], xy[0::2], xy[1::2], shared=True)
+    assert np.abs(Xe - g["X_gt"].reshape(-1, 3)).max() < 1e-8
+    g = load_golden("tri_ring_5x6.npz")
+    P = g["P"].reshape(-1, 3, 4)
+    off = g["track_offsets"].astype(np.int64)
+    cam = g["camera_index"].astype(np.uint32)
+    xy = g["xy"].reshape(-1, 2)
+    for method in (abi.TRI_NVIEW, abi.TRI_NVIEW_ALGEBRAIC):
+        st, X, _ = nview(handle, abi, method, P, off, cam, xy)
+        h = np.einsum("vij,tj->tvi", P, X)
+        assert np.abs(h[..., :2] / h[..., 2:3] - xy.reshape(6, 5, 2)).max() < 1e-9
+
+
+def f32_path(handle, abi, tr, gn_steps=1):
+    nt = len(tr["track_offsets"]) - 1
+    P32 = np.ascontiguousarray(tr["P"], np.float32)
+    off = np.ascontiguousarray(tr["track_offsets"], np.uint32)
+    cam = np.ascontiguousarray(tr["camera_index"], np.uint32)
+    xy = np.ascontiguousarray(tr["xy"], np.float32)
+    X = np.zeros((nt, 3), np.float32)
+    st = np.zeros(nt, np.uint8)
+    md = np.zeros(nt, np.float32)
+    handle.check(handle.lib.gbtri_nview_batched_f32(handle.h, P32.ctypes.data, len(P32), off.ctypes.data,
+                                                    cam.ctypes.data, xy.ctypes.data, nt, gn_steps, X.ctypes.data,
+                                                    st.ctypes.data, md.ctypes.data, abi.MEMORY_HOST), "f32")
+    return X, st, md
+
+
+def test_fp32_path_matches_fp64_twin(handle, abi, scenes, oracle_mod):
+    tr = scenes.track_scene(num_cameras=200, num_tracks=20000, seed=2)
+    X, st, md = f32_path(handle, abi, tr)
+    Xo, sto, mdo = oracle_mod.tri_linear_gn(tr["P"], tr["track_offsets"], tr["camera_index"], tr["xy"], 1)
+    assert np.array_equal(st, sto)
+    assert np.abs(X - Xo).max() < 2e-4
+    np.testing.assert_allclose(md, mdo, rtol=1e-4)
+    # and the estimate is as good as the reference's N-view DLT: error vs ground truth
+    e32 = np.linalg.norm(X - tr["X_true"], axis=1)
+    assert np.median(e32) < 0.01
+
+
+def test_fp32_path_edge_cases(handle, abi):
+    # a 1-view track (degenerate), a track behind its cameras, an empty track, a normal track
+    K = np.array([[1000, 0, 960], [0, 1000, 540], [0, 0, 1.0]])
+    Ps = []
+    for cx in (-1.0, 1.0):
+        Rt = np.concatenate([np.eye(3), np.array([[-cx], [0], [10.0]])], 1)
+        Ps.append((K @ Rt).ravel())
+    P = np.array(Ps)
+
+    def proj(X, c):
+        h = P[c].reshape(3, 4) @ np.append(X, 1.0)
+        return h[:2] / h[2]
+
+    Xg = np.array([0.3, -0.2, 1.0])
+    Xb = np.array([0.1, 0.1, -20.0])  # behind both cameras (depth 10 - 20 < 0)
+    xy = [proj(Xg, 0), proj(Xb, 0), proj(Xb, 1), proj(Xg, 0), proj(Xg, 1)]
+    tr = {"P": P, "track_offsets": np.array([0, 1, 3, 3, 5]), "camera_index": np.array([0, 0, 1, 0, 1], np.uint32),
+          "xy": np.array(xy)}
+    X, st, md = f32_path(handle, abi, tr, gn_steps=2)
+    assert list(st) == [abi.TRACK_DEGENERATE, abi.TRACK_BEHIND_CAMERA, abi.TRACK_DEGENERATE, abi.TRACK_OK]
+    assert np.abs(X[3] - Xg).max() < 1e-4
+
+
+def test_nview_too_long_track_rejected(handle, abi):
+    n = 40
+    P = np.tile(np.eye(3, 4).ravel(), (n, 1))
+    off = np.array([0, n])
+    cam = np.arange(n, dtype=np.uint32)
+    xy = np.zeros((n, 2))
+    st, _, _ = nview(handle, abi, abi.TRI_NVIEW, P, off, cam, xy)
+    assert st == abi.ERROR_TOO_LARGE
+
+
+def test_refine_gn_fp64(handle, abi, scenes, oracle_mod):
+    tr = scenes.track_scene(num_cameras=30, num_tracks=2000, seed=81, max_len=10)
+    Xo, _, _ = oracle_mod.tri_linear_gn(tr["P"], tr["track_offsets"], tr["camera_index"], tr["xy"], 0)
+    X = np.ascontiguousarray(Xo.copy())
+    P = np.ascontiguousarray(tr["P"])
+    off = np.ascontiguousarray(tr["track_offsets"], np.int64)
+    cam = np.ascontiguousarray(tr["camera_index"], np.uint32)
+    xy = np.ascontiguousarray(tr["xy"])
+    handle.check(handle.lib.gbtri_refine_gn(handle.h, P.ctypes.data, len(P), off.ctypes.data, cam.ctypes.data,
+                                            xy.ctypes.data, len(off) - 1, 2, X.ctypes.data, abi.MEMORY_HOST), "gn")
+    X2, _, _ = oracle_mod.tri_linear_gn(tr["P"], tr["track_offsets"], tr["camera_index"], tr["xy"], 2)
+    np.testing.assert_allclose(X, X2, atol=1e-9)
