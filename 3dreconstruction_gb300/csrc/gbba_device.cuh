@@ -57,7 +57,7 @@ __device__ __forceinline__ void rotate(const T w[3], const T X[3], T p[3], T R[3
       R[1][0] = s * u[2] + omc * u[1] * u[0]; R[1][1] = c + omc * u[1] * u[1];       R[1][2] = -s * u[0] + omc * u[1] * u[2];
       R[2][0] = -s * u[1] + omc * u[2] * u[0]; R[2][1] = s * u[0] + omc * u[2] * u[1]; R[2][2] = c + omc * u[2] * u[2];
       // d/dw_k with dtheta/dw_k = u_k and du_i/dw_k = (delta_ik - u_i u_k)/theta
-      const T eX[3][3] = {{T(0), -X[2], X[1]}, {X[2], T(0), -X[0]}, {-X[1], X[0], T(0)}};  // column k = e_k x X
+      const T eX[3][3] = {{T(0), X[2], -X[1]}, {-X[2], T(0), X[0]}, {X[1], -X[0], T(0)}};  // column k = e_k x X
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         const T duX = ith * (X[k] - u[k] * udX);  // (du/dw_k) . X
