@@ -115,6 +115,10 @@ class GbbaSummary(C.Structure):
         ("jacobian_time_s", C.c_double),
         ("linear_solver_time_s", C.c_double),
         ("residual_time_s", C.c_double),
+        ("schur_kernel_time_s", C.c_double),
+        ("schur_kernel_launches", C.c_int32),
+        ("factor_launches", C.c_int32),
+        ("factor_time_s", C.c_double),
     ]
 
     def as_dict(self):

@@ -884,8 +884,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   if (gmax <= o->gradient_tolerance) term = GBBA_CONVERGENCE;
   double radius = o->initial_trust_region_radius, decrease_factor = 2.0;
   int invalid_steps = 0, iteration = 0;
-  cudaEvent_t ev[4];
-  for (int i = 0; i < 4; ++i) GBBA_CUDA(cudaEventCreate(&ev[i]));
+  cudaEvent_t ev[6];
+  for (int i = 0; i < 6; ++i) GBBA_CUDA(cudaEventCreate(&ev[i]));
   while (term < 0) {
     if (iteration >= o->max_num_iterations) {
       term = GBBA_NO_CONVERGENCE;
@@ -901,13 +901,18 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     k_schur_init<T><<<(unsigned)std::min<int64_t>(ceil_div(s.n_pad, 256), 1024), 256, 0, st>>>(S, rhs, s.n_red, s.n_pad,
                                                                                             s.diag_c, s.radius);
     check_launch(h);
+    GBBA_CUDA(cudaEventRecord(ev[4], st));
     if (s.np > 0) {
       k_schur_point<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, s.diag_p, s.radius, S, s.n_pad, rhs,
                                                     (T*)s.Vinv, (T*)s.gpv, (T*)s.Wbuf, (T*)s.What, s.flag);
       check_launch(h);
+      ++sum->schur_kernel_launches;
     }
     GBBA_CUDA(cudaEventRecord(ev[1], st));
+    const int64_t launches0 = h->launches;
     dense_cholesky_solve<T>(h, S, s.n_pad, rhs, z, (T*)s.Linv, s.flag, st);
+    sum->factor_launches += (int32_t)(h->launches - launches0);
+    GBBA_CUDA(cudaEventRecord(ev[5], st));
     if (s.np > 0) {
       k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2, s.part_mcc,
                                                 s.part_step_p, s.flag);
@@ -927,10 +932,14 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     GBBA_CUDA(cudaMemcpyAsync(&hs->flag, s.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaMemcpyAsync(&hs->nonfinite, s.nonfinite, sizeof(int), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaStreamSynchronize(st));
-    float ms_a = 0, ms_b = 0, ms_c = 0;
+    float ms_a = 0, ms_b = 0, ms_c = 0, ms_k = 0, ms_f = 0;
     cudaEventElapsedTime(&ms_a, ev[0], ev[1]);
     cudaEventElapsedTime(&ms_b, ev[1], ev[2]);
     cudaEventElapsedTime(&ms_c, ev[2], ev[3]);
+    cudaEventElapsedTime(&ms_k, ev[4], ev[1]);
+    cudaEventElapsedTime(&ms_f, ev[1], ev[5]);
+    sum->schur_kernel_time_s += ms_k * 1e-3;
+    sum->factor_time_s += ms_f * 1e-3;
     sum->jacobian_time_s += ms_a * 1e-3;
     sum->linear_solver_time_s += ms_b * 1e-3;
     sum->residual_time_s += ms_c * 1e-3;
@@ -983,7 +992,7 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       if (radius < o->min_trust_region_radius) term = GBBA_CONVERGENCE;
     }
   }
-  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   sum->termination_type = term;
   sum->usable = term != GBBA_FAILURE ? 1 : 0;
   sum->final_cost = cost;

@@ -156,6 +156,12 @@ typedef struct gbba_summary {
   double jacobian_time_s;          /* Schur build (residual + Jacobian + elimination) */
   double linear_solver_time_s;     /* factorisation / PCG + back-substitution */
   double residual_time_s;          /* cost evaluations of candidate steps */
+  /* Device time of individual kernels, from CUDA events recorded around their
+   * launches on the solve's stream (used for roofline accounting). */
+  double schur_kernel_time_s;      /* point-major Schur elimination kernel(s) */
+  int32_t schur_kernel_launches;
+  int32_t factor_launches;         /* kernels in the dense factorisation + solves */
+  double factor_time_s;            /* dense Cholesky + triangular solves */
 } gbba_summary;
 
 typedef struct gbba_handle gbba_handle;
