@@ -100,10 +100,11 @@ def main():
     tri_noisy(tmp)
 
     # BA problems, each solved by ceres SPARSE_SCHUR/CX_SPARSE with the
-    # reference functor of the layout.  The per-camera-intrinsics scenes keep a
-    # scale gauge free (only camera 0 is held, as in the incremental engine),
-    # so they are run to convergence: two correct LM implementations then agree
-    # on the final cost, not on every rounding of the trajectory.
+    # reference functor of the layout.  With per-camera intrinsics, holding
+    # only camera 0 (the incremental engine's gauge) leaves the scale free and
+    # the minimum is a flat valley on which two correct LM implementations stop
+    # at different points; these scenes also hold camera 1 so that the
+    # minimum is isolated and runs to convergence are comparable.
     sc = scenes.ring_scene(num_cameras=16, num_points=300, seed=31)
     ba_case(tmp, "ring_k3_const", sc, max_num_iterations=20)
     sc = scenes.ring_scene(num_cameras=10, num_points=200, seed=32)
@@ -111,8 +112,10 @@ def main():
     sc["intrinsic_fixed_mask"] = 0b111110  # the incremental engine's !refine subset (:1396-1409)
     ba_case(tmp, "ring_k3_focal_huber", sc, max_num_iterations=20, loss_type=abi.LOSS_HUBER, loss_scale=4.0)
     sc = scenes.medium_scene(num_cameras=12, num_points=300, seed=33)
+    sc["camera_constant"][1] = 1
     ba_case(tmp, "k3_percam_huber", sc, max_num_iterations=100)
     sc = scenes.medium_scene(num_cameras=8, num_points=200, seed=34, model=abi.BROWN_T2)
+    sc["camera_constant"][1] = 1
     ba_case(tmp, "t2_percam_huber", sc, max_num_iterations=100)
     sc = scenes.ring_scene(num_cameras=8, num_points=150, seed=35, model=abi.PINHOLE_F)
     sc["intrinsic_constant"][:] = 0
