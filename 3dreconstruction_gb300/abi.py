@@ -42,6 +42,9 @@ CONVERGENCE = 0
 NO_CONVERGENCE = 1
 FAILURE = 2
 
+NOALLOC_MAX_BLOCKS = 16384
+NOALLOC_OBS_PER_BLOCK = 2048
+
 # gbtri_method
 TRI_NVIEW = 0
 TRI_NVIEW_ALGEBRAIC = 1
@@ -276,6 +279,8 @@ def declare_gbba(lib):
     lib.gbba_project_forward.restype = C.c_int
     lib.gbba_project_backward.argtypes = [vp, P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp, vp]
     lib.gbba_project_backward.restype = C.c_int
+    lib.gbba_project_forward_noalloc.argtypes = [P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp]
+    lib.gbba_project_forward_noalloc.restype = C.c_int
     lib.gbtri_dlt2_batched.argtypes = [vp, C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     lib.gbtri_dlt2_batched.restype = C.c_int
     lib.gbtri_nview_batched.argtypes = [vp, C.c_int32, vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp, C.c_int32]
@@ -291,6 +296,6 @@ def declare_gbba(lib):
 EXPORTED_SYMBOLS = (
     "gbba_create", "gbba_destroy", "gbba_default_options", "gbba_status_string",
     "gbba_abi_version", "gbba_launch_count", "gbba_solve", "gbba_solve_batched",
-    "gbba_project_forward", "gbba_project_backward",
+    "gbba_project_forward", "gbba_project_backward", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
 )

@@ -209,6 +209,29 @@ gbba_status gbba_project_backward(gbba_handle* handle, const gbba_problem* probl
                                   double* jac_extrinsic, double* jac_intrinsic,
                                   double* jac_point, double* gradient);
 
+/* Forward projection that allocates nothing.  It has no counterpart in the
+ * reference; it exists for callers that cannot call cudaMalloc -- a host
+ * application whose device memory is already owned by its own pool
+ * allocator, or a real-time loop that may not pay an allocation's implicit
+ * synchronisation.  Same outputs as gbba_project_forward (residuals r = pred -
+ * obs, [num_observations][2], and the robustified cost 1/2 sum rho(|r|^2)),
+ * but every array of `problem` and both outputs must be DEVICE memory on the
+ * current device (problem->memory == GBBA_MEMORY_DEVICE; `cost` points to one
+ * double, either output may be NULL), no handle is needed, and the call is
+ * asynchronous on `stream` (a cudaStream_t; NULL is the default stream).
+ * Its scratch is a fixed array inside the library (GBBA_NOALLOC_MAX_BLOCKS
+ * partial sums, ~128 KB held by every GPU that loads the library until exit):
+ * problems above GBBA_NOALLOC_MAX_BLOCKS * GBBA_NOALLOC_OBS_PER_BLOCK
+ * observations (33,554,432) are rejected with GBBA_ERROR_TOO_LARGE.  The first
+ * call on each device looks up the scratch's device address; make that first
+ * call before any stream capture.  All calls share the scratch: calls that
+ * overlap on the GPU race.  An out-of-range index yields NaN residuals and a
+ * NaN cost instead of a fault. */
+#define GBBA_NOALLOC_MAX_BLOCKS 16384
+#define GBBA_NOALLOC_OBS_PER_BLOCK 2048
+gbba_status gbba_project_forward_noalloc(const gbba_problem* problem, int32_t loss_type, double loss_scale,
+                                         double* residuals, double* cost, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
