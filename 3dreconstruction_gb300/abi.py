@@ -100,6 +100,8 @@ class GbbaOptions(C.Structure):
         ("refinement_interval", C.c_int32),
         ("use_cuda_graphs", C.c_int32),
         ("stream", C.c_void_p),
+        ("fp64_polish_iterations", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -153,6 +155,8 @@ def default_options(**kw):
     o.refinement_interval = 8
     o.use_cuda_graphs = 1
     o.stream = None
+    o.fp64_polish_iterations = 10
+    o.reserved = 0
     for k, v in kw.items():
         if not hasattr(o, k):
             raise AttributeError(k)

@@ -9,6 +9,8 @@
 
 namespace gbba {
 gbba_status solve_impl(gbba_handle* h, const gbba_problem* P, const gbba_options* o, gbba_summary* sum);
+gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_t n, const gbba_options* o,
+                               gbba_summary* sums);
 
 static int model_k(int m) { return m == kPinholeF ? 1 : m == kRadialK3 ? 6 : 8; }
 
@@ -214,6 +216,8 @@ void gbba_default_options(gbba_options* o) {
   o->refinement_interval = 8;
   o->use_cuda_graphs = 1;
   o->stream = nullptr;
+  o->fp64_polish_iterations = 10;
+  o->reserved = 0;
 }
 
 gbba_status gbba_create(int device, gbba_handle** out) {
@@ -245,6 +249,7 @@ void gbba_destroy(gbba_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->arena.release();
+  h->pair_arena.release();
   if (h->pinned) cudaFreeHost(h->pinned);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
@@ -263,11 +268,12 @@ gbba_status gbba_solve(gbba_handle* h, const gbba_problem* P, const gbba_options
 gbba_status gbba_solve_batched(gbba_handle* h, const gbba_problem* problems, int32_t num_problems,
                                const gbba_options* o, gbba_summary* summaries) {
   if (!problems || !o || !summaries || num_problems < 0) return GBBA_ERROR_INVALID_ARGUMENT;
+  if (num_problems == 0) return GBBA_SUCCESS;
   for (int32_t i = 0; i < num_problems; ++i) {
-    const gbba_status st = gbba_solve(h, &problems[i], o, &summaries[i]);
-    if (st != GBBA_SUCCESS) return st;
+    const gbba_status pc = check_problem(&problems[i]);
+    if (pc != GBBA_SUCCESS) return pc;
   }
-  return GBBA_SUCCESS;
+  return guarded(h, o->stream, [&]() { return solve_batched_impl(h, problems, num_problems, o, summaries); });
 }
 
 gbba_status gbba_project_forward(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,

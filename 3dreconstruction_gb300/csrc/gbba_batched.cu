@@ -1,0 +1,918 @@
+// Batched local bundle adjustment: thousands of independent problems in one
+// launch (gbba_solve_batched).
+//
+// Each problem is an independent ceres-style LM solve (the same semantics as
+// gbba_solve: Jacobi scaling, LM diagonal, Schur elimination, step quality and
+// radius update, ceres's terminations -- trust_region_minimizer.cc,
+// levenberg_marquardt_strategy.cc).  Local windows are small (<= 40 cameras,
+// reduced camera system <= 256 unknowns), so one CTA owns one problem for its
+// whole solve:
+//   - the lower triangle of S, rhs, the step and the camera-side scaling live
+//     in shared memory (S: n(n+1)/2 values, <= 131.6 KB in FP32);
+//   - points are processed one warp per point (V, V^-1, g_p, W, W V^-1), the
+//     pair products are accumulated into shared-memory S with shared atomics;
+//   - the Cholesky factorisation and both triangular solves run in shared
+//     memory; the accept / reject decision is taken by thread 0.
+// CTAs never wait on each other, so the launch cannot deadlock; the hardware
+// schedules the next problem onto an SM as soon as one finishes (problems are
+// ordered largest first to shorten the tail).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gbba_device.cuh"
+#include "gbba_internal.h"
+
+namespace gbba {
+
+void scan_offsets(gbba_handle* h, const uint32_t* counts, uint32_t* off, int64_t n, uint32_t* tmp_chunks,
+                  cudaStream_t st);
+__global__ void k_scatter(const uint32_t* pt, int64_t no, const uint32_t* off, uint32_t* fill, uint32_t* perm);
+__global__ void k_segment_sort(uint32_t* perm, const uint32_t* off, int64_t np);
+
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kWarps = kThreads / 32;
+
+template <typename T> struct NMax;
+template <> struct NMax<float> { static constexpr int v = 256; };
+template <> struct NMax<double> { static constexpr int v = 176; };
+
+struct BProb {
+  uint32_t o0, o1;  // observations (sorted by point)
+  uint32_t x0, x1;  // points
+  uint32_t c0, nc;  // cameras
+  uint32_t g0, ni;  // intrinsic groups
+  uint32_t n;       // reduced camera-side size
+  uint32_t pad;
+};
+
+struct BOut {
+  double initial_cost, final_cost;
+  int32_t iterations, successful, unsuccessful, termination, usable, status;
+};
+
+struct BArgs {
+  const BProb* probs;
+  const uint32_t* order;
+  double *ext, *intr, *pts, *ext2, *intr2, *pts2;
+  const double2* obs;
+  const uint32_t *cam, *icam, *pt_off;
+  const int32_t *ext_col, *intr_col;  // problem-local reduced columns (-1 = held)
+  const uint8_t* intr_var;
+  double *scale_p, *diag_p;
+  void *Vinv, *gp, *wscratch;  // compute type
+  int max_views;
+  BOut* out;
+  // options
+  int max_iterations, max_invalid, jacobi, loss_type;
+  double loss_a, ftol, gtol, ptol, r0, rmax, rmin, min_rel, dmin, dmax;
+};
+
+template <typename T, int N>
+struct Shared {
+  T S[N * (N + 1) / 2];
+  T rhs[N];
+  T z[N];
+  double scale_c[N];
+  double diag_c[N];
+  double acc_c[N];  // column norms during linearisation
+  double g_c[N];
+  double red[kWarps];
+  double bcast[8];
+  int flag;
+};
+
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__device__ __forceinline__ double block_sum(double v, double* red, double* out) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kWarps; ++w) s += red[w];
+    *out = s;
+  }
+  __syncthreads();
+  return *out;
+}
+__device__ __forceinline__ double block_max(double v, double* red, double* out) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kWarps; ++w) s = fmax(s, red[w]);
+    *out = s;
+  }
+  __syncthreads();
+  return *out;
+}
+
+// Residual (FP64), corrected Jacobian blocks (compute type) of observation o.
+template <int M, typename T>
+__device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, const double* intr, const double* pts,
+                                           int64_t o, uint32_t p, double r[2], T Jc[2][6 + Model<M>::K], T Jp[2][3],
+                                           int col[6 + Model<M>::K]) {
+  constexpr int K = Model<M>::K;
+  const uint32_t c = a.cam[o], g = a.icam[o];
+  const double2 ob = a.obs[o];
+  double Ed[6], Kd[K], Xd[3];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) Ed[i] = ext[6 * (int64_t)c + i];
+#pragma unroll
+  for (int i = 0; i < K; ++i) Kd[i] = intr[K * (int64_t)g + i];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) Xd[i] = pts[3 * (int64_t)p + i];
+  T Je[2][6], Jk[2][K], Jx[2][3];
+  if constexpr (sizeof(T) == 8) {
+    residual<M, double, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (double*)nullptr);
+  } else {
+    double dJe[2][6], dJk[2][K], dJx[2][3];
+    residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    T Ef[6], Kf[K], Xf[3], rf[2];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
+#pragma unroll
+    for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
+    residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
+  }
+  double sr1;
+  const double cost = robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+  r[0] *= sr1;
+  r[1] *= sr1;
+#pragma unroll
+  for (int j = 0; j < 6; ++j) col[j] = a.ext_col[6 * (int64_t)c + j];
+#pragma unroll
+  for (int j = 0; j < K; ++j) col[6 + j] = a.intr_col[K * (int64_t)g + j];
+  const T s = (T)sr1;
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+#pragma unroll
+    for (int j = 0; j < 6; ++j) Jc[i][j] = Je[i][j] * s;
+#pragma unroll
+    for (int j = 0; j < K; ++j) Jc[i][6 + j] = Jk[i][j] * s;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Jp[i][j] = Jx[i][j] * s;
+  }
+  return cost;
+}
+
+// T: Jacobians and point blocks; SS: the shared-memory S, its factor and the step.
+template <int M, typename T, typename SS>
+__global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
+  constexpr int K = Model<M>::K;
+  constexpr int B = 6 + K;
+  constexpr int N = NMax<SS>::v;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Shared<SS, N>& sh = *reinterpret_cast<Shared<SS, N>*>(smem_raw);
+  const uint32_t pid = a.order[blockIdx.x];
+  const BProb P = a.probs[pid];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int n = (int)P.n;
+  T* Vinv = (T*)a.Vinv;
+  T* gpv = (T*)a.gp;
+  // per-warp scratch: W and W V^-1 of the warp's current point
+  T* wsc = (T*)a.wscratch + ((int64_t)blockIdx.x * kWarps + warp) * (int64_t)a.max_views * 6 * B;
+
+  auto cost_at = [&](const double* ext, const double* intr, const double* pts, bool* finite) -> double {
+    double acc = 0.0;
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      // obs of point p are [pt_off[p], pt_off[p+1])
+      for (uint32_t o = a.pt_off[p] + lane; o < a.pt_off[p + 1]; o += 32) {
+        const uint32_t c = a.cam[o], g = a.icam[o];
+        double E[6], Kp[K], X[3], r[2], dJe[2][6], dJk[2][K], dJx[2][3];
+        for (int i = 0; i < 6; ++i) E[i] = ext[6 * (int64_t)c + i];
+        for (int i = 0; i < K; ++i) Kp[i] = intr[K * (int64_t)g + i];
+        for (int i = 0; i < 3; ++i) X[i] = pts[3 * (int64_t)p + i];
+        const double2 ob = a.obs[o];
+        residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+        double sr1;
+        acc += robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+      }
+    }
+    const double c = block_sum(acc, sh.red, &sh.bcast[0]);
+    *finite = isfinite(c);
+    return c;
+  };
+
+  // gradient max norm, x norm; scale (first) and LM diagonal
+  auto linearize = [&](bool first, double* gmax, double* xnorm) {
+    for (int i = tid; i < n; i += kThreads) {
+      sh.acc_c[i] = 0.0;
+      sh.g_c[i] = 0.0;
+    }
+    __syncthreads();
+    double gm = 0.0;
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      double cp[3] = {0, 0, 0}, gp3[3] = {0, 0, 0};
+      for (uint32_t o = a.pt_off[p] + lane; o < a.pt_off[p + 1]; o += 32) {
+        double r[2];
+        T Jc[2][B], Jp[2][3];
+        int col[B];
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          if (col[j] < 0) continue;
+          const double x0 = Jc[0][j], x1 = Jc[1][j];
+          atomicAdd(&sh.acc_c[col[j]], x0 * x0 + x1 * x1);
+          atomicAdd(&sh.g_c[col[j]], x0 * r[0] + x1 * r[1]);
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const double x0 = Jp[0][j], x1 = Jp[1][j];
+          cp[j] += x0 * x0 + x1 * x1;
+          gp3[j] += x0 * r[0] + x1 * r[1];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        cp[j] = warp_sum(cp[j]);
+        gp3[j] = warp_sum(gp3[j]);
+      }
+      if (lane < 3) {
+        const double c = cp[lane];
+        if (first) a.scale_p[3 * (int64_t)p + lane] = a.jacobi ? 1.0 / (1.0 + sqrt(c)) : 1.0;
+        const double sc = a.scale_p[3 * (int64_t)p + lane];
+        a.diag_p[3 * (int64_t)p + lane] = fmin(fmax(c * sc * sc, a.dmin), a.dmax);
+        gm = fmax(gm, fabs(gp3[lane]));
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += kThreads) {
+      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(sh.acc_c[i])) : 1.0;
+      const double sc = sh.scale_c[i];
+      sh.diag_c[i] = fmin(fmax(sh.acc_c[i] * sc * sc, a.dmin), a.dmax);
+      gm = fmax(gm, fabs(sh.g_c[i]));
+    }
+    *gmax = block_max(gm, sh.red, &sh.bcast[1]);
+    double xs = 0.0;
+    for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) {
+      const int64_t j = 6 * (int64_t)P.c0 + i;
+      if (a.ext_col[j] >= 0) xs += a.ext[j] * a.ext[j];
+    }
+    for (uint32_t i = tid; i < K * P.ni; i += kThreads) {
+      const int64_t j = K * (int64_t)P.g0 + i;
+      if (a.intr_var[j / K]) xs += a.intr[j] * a.intr[j];
+    }
+    for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads) {
+      const double v = a.pts[3 * (int64_t)P.x0 + i];
+      xs += v * v;
+    }
+    *xnorm = sqrt(block_sum(xs, sh.red, &sh.bcast[2]));
+  };
+
+  bool finite = true;
+  double cost = cost_at(a.ext, a.intr, a.pts, &finite);
+  BOut res;
+  res.initial_cost = cost;
+  res.final_cost = cost;
+  res.iterations = res.successful = res.unsuccessful = 0;
+  res.status = 0;
+  if (!finite) {
+    if (tid == 0) {
+      res.termination = GBBA_FAILURE;
+      res.usable = 0;
+      res.status = GBBA_ERROR_NUMERICAL;
+      a.out[pid] = res;
+    }
+    return;
+  }
+  double gmax, xnorm;
+  linearize(true, &gmax, &xnorm);
+  int term = gmax <= a.gtol ? GBBA_CONVERGENCE : -1;
+  double radius = a.r0, decrease = 2.0;
+  int invalid = 0, iter = 0;
+  while (term < 0) {
+    if (iter >= a.max_iterations) {
+      term = GBBA_NO_CONVERGENCE;
+      break;
+    }
+    // ---- S = diag(D_c^2) + sum F'F - sum (F'E) V^-1 (E'F), rhs
+    for (int i = tid; i < n * (n + 1) / 2; i += kThreads) sh.S[i] = SS(0);
+    for (int i = tid; i < n; i += kThreads) sh.rhs[i] = SS(0);
+    if (tid == 0) sh.flag = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += kThreads) sh.S[tri(i, i)] = (SS)(sh.diag_c[i] / radius);
+    __syncthreads();
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1], m = oe - ob;
+      T v[6] = {}, g[3] = {};
+      for (uint32_t o = ob + lane; o < oe; o += 32) {
+        double r[2];
+        T Jc[2][B], Jp[2][3];
+        int col[B];
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          const T s = col[j] >= 0 ? (T)sh.scale_c[col[j]] : T(0);
+          Jc[0][j] *= s;
+          Jc[1][j] *= s;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const T s = (T)a.scale_p[3 * (int64_t)p + j];
+          Jp[0][j] *= s;
+          Jp[1][j] *= s;
+        }
+        const T r0 = (T)r[0], r1 = (T)r[1];
+        v[0] += Jp[0][0] * Jp[0][0] + Jp[1][0] * Jp[1][0];
+        v[1] += Jp[0][0] * Jp[0][1] + Jp[1][0] * Jp[1][1];
+        v[2] += Jp[0][0] * Jp[0][2] + Jp[1][0] * Jp[1][2];
+        v[3] += Jp[0][1] * Jp[0][1] + Jp[1][1] * Jp[1][1];
+        v[4] += Jp[0][1] * Jp[0][2] + Jp[1][1] * Jp[1][2];
+        v[5] += Jp[0][2] * Jp[0][2] + Jp[1][2] * Jp[1][2];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) g[j] += Jp[0][j] * r0 + Jp[1][j] * r1;
+        T* W = wsc + (int64_t)(o - ob) * 6 * B;
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j) W[i * 3 + j] = Jc[0][i] * Jp[0][j] + Jc[1][i] * Jp[1][j];
+          const int ci = col[i];
+          if (ci < 0) continue;
+          atomicAdd(&sh.rhs[ci], (SS)(Jc[0][i] * r0 + Jc[1][i] * r1));
+#pragma unroll
+          for (int j = 0; j < B; ++j) {
+            const int cj = col[j];
+            if (cj < 0 || cj > ci) continue;
+            atomicAdd(&sh.S[tri(ci, cj)], (SS)(Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j]));
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < 6; ++i) v[i] = warp_sum(v[i]);
+#pragma unroll
+      for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
+      const T a00 = v[0] + (T)(a.diag_p[3 * (int64_t)p] / radius), a11 = v[3] + (T)(a.diag_p[3 * (int64_t)p + 1] / radius),
+              a22 = v[5] + (T)(a.diag_p[3 * (int64_t)p + 2] / radius);
+      const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
+      const T d1 = a11 - l10 * l10;
+      const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
+      const T d2 = a22 - l20 * l20 - l21 * l21;
+      const T l22 = sqrt(d2);
+      const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
+      const T i10 = -l10 * i00 * i11, i21 = -l21 * i11 * i22, i20 = -(l20 * i00 + l21 * i10) * i22;
+      const T vi[6] = {i00 * i00 + i10 * i10 + i20 * i20, i10 * i11 + i20 * i21, i20 * i22,
+                       i11 * i11 + i21 * i21, i21 * i22, i22 * i22};
+      if (!(a00 > T(0)) || !(d1 > T(0)) || !(d2 > T(0)) || !isfinite((double)vi[0])) sh.flag = 2;
+      if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) gpv[3 * (int64_t)p + i] = g[i];
+      }
+      const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
+      for (uint32_t o = ob + lane; o < oe; o += 32) {
+        T* W = wsc + (int64_t)(o - ob) * 6 * B;
+        const uint32_t c = a.cam[o], gi = a.icam[o];
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          T y[3];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) y[j] = W[i * 3] * Vf[0][j] + W[i * 3 + 1] * Vf[1][j] + W[i * 3 + 2] * Vf[2][j];
+#pragma unroll
+          for (int j = 0; j < 3; ++j) W[3 * B + i * 3 + j] = y[j];
+          const int ci = i < 6 ? a.ext_col[6 * (int64_t)c + i] : a.intr_col[K * (int64_t)gi + (i - 6)];
+          if (ci >= 0) atomicAdd(&sh.rhs[ci], (SS)(-(y[0] * g[0] + y[1] * g[1] + y[2] * g[2])));
+        }
+      }
+      __syncwarp();
+      for (uint32_t x = 0; x < m; ++x) {
+        const uint32_t oa = ob + x;
+        const uint32_t ca = a.cam[oa], ga = a.icam[oa];
+        const T* Wha = wsc + (int64_t)x * 6 * B + 3 * B;
+        for (uint32_t y = 0; y < m; ++y) {
+          const uint32_t obb = ob + y;
+          const uint32_t cb = a.cam[obb], gb = a.icam[obb];
+          const T* Wb = wsc + (int64_t)y * 6 * B;
+          for (int e = lane; e < B * B; e += 32) {
+            const int i = e / B, j = e % B;
+            const int ci = i < 6 ? a.ext_col[6 * (int64_t)ca + i] : a.intr_col[K * (int64_t)ga + (i - 6)];
+            const int cj = j < 6 ? a.ext_col[6 * (int64_t)cb + j] : a.intr_col[K * (int64_t)gb + (j - 6)];
+            if (ci < 0 || cj < 0 || cj > ci) continue;
+            atomicAdd(&sh.S[tri(ci, cj)],
+                      (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
+          }
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    // ---- Cholesky of S (outer-product elimination, one barrier per column)
+    for (int j = 0; j < n; ++j) {
+      SS d = sh.S[tri(j, j)];
+      if (!(d > SS(0)) || !isfinite((double)d)) {
+        d = SS(1);
+        if (tid == 0) {
+          sh.flag = 1;
+          sh.S[tri(j, j)] = d;
+        }
+      }
+      const SS invd = SS(1) / d;
+      const int mm = n - 1 - j;
+      for (int idx = tid; idx < mm * mm; idx += kThreads) {
+        const int i = j + 1 + idx / mm, l = j + 1 + idx % mm;
+        if (l <= i) sh.S[tri(i, l)] -= sh.S[tri(i, j)] * sh.S[tri(l, j)] * invd;
+      }
+      __syncthreads();
+    }
+    for (int j = tid; j < n; j += kThreads) sh.z[j] = sqrt(sh.S[tri(j, j)]);
+    __syncthreads();
+    for (int idx = tid; idx < n * (n + 1) / 2; idx += kThreads) {
+      int i = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
+      while (tri(i + 1, 0) <= idx) ++i;
+      while (tri(i, 0) > idx) --i;
+      const int j = idx - tri(i, 0);
+      if (j < i) sh.S[idx] /= sh.z[j];
+    }
+    __syncthreads();
+    for (int j = tid; j < n; j += kThreads) sh.S[tri(j, j)] = sh.z[j];
+    __syncthreads();
+    // forward L y = rhs (column oriented), then backward L^T z = y; z holds the solution
+    for (int j = 0; j < n; ++j) {
+      const SS yj = sh.rhs[j] / sh.S[tri(j, j)];
+      for (int i = j + 1 + tid; i < n; i += kThreads) sh.rhs[i] -= sh.S[tri(i, j)] * yj;
+      __syncthreads();
+      if (tid == 0) sh.rhs[j] = yj;
+      __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      const SS xj = sh.rhs[j] / sh.S[tri(j, j)];
+      for (int i = tid; i < j; i += kThreads) sh.rhs[i] -= sh.S[tri(j, i)] * xj;
+      __syncthreads();
+      if (tid == 0) sh.z[j] = xj;
+      __syncthreads();
+    }
+    // ---- back substitution, model cost change, candidate points
+    double mcc = 0.0, stp = 0.0;
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1];
+      T t[3] = {};
+      for (uint32_t o = ob + lane; o < oe; o += 32) {
+        double r[2];
+        T Jc[2][B], Jp[2][3];
+        int col[B];
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        T fz0 = T(0), fz1 = T(0);
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          if (col[i] < 0) continue;
+          const T zi = (T)(sh.z[col[i]] * sh.scale_c[col[i]]);
+          fz0 += Jc[0][i] * zi;
+          fz1 += Jc[1][i] * zi;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const T s = (T)a.scale_p[3 * (int64_t)p + j];
+          t[j] += (Jp[0][j] * fz0 + Jp[1][j] * fz1) * s;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+      const T* vi = Vinv + 6 * (int64_t)p;
+      const T q0 = gpv[3 * (int64_t)p] - t[0], q1 = gpv[3 * (int64_t)p + 1] - t[1], q2 = gpv[3 * (int64_t)p + 2] - t[2];
+      const T y[3] = {vi[0] * q0 + vi[1] * q1 + vi[2] * q2, vi[1] * q0 + vi[3] * q1 + vi[4] * q2,
+                      vi[2] * q0 + vi[4] * q1 + vi[5] * q2};
+      if (!isfinite((double)y[0]) || !isfinite((double)y[1]) || !isfinite((double)y[2])) sh.flag = 3;
+      for (uint32_t o = ob + lane; o < oe; o += 32) {
+        double r[2];
+        T Jc[2][B], Jp[2][3];
+        int col[B];
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        double m0 = 0.0, m1 = 0.0;
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          if (col[i] < 0) continue;
+          const double zi = (double)sh.z[col[i]] * sh.scale_c[col[i]];
+          m0 += (double)Jc[0][i] * zi;
+          m1 += (double)Jc[1][i] * zi;
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const double yj = (double)y[j] * a.scale_p[3 * (int64_t)p + j];
+          m0 += (double)Jp[0][j] * yj;
+          m1 += (double)Jp[1][j] * yj;
+        }
+        m0 = -m0;
+        m1 = -m1;
+        mcc += -(m0 * (r[0] + m0 / 2.0) + m1 * (r[1] + m1 / 2.0));
+      }
+      if (lane < 3) {
+        const double d = -(double)y[lane] * a.scale_p[3 * (int64_t)p + lane];
+        a.pts2[3 * (int64_t)p + lane] = a.pts[3 * (int64_t)p + lane] + d;
+        stp += d * d;
+      }
+    }
+    for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) {
+      const int64_t j = 6 * (int64_t)P.c0 + i;
+      const int col = a.ext_col[j];
+      const double d = col >= 0 ? -(double)sh.z[col] * sh.scale_c[col] : 0.0;
+      a.ext2[j] = a.ext[j] + d;
+      stp += d * d;
+    }
+    for (uint32_t i = tid; i < K * P.ni; i += kThreads) {
+      const int64_t j = K * (int64_t)P.g0 + i;
+      const int col = a.intr_col[j];
+      const double d = col >= 0 ? -(double)sh.z[col] * sh.scale_c[col] : 0.0;
+      a.intr2[j] = a.intr[j] + d;
+      stp += d * d;
+    }
+    mcc = block_sum(mcc, sh.red, &sh.bcast[3]);
+    stp = block_sum(stp, sh.red, &sh.bcast[4]);
+    __threadfence_block();
+    bool cfinite = true;
+    const double new_cost_raw = cost_at(a.ext2, a.intr2, a.pts2, &cfinite);
+    ++iter;
+    // ---- step evaluation (TrustRegionMinimizer), identical in every thread
+    const bool solved = sh.flag == 0;
+    const bool valid = solved && isfinite(mcc) && mcc >= 0.0;
+    bool success = false;
+    double rel = 0.0;
+    if (!valid) {
+      if (++invalid >= a.max_invalid) {
+        term = GBBA_FAILURE;
+        break;
+      }
+    } else {
+      invalid = 0;
+      const double new_cost = cfinite ? new_cost_raw : 1.7976931348623157e308;
+      if (sqrt(stp) <= a.ptol * (xnorm + a.ptol)) {
+        term = GBBA_CONVERGENCE;
+        break;
+      }
+      const double change = cost - new_cost;
+      if (fabs(change) <= a.ftol * cost) {
+        term = GBBA_CONVERGENCE;
+        break;
+      }
+      rel = change / mcc;
+      success = rel > a.min_rel;
+      if (success) cost = new_cost;
+    }
+    if (success) {
+      ++res.successful;
+      const double f = 1.0 - (2.0 * rel - 1.0) * (2.0 * rel - 1.0) * (2.0 * rel - 1.0);
+      radius = fmin(a.rmax, radius / fmax(1.0 / 3.0, f));
+      decrease = 2.0;
+      for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads) a.pts[3 * (int64_t)P.x0 + i] = a.pts2[3 * (int64_t)P.x0 + i];
+      for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) a.ext[6 * (int64_t)P.c0 + i] = a.ext2[6 * (int64_t)P.c0 + i];
+      for (uint32_t i = tid; i < K * P.ni; i += kThreads) a.intr[K * (int64_t)P.g0 + i] = a.intr2[K * (int64_t)P.g0 + i];
+      __syncthreads();
+      linearize(false, &gmax, &xnorm);
+      if (gmax <= a.gtol) term = GBBA_CONVERGENCE;
+    } else {
+      ++res.unsuccessful;
+      radius /= decrease;
+      decrease *= 2.0;
+      if (radius < a.rmin) term = GBBA_CONVERGENCE;
+    }
+  }
+  if (tid == 0) {
+    res.termination = term;
+    res.usable = term != GBBA_FAILURE ? 1 : 0;
+    res.final_cost = cost;
+    res.iterations = res.successful + res.unsuccessful;
+    a.out[pid] = res;
+  }
+}
+
+}  // namespace
+
+// Host side of gbba_solve_batched.
+gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_t np_, const gbba_options* o,
+                               gbba_summary* sums) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const int model = probs[0].camera_model;
+  const int mem = probs[0].memory;
+  const int k = model == kPinholeF ? 1 : model == kRadialK3 ? 6 : 8;
+  const bool fp64 = o->precision == GBBA_PRECISION_FP64;
+  const int nmax = fp64 ? NMax<double>::v : NMax<float>::v;
+  cudaStream_t st = h->active;
+  // sizes, offsets and problem-local reduced column maps (host)
+  std::vector<BProb> bp(np_);
+  int64_t tc = 0, tg = 0, tx = 0, to = 0;
+  for (int i = 0; i < np_; ++i) {
+    const gbba_problem& P = probs[i];
+    GBBA_REQUIRE(P.camera_model == model && P.memory == mem, GBBA_ERROR_INVALID_ARGUMENT,
+                 "all problems of a batch must share the camera model and memory kind");
+    bp[i].c0 = (uint32_t)tc; bp[i].nc = (uint32_t)P.num_cameras;
+    bp[i].g0 = (uint32_t)tg; bp[i].ni = (uint32_t)P.num_intrinsics;
+    bp[i].x0 = (uint32_t)tx; bp[i].x1 = (uint32_t)(tx + P.num_points);
+    bp[i].o0 = (uint32_t)to; bp[i].o1 = (uint32_t)(to + P.num_observations);
+    tc += P.num_cameras; tg += P.num_intrinsics; tx += P.num_points; to += P.num_observations;
+  }
+  GBBA_REQUIRE(to < 0xffffffffLL && tx < 0xffffffffLL, GBBA_ERROR_TOO_LARGE, "batch too large");
+  auto host_copy = [&](void* dst, const void* src, size_t bytes) {
+    if (!bytes) return;
+    if (mem == GBBA_MEMORY_HOST) std::memcpy(dst, src, bytes);
+    else GBBA_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+  };
+  // index arrays and column maps are assembled on the host (global indices)
+  std::vector<uint32_t> cam(to), icam(to), pt(to);
+  std::vector<int32_t> ecol(6 * tc, -1), icol(k * tg, -1);
+  std::vector<uint8_t> ivar(tg, 0);
+  int max_views = 1;
+  for (int i = 0; i < np_; ++i) {
+    const gbba_problem& P = probs[i];
+    const int64_t no = P.num_observations;
+    host_copy(&cam[bp[i].o0], P.camera_index, 4 * no);
+    host_copy(&icam[bp[i].o0], P.intrinsic_index, 4 * no);
+    host_copy(&pt[bp[i].o0], P.point_index, 4 * no);
+    std::vector<uint8_t> cc(P.num_cameras, 0), ic(P.num_intrinsics, 0), cu(P.num_cameras, 0), iu(P.num_intrinsics, 0);
+    if (P.camera_constant) host_copy(cc.data(), P.camera_constant, P.num_cameras);
+    if (P.intrinsic_constant) host_copy(ic.data(), P.intrinsic_constant, P.num_intrinsics);
+    std::vector<int> views(P.num_points, 0);
+    for (int64_t q = 0; q < no; ++q) {
+      uint32_t& c = cam[bp[i].o0 + q];
+      uint32_t& g = icam[bp[i].o0 + q];
+      uint32_t& x = pt[bp[i].o0 + q];
+      GBBA_REQUIRE(c < P.num_cameras && g < P.num_intrinsics && x < P.num_points, GBBA_ERROR_INVALID_ARGUMENT,
+                   "observation index out of range");
+      cu[c] = 1;
+      iu[g] = 1;
+      max_views = std::max(max_views, ++views[x]);
+      c += bp[i].c0;
+      g += bp[i].g0;
+      x += bp[i].x0;
+    }
+    int n = 0;
+    for (int64_t c = 0; c < P.num_cameras; ++c) {
+      if (!cu[c] || cc[c]) continue;
+      for (int j = 0; j < 6; ++j)
+        if (!(P.extrinsic_fixed_mask & (1u << j))) ecol[6 * (bp[i].c0 + c) + j] = n++;
+    }
+    for (int64_t g = 0; g < P.num_intrinsics; ++g) {
+      if (!iu[g] || ic[g]) continue;
+      for (int j = 0; j < k; ++j)
+        if (!(P.intrinsic_fixed_mask & (1u << j))) {
+          icol[k * (bp[i].g0 + g) + j] = n++;
+          ivar[bp[i].g0 + g] = 1;
+        }
+    }
+    GBBA_REQUIRE(n <= nmax, GBBA_ERROR_TOO_LARGE, "a batched problem's reduced camera system exceeds the per-CTA limit");
+    bp[i].n = (uint32_t)n;
+  }
+  // problems ordered by observation count, largest first
+  std::vector<uint32_t> order(np_);
+  for (int i = 0; i < np_; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t x, uint32_t y) { return (bp[x].o1 - bp[x].o0) > (bp[y].o1 - bp[y].o0); });
+  const int B = 6 + k;
+  const size_t tsize = 8;  // FP64-sized: the mixed path ends with an FP64 polish
+  Planner pl;
+  auto plan = [&](auto& A) {
+    struct Ptrs {
+      double *ext, *intr, *pts, *ext2, *intr2, *pts2, *obs_in, *scale_p, *diag_p;
+      double2* obs;
+      uint32_t *cam, *icam, *pt, *cam_s, *icam_s, *counts, *off, *fill, *chunks, *perm, *order;
+      int32_t *ecol, *icol;
+      uint8_t* ivar;
+      BProb* probs;
+      BOut* out;
+      void *Vinv, *gp, *wsc;
+    } q;
+    q.ext = A.template take<double>(6 * tc); q.intr = A.template take<double>(k * tg); q.pts = A.template take<double>(3 * tx);
+    q.ext2 = A.template take<double>(6 * tc); q.intr2 = A.template take<double>(k * tg); q.pts2 = A.template take<double>(3 * tx);
+    q.obs_in = A.template take<double>(2 * to); q.obs = A.template take<double2>(to);
+    q.scale_p = A.template take<double>(3 * tx); q.diag_p = A.template take<double>(3 * tx);
+    q.cam = A.template take<uint32_t>(to); q.icam = A.template take<uint32_t>(to); q.pt = A.template take<uint32_t>(to);
+    q.cam_s = A.template take<uint32_t>(to); q.icam_s = A.template take<uint32_t>(to);
+    q.counts = A.template take<uint32_t>(tx + 1); q.off = A.template take<uint32_t>(tx + 1);
+    q.fill = A.template take<uint32_t>(tx + 1); q.chunks = A.template take<uint32_t>(ceil_div(tx + 1, 1024) + 1);
+    q.perm = A.template take<uint32_t>(to); q.order = A.template take<uint32_t>(np_);
+    q.ecol = A.template take<int32_t>(6 * tc); q.icol = A.template take<int32_t>(k * tg); q.ivar = A.template take<uint8_t>(tg);
+    q.probs = A.template take<BProb>(np_); q.out = A.template take<BOut>(2 * np_);
+    q.Vinv = A.template take<char>(6 * tx * tsize); q.gp = A.template take<char>(3 * tx * tsize);
+    q.wsc = A.template take<char>((size_t)np_ * kWarps * max_views * 6 * B * tsize);
+    return q;
+  };
+  plan(pl);
+  h->arena.reset();
+  h->arena.reserve(pl.used + 4096);
+  auto q = plan(h->arena);
+  // parameters and observations, packed
+  std::vector<double> hbuf;
+  auto upload_packed = [&](double* dst, int field_doubles, int64_t total, auto count_of, auto ptr_of) {
+    if (mem == GBBA_MEMORY_DEVICE) {
+      for (int i = 0; i < np_; ++i) {
+        const int64_t cnt = count_of(i) * field_doubles;
+        if (cnt) GBBA_CUDA(cudaMemcpyAsync(dst, ptr_of(i), 8 * cnt, cudaMemcpyDeviceToDevice, st));
+        dst += cnt;
+      }
+      return;
+    }
+    hbuf.resize(total * field_doubles);
+    int64_t w = 0;
+    for (int i = 0; i < np_; ++i) {
+      const int64_t cnt = count_of(i) * field_doubles;
+      std::memcpy(&hbuf[w], ptr_of(i), 8 * cnt);
+      w += cnt;
+    }
+    GBBA_CUDA(cudaMemcpyAsync(dst, hbuf.data(), 8 * w, cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+  };
+  upload_packed(q.ext, 6, tc, [&](int i) { return probs[i].num_cameras; }, [&](int i) { return (const void*)probs[i].extrinsics; });
+  upload_packed(q.intr, k, tg, [&](int i) { return probs[i].num_intrinsics; }, [&](int i) { return (const void*)probs[i].intrinsics; });
+  upload_packed(q.pts, 3, tx, [&](int i) { return probs[i].num_points; }, [&](int i) { return (const void*)probs[i].points; });
+  upload_packed(q.obs_in, 2, to, [&](int i) { return probs[i].num_observations; }, [&](int i) { return (const void*)probs[i].observations; });
+  GBBA_CUDA(cudaMemcpyAsync(q.cam, cam.data(), 4 * to, cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.icam, icam.data(), 4 * to, cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.pt, pt.data(), 4 * to, cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.ecol, ecol.data(), 4 * ecol.size(), cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.icol, icol.data(), 4 * icol.size(), cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.ivar, ivar.data(), ivar.size(), cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.probs, bp.data(), sizeof(BProb) * np_, cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemcpyAsync(q.order, order.data(), 4 * np_, cudaMemcpyHostToDevice, st));
+  // sort observations by (global) point, input order kept inside a point
+  std::vector<uint32_t> counts(tx + 1, 0);
+  for (int64_t i = 0; i < to; ++i) counts[pt[i]]++;
+  GBBA_CUDA(cudaMemcpyAsync(q.counts, counts.data(), 4 * (tx + 1), cudaMemcpyHostToDevice, st));
+  GBBA_CUDA(cudaMemsetAsync(q.fill, 0, 4 * (tx + 1), st));
+  scan_offsets(h, q.counts, q.off, tx, q.chunks, st);
+  const int grid = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(to, 1), 256), h->sm_count * 8));
+  if (to > 0) {
+    k_scatter<<<grid, 256, 0, st>>>(q.pt, to, q.off, q.fill, q.perm);
+    check_launch(h);
+    k_segment_sort<<<std::max(1, (int)std::min<int64_t>(ceil_div(tx, 256), h->sm_count * 8)), 256, 0, st>>>(q.perm, q.off, tx);
+    check_launch(h);
+  }
+  // gather
+  {
+    std::vector<uint32_t> hperm(to);
+    GBBA_CUDA(cudaMemcpyAsync(hperm.data(), q.perm, 4 * to, cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    std::vector<uint32_t> c2(to), g2(to);
+    for (int64_t i = 0; i < to; ++i) {
+      c2[i] = cam[hperm[i]];
+      g2[i] = icam[hperm[i]];
+    }
+    GBBA_CUDA(cudaMemcpyAsync(q.cam_s, c2.data(), 4 * to, cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaMemcpyAsync(q.icam_s, g2.data(), 4 * to, cudaMemcpyHostToDevice, st));
+    std::vector<double> ob(2 * to);
+    if (mem == GBBA_MEMORY_HOST) {
+      for (int64_t i = 0; i < to; ++i) {
+        ob[2 * i] = hbuf[2 * hperm[i]];
+        ob[2 * i + 1] = hbuf[2 * hperm[i] + 1];
+      }
+    } else {
+      std::vector<double> raw(2 * to);
+      GBBA_CUDA(cudaMemcpyAsync(raw.data(), q.obs_in, 16 * to, cudaMemcpyDeviceToHost, st));
+      GBBA_CUDA(cudaStreamSynchronize(st));
+      for (int64_t i = 0; i < to; ++i) {
+        ob[2 * i] = raw[2 * hperm[i]];
+        ob[2 * i + 1] = raw[2 * hperm[i] + 1];
+      }
+    }
+    GBBA_CUDA(cudaMemcpyAsync(q.obs, ob.data(), 16 * to, cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+  }
+  BArgs a;
+  a.probs = q.probs; a.order = q.order;
+  a.ext = q.ext; a.intr = q.intr; a.pts = q.pts; a.ext2 = q.ext2; a.intr2 = q.intr2; a.pts2 = q.pts2;
+  a.obs = q.obs; a.cam = q.cam_s; a.icam = q.icam_s; a.pt_off = q.off;
+  a.ext_col = q.ecol; a.intr_col = q.icol; a.intr_var = q.ivar;
+  a.scale_p = q.scale_p; a.diag_p = q.diag_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc;
+  a.max_views = max_views; a.out = q.out;
+  a.max_iterations = o->max_num_iterations; a.max_invalid = o->max_num_consecutive_invalid_steps;
+  a.jacobi = o->jacobi_scaling; a.loss_type = o->loss_type; a.loss_a = o->loss_scale;
+  a.ftol = o->function_tolerance; a.gtol = o->gradient_tolerance; a.ptol = o->parameter_tolerance;
+  a.r0 = o->initial_trust_region_radius; a.rmax = o->max_trust_region_radius; a.rmin = o->min_trust_region_radius;
+  a.min_rel = o->min_relative_decrease; a.dmin = o->min_lm_diagonal; a.dmax = o->max_lm_diagonal;
+  cudaEvent_t e0, e1;
+  GBBA_CUDA(cudaEventCreate(&e0));
+  GBBA_CUDA(cudaEventCreate(&e1));
+  GBBA_CUDA(cudaEventRecord(e0, st));
+  // Problems whose reduced system fits shared memory in FP64 keep S, its
+  // factor and the step in FP64 (the mixed path then only has FP32 Jacobians);
+  // larger windows of the mixed path keep S in FP32.  The order list holds the
+  // FP64-S problems first, each group largest first.
+  int n64 = 0;
+  {
+    std::vector<uint32_t> o64, o32;
+    for (uint32_t i : order) (bp[i].n <= (uint32_t)NMax<double>::v ? o64 : o32).push_back(i);
+    n64 = (int)o64.size();
+    o64.insert(o64.end(), o32.begin(), o32.end());
+    GBBA_CUDA(cudaMemcpyAsync(q.order, o64.data(), 4 * np_, cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+  }
+  BArgs* base = &a;
+  auto launch = [&](auto kern, size_t smem, int count, int first) {
+    if (count <= 0) return;
+    GBBA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    BArgs b = *base;
+    b.order = q.order + first;
+    b.wscratch = (char*)q.wsc + (size_t)first * kWarps * max_views * 6 * B * tsize;
+    kern<<<count, kThreads, smem, st>>>(b);
+    check_launch(h);
+  };
+  const size_t sm64 = sizeof(Shared<double, NMax<double>::v>), sm32 = sizeof(Shared<float, NMax<float>::v>);
+  if (fp64) {
+    if (model == kPinholeF) launch(k_lm_batched<kPinholeF, double, double>, sm64, n64, 0);
+    else if (model == kRadialK3) launch(k_lm_batched<kRadialK3, double, double>, sm64, n64, 0);
+    else launch(k_lm_batched<kBrownT2, double, double>, sm64, n64, 0);
+  } else {
+    if (model == kPinholeF) {
+      launch(k_lm_batched<kPinholeF, float, double>, sm64, n64, 0);
+      launch(k_lm_batched<kPinholeF, float, float>, sm32, np_ - n64, n64);
+    } else if (model == kRadialK3) {
+      launch(k_lm_batched<kRadialK3, float, double>, sm64, n64, 0);
+      launch(k_lm_batched<kRadialK3, float, float>, sm32, np_ - n64, n64);
+    } else {
+      launch(k_lm_batched<kBrownT2, float, double>, sm64, n64, 0);
+      launch(k_lm_batched<kBrownT2, float, float>, sm32, np_ - n64, n64);
+    }
+  }
+  // Mixed path: the FP64 kernel continues from the mixed solution (its own
+  // LM restart, at most 10 iterations, tolerances 1000x tighter) on the
+  // problems that fit it, so that the final iterates carry FP64 Jacobians and
+  // steps and end at the minimum rather than anywhere inside the stopping band
+  // |dcost| <= 1e-6 cost.
+  const bool polish = !fp64 && o->fp64_polish_iterations > 0;
+  BArgs pol = a;
+  if (polish) {
+    pol.out = q.out + np_;
+    pol.max_iterations = o->fp64_polish_iterations;
+    pol.ftol = a.ftol * 1e-3;  // converge past ceres's 1e-6 stopping band
+    pol.ptol = a.ptol * 1e-3;
+    base = &pol;
+    // windows whose S does not fit shared memory in FP64 polish with FP64
+    // Jacobians and an FP32 S
+    if (model == kPinholeF) {
+      launch(k_lm_batched<kPinholeF, double, double>, sm64, n64, 0);
+      launch(k_lm_batched<kPinholeF, double, float>, sm32, np_ - n64, n64);
+    } else if (model == kRadialK3) {
+      launch(k_lm_batched<kRadialK3, double, double>, sm64, n64, 0);
+      launch(k_lm_batched<kRadialK3, double, float>, sm32, np_ - n64, n64);
+    } else {
+      launch(k_lm_batched<kBrownT2, double, double>, sm64, n64, 0);
+      launch(k_lm_batched<kBrownT2, double, float>, sm32, np_ - n64, n64);
+    }
+  }
+  GBBA_CUDA(cudaEventRecord(e1, st));
+  std::vector<BOut> out(2 * np_);
+  GBBA_CUDA(cudaMemcpyAsync(out.data(), q.out, sizeof(BOut) * 2 * np_, cudaMemcpyDeviceToHost, st));
+  // write back refined parameters of the usable problems
+  std::vector<double> he(6 * tc), hi(k * tg), hx(3 * tx);
+  GBBA_CUDA(cudaMemcpyAsync(he.data(), q.ext, 8 * he.size(), cudaMemcpyDeviceToHost, st));
+  GBBA_CUDA(cudaMemcpyAsync(hi.data(), q.intr, 8 * hi.size(), cudaMemcpyDeviceToHost, st));
+  GBBA_CUDA(cudaMemcpyAsync(hx.data(), q.pts, 8 * hx.size(), cudaMemcpyDeviceToHost, st));
+  GBBA_CUDA(cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double total = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  gbba_status status = GBBA_SUCCESS;
+  for (int i = 0; i < np_; ++i) {
+    if (polish && out[np_ + i].status == 0) {
+      const BOut& f = out[np_ + i];
+      out[i].final_cost = f.final_cost;
+      out[i].iterations += f.iterations;
+      out[i].successful += f.successful;
+      out[i].unsuccessful += f.unsuccessful;
+      if (f.termination != GBBA_FAILURE) {
+        out[i].termination = f.termination;
+        out[i].usable = 1;
+      }
+    }
+    gbba_summary& s = sums[i];
+    std::memset(&s, 0, sizeof(s));
+    s.initial_cost = out[i].initial_cost;
+    s.final_cost = out[i].final_cost;
+    s.num_iterations = out[i].iterations;
+    s.num_successful_steps = out[i].successful;
+    s.num_unsuccessful_steps = out[i].unsuccessful;
+    s.termination_type = out[i].termination;
+    s.usable = out[i].usable;
+    s.reduced_system_size = bp[i].n;
+    s.total_time_s = total;
+    s.linear_solver_time_s = ms * 1e-3;  // the whole batched launch
+    if (out[i].status != 0 && status == GBBA_SUCCESS) status = (gbba_status)out[i].status;
+    if (!s.usable) continue;
+    const gbba_problem& P = probs[i];
+    auto put = [&](double* dst, const double* src, size_t count) {
+      if (!count) return;
+      if (mem == GBBA_MEMORY_HOST) std::memcpy(dst, src, 8 * count);
+      else GBBA_CUDA(cudaMemcpyAsync(dst, src, 8 * count, cudaMemcpyHostToDevice, st));
+    };
+    put(P.extrinsics, &he[6 * (int64_t)bp[i].c0], 6 * P.num_cameras);
+    put(P.intrinsics, &hi[k * (int64_t)bp[i].g0], k * P.num_intrinsics);
+    put(P.points, &hx[3 * (int64_t)bp[i].x0], 3 * P.num_points);
+  }
+  GBBA_CUDA(cudaStreamSynchronize(st));
+  return status;
+}
+
+}  // namespace gbba

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(256) k_potrf_diag(T* __restrict__ S, int64_t l
   T(*A)[NB + 1] = tile_at<T>(0);
   T(*Li)[NB + 1] = tile_at<T>(1);
   T* yb = vec_at<T>(0);
+  T* sq = vec_at<T>(1);
   const int tid = threadIdx.x;
   const int64_t off = (int64_t)kb * NB;
   for (int idx = tid; idx < NB * NB; idx += 256) {
@@ -54,40 +55,44 @@ __global__ void __launch_bounds__(256) k_potrf_diag(T* __restrict__ S, int64_t l
   }
   if (tid < NB) yb[tid] = b[off + tid];
   __syncthreads();
+  // Outer-product elimination on the lower triangle: after step j, column j
+  // holds the unscaled multipliers and A[j][j] the pivot; one barrier per step.
   for (int j = 0; j < NB; ++j) {
-    if (tid == 0) {
-      T d = A[j][j];
-      if (!(d > T(0)) || !isfinite((double)d)) {
-        atomicExch(flag, 1);
-        d = T(1);
-      }
-      A[j][j] = sqrt(d);
+    T d = A[j][j];
+    if (!(d > T(0)) || !isfinite((double)d)) {
+      if (tid == 0) atomicExch(flag, 1);
+      d = T(1);
+      if (tid == 0) A[j][j] = d;
     }
-    __syncthreads();
-    const T djj = A[j][j];
-    for (int i = j + 1 + tid; i < NB; i += 256) A[i][j] /= djj;
-    __syncthreads();
+    const T invd = T(1) / d;
     const int m = NB - 1 - j;
     for (int idx = tid; idx < m * m; idx += 256) {
       const int ii = j + 1 + idx / m, ll = j + 1 + idx % m;
-      if (ll <= ii) A[ii][ll] -= A[ii][j] * A[ll][j];
+      if (ll <= ii) A[ii][ll] -= A[ii][j] * A[ll][j] * invd;
     }
     __syncthreads();
   }
-  // L^-1 by forward substitution, one column per thread.
-  if (tid < NB) {
-    const int c = tid;
-    for (int i = 0; i < NB; ++i) {
-      if (i < c) {
-        Li[i][c] = T(0);
-        continue;
-      }
-      T s = (i == c) ? T(1) : T(0);
-      for (int j = c; j < i; ++j) s -= A[i][j] * Li[j][c];
-      Li[i][c] = s / A[i][i];
-    }
+  if (tid < NB) sq[tid] = sqrt(A[tid][tid]);
+  __syncthreads();
+  for (int idx = tid; idx < NB * NB; idx += 256) {
+    const int r = idx / NB, c = idx % NB;
+    if (c < r) A[r][c] /= sq[c];
+    else if (c == r) A[r][c] = sq[c];
   }
   __syncthreads();
+  // L^-1 row by row: Li[i][c] = (delta_ic - sum_{c<=j<i} L[i][j] Li[j][c]) / L[i][i],
+  // four threads per column c, one barrier per row.
+  {
+    const int c = tid >> 2, q = tid & 3;
+    for (int i = 0; i < NB; ++i) {
+      T s = T(0);
+      for (int j = c + q; j < i; j += 4) s += A[i][j] * Li[j][c];
+      s += __shfl_xor_sync(0xffffffffu, s, 1);
+      s += __shfl_xor_sync(0xffffffffu, s, 2);
+      if (q == 0) Li[i][c] = (c > i) ? T(0) : (((i == c) ? T(1) : T(0)) - s) / A[i][i];
+      __syncthreads();
+    }
+  }
   for (int idx = tid; idx < NB * NB; idx += 256) {
     const int r = idx / NB, c = idx % NB;
     if (c <= r) S[(off + r) * ld + off + c] = A[r][c];
@@ -214,19 +219,26 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64
   if (q == 0) b[(int64_t)jb * NB + c] -= s;
 }
 
+// Opt the kernels into their dynamic shared memory (once per process and
+// type; called before any stream capture).
+template <typename T>
+void dense_cholesky_prepare() {
+  static bool configured = false;
+  if (configured) return;
+  const int sm = (int)dense_smem_bytes<T>();
+  GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  GBBA_CUDA(cudaFuncSetAttribute(k_syrk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  configured = true;
+}
+
 // Solve S x = b in place of (S -> L, b -> y); x receives the solution.
 template <typename T>
 void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st) {
   const int nb = (int)(n_pad / NB);
   const size_t sm = dense_smem_bytes<T>();
-  static bool configured = false;  // per instantiation
-  if (!configured) {
-    GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    GBBA_CUDA(cudaFuncSetAttribute(k_syrk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    configured = true;
-  }
+  dense_cholesky_prepare<T>();
   for (int kb = 0; kb < nb; ++kb) {
     k_potrf_diag<T><<<1, 256, sm, st>>>(S, n_pad, kb, Linv_all, b, flag);
     check_launch(h);
@@ -245,6 +257,8 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
   }
 }
 
+template void dense_cholesky_prepare<double>();
+template void dense_cholesky_prepare<float>();
 template void dense_cholesky_solve<double>(gbba_handle*, double*, int64_t, double*, double*, double*, int*, cudaStream_t);
 template void dense_cholesky_solve<float>(gbba_handle*, float*, int64_t, float*, float*, float*, int*, cudaStream_t);
 

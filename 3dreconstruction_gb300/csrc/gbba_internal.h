@@ -85,6 +85,7 @@ struct gbba_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
   gbba::Arena arena;
+  gbba::Arena pair_arena;  // pair list + camera CSR of the atomic-free Schur build
   // small pinned host buffer for per-iteration scalars
   double* pinned = nullptr;
   int64_t launches = 0;

@@ -32,6 +32,8 @@
 #include <cstring>
 #include <limits>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "gbba_device.cuh"
 #include "gbba_internal.h"
 
@@ -39,6 +41,8 @@ namespace gbba {
 
 template <typename T>
 void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st);
+template <typename T>
+void dense_cholesky_prepare();
 
 static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -375,6 +379,543 @@ __global__ void __launch_bounds__(128) k_schur_point(Prob P, const double* __res
   }
 }
 
+// ---------------------------------------------------------------- atomic-free Schur build
+// Used when every free intrinsic block belongs to a single camera (per-camera
+// intrinsics, or intrinsics held): the camera-side columns of an observation
+// are then owned by its camera, so S splits into camera-pair blocks.
+//
+// Per-observation record of B' = 9B values (B = 6 + K):
+//   [ Jc (2 x B) | W = Jc^T Jp (B x 3) | W V^-1 (B x 3) | q = Jc^T r - W V^-1 g_p (B) ]
+template <int B>
+struct Rec {
+  static constexpr int kJc = 0, kW = 2 * B, kWh = 5 * B, kQ = 8 * B, kSize = 9 * B;
+};
+
+// Stage 1, one warp per point: V, V^-1, g_p and the observation records.
+template <int M, typename T>
+__global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const double* __restrict__ scale_c,
+                                                         const double* __restrict__ scale_p,
+                                                         const double* __restrict__ diag_p,
+                                                         const double* __restrict__ radius, T* __restrict__ Vinv,
+                                                         T* __restrict__ gp, T* __restrict__ rec,
+                                                         int* __restrict__ flag) {
+  constexpr int B = ObsJac<M, T>::B;
+  using R = Rec<B>;
+  const int lane = threadIdx.x & 31;
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= P.np) return;
+  const uint32_t ob = P.pt_off[p], oe = P.pt_off[p + 1];
+  T v[6] = {}, g[3] = {};
+  for (uint32_t o = ob + lane; o < oe; o += 32) {
+    ObsJac<M, T> J;
+    double cost;
+    obs_jacobian<M, T, true>(P, o, scale_c, scale_p, J, &cost);
+    const T r0 = (T)J.r[0], r1 = (T)J.r[1];
+    v[0] += J.Jp[0][0] * J.Jp[0][0] + J.Jp[1][0] * J.Jp[1][0];
+    v[1] += J.Jp[0][0] * J.Jp[0][1] + J.Jp[1][0] * J.Jp[1][1];
+    v[2] += J.Jp[0][0] * J.Jp[0][2] + J.Jp[1][0] * J.Jp[1][2];
+    v[3] += J.Jp[0][1] * J.Jp[0][1] + J.Jp[1][1] * J.Jp[1][1];
+    v[4] += J.Jp[0][1] * J.Jp[0][2] + J.Jp[1][1] * J.Jp[1][2];
+    v[5] += J.Jp[0][2] * J.Jp[0][2] + J.Jp[1][2] * J.Jp[1][2];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) g[j] += J.Jp[0][j] * r0 + J.Jp[1][j] * r1;
+    T* rc = rec + (int64_t)o * R::kSize;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      rc[R::kJc + i] = J.Jc[0][i];
+      rc[R::kJc + B + i] = J.Jc[1][i];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) rc[R::kW + i * 3 + j] = J.Jc[0][i] * J.Jp[0][j] + J.Jc[1][i] * J.Jp[1][j];
+      rc[R::kQ + i] = J.Jc[0][i] * r0 + J.Jc[1][i] * r1;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) v[i] = warp_sum(v[i]);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
+  const double rad = *radius;
+  const T a00 = v[0] + (T)(diag_p[3 * p] / rad), a11 = v[3] + (T)(diag_p[3 * p + 1] / rad),
+          a22 = v[5] + (T)(diag_p[3 * p + 2] / rad);
+  const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
+  const T d1 = a11 - l10 * l10;
+  const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
+  const T d2 = a22 - l20 * l20 - l21 * l21;
+  const T l22 = sqrt(d2);
+  const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
+  const T i10 = -l10 * i00 * i11, i21 = -l21 * i11 * i22, i20 = -(l20 * i00 + l21 * i10) * i22;
+  T vi[6];
+  vi[0] = i00 * i00 + i10 * i10 + i20 * i20;
+  vi[1] = i10 * i11 + i20 * i21;
+  vi[2] = i20 * i22;
+  vi[3] = i11 * i11 + i21 * i21;
+  vi[4] = i21 * i22;
+  vi[5] = i22 * i22;
+  if (!(a00 > T(0)) || !(d1 > T(0)) || !(d2 > T(0)) || !isfinite((double)vi[0]) || !isfinite((double)vi[3]) ||
+      !isfinite((double)vi[5])) {
+    if (lane == 0) atomicExch(flag, 2);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Vinv[6 * p + i] = vi[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) gp[3 * p + i] = g[i];
+  }
+  const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
+  for (uint32_t o = ob + lane; o < oe; o += 32) {
+    T* rc = rec + (int64_t)o * R::kSize;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const T w0 = rc[R::kW + i * 3], w1 = rc[R::kW + i * 3 + 1], w2 = rc[R::kW + i * 3 + 2];
+      T y[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) y[j] = w0 * Vf[0][j] + w1 * Vf[1][j] + w2 * Vf[2][j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) rc[R::kWh + i * 3 + j] = y[j];
+      rc[R::kQ + i] -= y[0] * g[0] + y[1] * g[1] + y[2] * g[2];
+    }
+  }
+}
+
+// Column of camera c's i-th camera-side coordinate (-1 = held).
+__device__ __forceinline__ int cam_col(const int32_t* ext_col, const int32_t* intr_col, const int32_t* cam_group, int K,
+                                       uint32_t c, int i) {
+  if (i < 6) return ext_col[6 * (int64_t)c + i];
+  const int32_t g = cam_group[c];
+  return g < 0 ? -1 : intr_col[K * (int64_t)g + (i - 6)];
+}
+
+// Stage 2, one warp per non-empty camera-pair block (ca >= cb): a segmented
+// reduction over the block's observation pairs (a, b) of
+//   U_a [a == b]  -  (W V^-1)_a  W_b^T
+// written once into S (lower triangle; entries that fall above the diagonal
+// are written transposed).  No atomics: each S entry has a single writer.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_schur_pairs(const uint32_t* __restrict__ blocks, int64_t nblocks,
+                                                     const uint32_t* __restrict__ blk_off,
+                                                     const unsigned long long* __restrict__ pairs,
+                                                     const T* __restrict__ rec, const int32_t* __restrict__ ext_col,
+                                                     const int32_t* __restrict__ intr_col,
+                                                     const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                     T* __restrict__ S, int64_t ld) {
+  using R = Rec<B>;
+  constexpr int E = (B * B + 31) / 32;
+  __shared__ T sh[4][8 * B];  // per warp: Wh_a (3B) | W_b (3B) | Jc_a (2B)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= nblocks) return;
+  const uint32_t key = blocks[w];
+  const uint32_t ca = (uint32_t)(key / nc), cb = (uint32_t)(key % nc);
+  T acc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) acc[e] = T(0);
+  T* sw = sh[warp];
+  for (uint32_t q = blk_off[key]; q < blk_off[key + 1]; ++q) {
+    const unsigned long long pr = pairs[q];
+    const uint32_t a = (uint32_t)(pr >> 32), b = (uint32_t)(pr & 0xffffffffu);
+    const T* ra = rec + (int64_t)a * R::kSize;
+    const T* rb = rec + (int64_t)b * R::kSize;
+    for (int i = lane; i < 3 * B; i += 32) {
+      sw[i] = ra[R::kWh + i];
+      sw[3 * B + i] = rb[R::kW + i];
+    }
+    const bool same = a == b;
+    if (same)
+      for (int i = lane; i < 2 * B; i += 32) sw[6 * B + i] = ra[R::kJc + i];
+    __syncwarp();
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int idx = lane + 32 * e;
+      if (idx < B * B) {
+        const int i = idx / B, j = idx % B;
+        T v = -(sw[3 * i] * sw[3 * B + 3 * j] + sw[3 * i + 1] * sw[3 * B + 3 * j + 1] + sw[3 * i + 2] * sw[3 * B + 3 * j + 2]);
+        if (same) v += sw[6 * B + i] * sw[6 * B + j] + sw[7 * B + i] * sw[7 * B + j];
+        acc[e] += v;
+      }
+    }
+    __syncwarp();
+  }
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int idx = lane + 32 * e;
+    if (idx >= B * B) continue;
+    const int i = idx / B, j = idx % B;
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, ca, i);
+    const int cj = cam_col(ext_col, intr_col, cam_group, K, cb, j);
+    if (ci < 0 || cj < 0) continue;
+    if (ca == cb && ci < cj) continue;
+    if (ci >= cj) S[(int64_t)ci * ld + cj] += acc[e];
+    else S[(int64_t)cj * ld + ci] += acc[e];
+  }
+}
+
+// Stage 3, one warp per camera: rhs of the camera's columns = sum of q over
+// the camera's observations (fixed order: the camera CSR).
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_rhs_camera(const uint32_t* __restrict__ cam_off,
+                                                    const uint32_t* __restrict__ cam_obs, const T* __restrict__ rec,
+                                                    const int32_t* __restrict__ ext_col,
+                                                    const int32_t* __restrict__ intr_col,
+                                                    const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                    T* __restrict__ rhs) {
+  using R = Rec<B>;
+  const int lane = threadIdx.x & 31;
+  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (c >= nc) return;
+  T acc[B];
+#pragma unroll
+  for (int i = 0; i < B; ++i) acc[i] = T(0);
+  for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+    const T* r = rec + (int64_t)cam_obs[q] * R::kSize + R::kQ;
+#pragma unroll
+    for (int i = 0; i < B; ++i) acc[i] += r[i];
+  }
+#pragma unroll
+  for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane < B) {
+    T v = acc[0];
+#pragma unroll
+    for (int i = 1; i < B; ++i)
+      if (lane == i) v = acc[i];
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
+    if (ci >= 0) rhs[ci] = v;
+  }
+}
+
+// ---------------------------------------------------------------- iterative Schur (PCG)
+// Implicit Schur products and a block-Jacobi preconditioner on the camera
+// blocks of S (ceres SCHUR_JACOBI, internal/ceres/schur_jacobi_preconditioner.cc;
+// implicit products as in internal/ceres/implicit_schur_complement.cc:69-110):
+//   S p = (U + D_c^2) p - sum_o W_o V_p(o)^-1 W_o^T p
+// The operator data (W, V^-1, U) are in the compute type T, the PCG vectors
+// and every accumulation are FP64.
+
+// Camera diagonal blocks U_c = sum Jc^T Jc, the preconditioner block
+// (U_c + D_c^2 - sum (W V^-1) W^T)^-1 (identity on held coordinates); one warp per camera.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__ cam_off,
+                                                    const uint32_t* __restrict__ cam_obs, const T* __restrict__ rec,
+                                                    const int32_t* __restrict__ ext_col,
+                                                    const int32_t* __restrict__ intr_col,
+                                                    const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                    const double* __restrict__ diag_c, const double* __restrict__ radius,
+                                                    T* __restrict__ U, double* __restrict__ Minv, int* __restrict__ flag) {
+  using R = Rec<B>;
+  constexpr int E = (B * B + 31) / 32;
+  __shared__ double sm[4][B * B];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (c >= nc) return;
+  double accU[E], accS[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) accU[e] = accS[e] = 0.0;
+  for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
+    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int idx = lane + 32 * e;
+      if (idx < B * B) {
+        const int i = idx / B, j = idx % B;
+        const double u = (double)r[R::kJc + i] * r[R::kJc + j] + (double)r[R::kJc + B + i] * r[R::kJc + B + j];
+        const double w = (double)r[R::kWh + 3 * i] * r[R::kW + 3 * j] + (double)r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
+                         (double)r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
+        accU[e] += u;
+        accS[e] += u - w;
+      }
+    }
+  }
+  const double rad = *radius;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int idx = lane + 32 * e;
+    if (idx >= B * B) continue;
+    const int i = idx / B, j = idx % B;
+    U[c * B * B + idx] = (T)accU[e];
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, i);
+    const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
+    double v = accS[e];
+    if (i == j && ci >= 0) v += diag_c[ci] / rad;
+    if (ci < 0 || cj < 0) v = (i == j) ? 1.0 : 0.0;
+    sm[warp][idx] = v;
+  }
+  __syncwarp();
+  if (lane == 0) {
+    double* A = sm[warp];
+    bool ok = true;
+    for (int j = 0; j < B && ok; ++j) {  // Cholesky, lower, in place
+      double d = A[j * B + j];
+      for (int t = 0; t < j; ++t) d -= A[j * B + t] * A[j * B + t];
+      if (!(d > 0.0)) {
+        ok = false;
+        break;
+      }
+      d = sqrt(d);
+      A[j * B + j] = d;
+      for (int i = j + 1; i < B; ++i) {
+        double v = A[i * B + j];
+        for (int t = 0; t < j; ++t) v -= A[i * B + t] * A[j * B + t];
+        A[i * B + j] = v / d;
+      }
+    }
+    if (!ok) atomicExch(flag, 4);
+    double* Mi = Minv + c * B * B;
+    for (int col = 0; col < B; ++col) {  // columns of the inverse by two triangular solves
+      double y[B];
+      for (int i = 0; i < B; ++i) {
+        double v = (i == col) ? 1.0 : 0.0;
+        for (int t = 0; t < i; ++t) v -= A[i * B + t] * y[t];
+        y[i] = ok ? v / A[i * B + i] : 0.0;
+      }
+      for (int i = B - 1; i >= 0; --i) {
+        double v = y[i];
+        for (int t = i + 1; t < B; ++t) v -= A[t * B + i] * y[t];
+        y[i] = ok ? v / A[i * B + i] : 0.0;
+      }
+      for (int i = 0; i < B; ++i) Mi[i * B + col] = y[i];
+    }
+  }
+}
+
+// y_p = V_p^-1 sum_{o in p} W_o^T x_c(o); one warp per point.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ cam,
+                                                    const T* __restrict__ rec, const T* __restrict__ Vinv,
+                                                    const int32_t* __restrict__ ext_col,
+                                                    const int32_t* __restrict__ intr_col,
+                                                    const int32_t* __restrict__ cam_group, int K, int64_t np,
+                                                    const double* __restrict__ x, double* __restrict__ y) {
+  using R = Rec<B>;
+  const int lane = threadIdx.x & 31;
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (p >= np) return;
+  double t[3] = {0.0, 0.0, 0.0};
+  for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
+    const T* r = rec + (int64_t)o * R::kSize;
+    const uint32_t c = cam[o];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
+      if (ci < 0) continue;
+      const double xi = x[ci];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[j] += (double)r[R::kW + 3 * i + j] * xi;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+  if (lane < 3) {
+    const T* v = Vinv + 6 * p;
+    const double row[3][3] = {{(double)v[0], (double)v[1], (double)v[2]},
+                              {(double)v[1], (double)v[3], (double)v[4]},
+                              {(double)v[2], (double)v[4], (double)v[5]}};
+    y[3 * p + lane] = row[lane][0] * t[0] + row[lane][1] * t[1] + row[lane][2] * t[2];
+  }
+}
+
+// out_c = (U_c + D_c^2) x_c - sum_{o in c} W_o y_p(o); one warp per camera.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_spmv_camera(const uint32_t* __restrict__ cam_off,
+                                                     const uint32_t* __restrict__ cam_obs,
+                                                     const uint32_t* __restrict__ pt, const T* __restrict__ rec,
+                                                     const T* __restrict__ U, const int32_t* __restrict__ ext_col,
+                                                     const int32_t* __restrict__ intr_col,
+                                                     const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                     const double* __restrict__ diag_c,
+                                                     const double* __restrict__ radius, const double* __restrict__ x,
+                                                     const double* __restrict__ y, double* __restrict__ out) {
+  using R = Rec<B>;
+  const int lane = threadIdx.x & 31;
+  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (c >= nc) return;
+  double acc[B];
+#pragma unroll
+  for (int i = 0; i < B; ++i) acc[i] = 0.0;
+  for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+    const uint32_t o = cam_obs[q];
+    const T* r = rec + (int64_t)o * R::kSize;
+    const double* yp = y + 3 * (int64_t)pt[o];
+    const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
+#pragma unroll
+    for (int i = 0; i < B; ++i)
+      acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
+  }
+#pragma unroll
+  for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane < B) {
+    double v = acc[0];
+#pragma unroll
+    for (int i = 1; i < B; ++i)
+      if (lane == i) v = acc[i];
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
+    if (ci >= 0) {
+      double u = diag_c[ci] / *radius * x[ci];
+      for (int j = 0; j < B; ++j) {
+        const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
+        if (cj >= 0) u += (double)U[c * B * B + lane * B + j] * x[cj];
+      }
+      out[ci] = v + u;
+    }
+  }
+}
+
+// z_c = Minv_c r_c, one thread per camera.
+template <int B>
+__global__ void k_precond(const double* __restrict__ Minv, const int32_t* __restrict__ ext_col,
+                          const int32_t* __restrict__ intr_col, const int32_t* __restrict__ cam_group, int K,
+                          int64_t nc, const double* __restrict__ r, double* __restrict__ z) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    int col[B];
+    double rv[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      col[i] = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, i);
+      rv[i] = col[i] >= 0 ? r[col[i]] : 0.0;
+    }
+    const double* Mi = Minv + c * B * B;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      if (col[i] < 0) continue;
+      double v = 0.0;
+#pragma unroll
+      for (int j = 0; j < B; ++j) v += Mi[i * B + j] * rv[j];
+      z[col[i]] = v;
+    }
+  }
+}
+
+// Two dot products with per-block partials: part[b] = a1.b1, part[nb + b] = a2.b2.
+__global__ void k_dot2(const double* a1, const double* b1, const double* a2, const double* b2, int64_t n, double* part) {
+  __shared__ double sh[2][8];
+  double s1 = 0.0, s2 = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    s1 += a1[i] * b1[i];
+    if (a2) s2 += a2[i] * b2[i];
+  }
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
+  if ((threadIdx.x & 31) == 0) {
+    sh[0][threadIdx.x >> 5] = s1;
+    sh[1][threadIdx.x >> 5] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0.0, t2 = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      t1 += sh[0][w];
+      t2 += sh[1][w];
+    }
+    part[blockIdx.x] = t1;
+    part[gridDim.x + blockIdx.x] = t2;
+  }
+}
+
+// p = z + beta p
+__global__ void k_axpby(double* p, const double* z, double beta, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+// x += alpha p; r = reset ? b - q : r - alpha q  (q holds S x when reset)
+__global__ void k_update_xr(double* x, double* r, const double* p, const double* q, const double* b, double alpha,
+                            int reset, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    if (!reset) r[i] -= alpha * q[i];
+  }
+}
+__global__ void k_sub(double* r, const double* b, const double* q, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    r[i] = b[i] - q[i];
+}
+// t[i] = b[i] + r[i]  (for Q = -x.(b + r))
+__global__ void k_add(double* t, const double* b, const double* r, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    t[i] = b[i] + r[i];
+}
+template <typename T, typename U2>
+__global__ void k_convert(const T* a, U2* b, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (U2)a[i];
+}
+
+// ---------------------------------------------------------------- pair-list setup kernels
+// Per point: number of ordered observation pairs (a, b) with cam(a) >= cam(b).
+__global__ void k_pair_count(const uint32_t* pt_off, const uint32_t* cam, int64_t np, uint32_t* cnt) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t n = 0;
+    for (uint32_t a = pt_off[p]; a < pt_off[p + 1]; ++a)
+      for (uint32_t b = pt_off[p]; b < pt_off[p + 1]; ++b) n += cam[a] >= cam[b];
+    cnt[p] = n;
+  }
+}
+__global__ void k_pair_write(const uint32_t* pt_off, const uint32_t* cam, int64_t np, int64_t nc, const uint32_t* pair_off,
+                             unsigned long long* pairs, uint32_t* keys, uint32_t* hist) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t w = pair_off[p];
+    for (uint32_t a = pt_off[p]; a < pt_off[p + 1]; ++a)
+      for (uint32_t b = pt_off[p]; b < pt_off[p + 1]; ++b)
+        if (cam[a] >= cam[b]) {
+          const uint32_t key = (uint32_t)(cam[a] * (uint64_t)nc + cam[b]);
+          pairs[w] = ((unsigned long long)a << 32) | b;
+          keys[w] = key;
+          atomicAdd(&hist[key], 1u);
+          ++w;
+        }
+  }
+}
+__global__ void k_bucket_scatter64(const unsigned long long* in, const uint32_t* keys, int64_t n, const uint32_t* off,
+                                   uint32_t* fill, unsigned long long* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t k = keys[i];
+    out[off[k] + atomicAdd(&fill[k], 1u)] = in[i];
+  }
+}
+__global__ void k_segment_sort64(unsigned long long* v, const uint32_t* off, int64_t nseg) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < nseg; s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = off[s], e = off[s + 1];
+    for (uint32_t i = b + 1; i < e; ++i) {
+      const unsigned long long x = v[i];
+      uint32_t j = i;
+      while (j > b && v[j - 1] > x) {
+        v[j] = v[j - 1];
+        --j;
+      }
+      v[j] = x;
+    }
+  }
+}
+__global__ void k_nonempty(const uint32_t* off, int64_t nkeys, uint32_t* list, uint32_t* count) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nkeys; k += (int64_t)gridDim.x * blockDim.x)
+    if (off[k + 1] > off[k]) list[atomicAdd(count, 1u)] = (uint32_t)k;
+}
+__global__ void k_iota(uint32_t* v, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v[i] = (uint32_t)i;
+}
+static int key_bits(uint64_t max_key) {
+  int b = 1;
+  while (b < 32 && (1ull << b) <= max_key) ++b;
+  return b;
+}
+// Camera -> intrinsic group map and the "free intrinsic blocks are private" check.
+__global__ void k_cam_groups(const uint32_t* cam, const uint32_t* icam, int64_t no, const uint8_t* intr_var,
+                             int32_t* cam_group, uint32_t* group_cam, int* conflict, uint32_t* cam_hist) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < no; o += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cam[o], g = icam[o];
+    const int32_t prev = atomicCAS(&cam_group[c], -1, (int32_t)g);
+    if (prev != -1 && prev != (int32_t)g) atomicExch(conflict, 1);
+    if (intr_var[g]) {
+      const uint32_t pc = atomicCAS(&group_cam[g], 0xffffffffu, c);
+      if (pc != 0xffffffffu && pc != c) atomicExch(conflict, 1);
+    }
+    atomicAdd(&cam_hist[c], 1u);
+  }
+}
+__global__ void k_cam_scatter(const uint32_t* cam, int64_t no, const uint32_t* off, uint32_t* fill, uint32_t* out) {
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < no; o += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t c = cam[o];
+    out[off[c] + atomicAdd(&fill[c], 1u)] = (uint32_t)o;
+  }
+}
+
 // Back substitution (one warp per point) + model cost change + candidate points.
 //   y_p = V^-1 (g_p - sum E'F z), step = -(z, y), m = J step,
 //   model_cost_change += -m.(r + m/2)
@@ -588,6 +1129,19 @@ struct Solve {
   void *S, *rhs, *zsol, *Linv, *Vinv, *gpv, *Wbuf, *What;
   double *part_mcc, *part_step_p, *part_step_c, *part_cost, *part_x, *scalars;
   int nb_obs, nb_pt, nb_cam, nb_x;
+  // atomic-free Schur build (pair list in the handle's pair arena)
+  bool pair_path = false;
+  int64_t n_blocks = 0;
+  uint32_t *blocks = nullptr, *blk_off = nullptr, *cam_off = nullptr, *cam_obs = nullptr;
+  unsigned long long* pairs = nullptr;
+  int32_t* cam_group = nullptr;
+  void* rec = nullptr;
+  bool dense = true;
+  // iterative Schur (PCG) state
+  double *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr, *pcg_b = nullptr;
+  double *pcg_y = nullptr, *pcg_minv = nullptr, *pcg_part = nullptr;
+  void* pcg_u = nullptr;
+  int nb_pcg = 0;
 };
 
 static Prob make_prob(const Solve& s, const double* ext, const double* intr, const double* pts, const gbba_options* o) {
@@ -640,14 +1194,13 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.gmax_bits = a.template take<unsigned long long>(1);
   s.flag = a.template take<int>(1);
   s.nonfinite = a.template take<int>(1);
-  s.S = a.template take<char>((size_t)s.n_pad * s.n_pad * tsize);
+  const int64_t n_s = s.dense ? s.n_pad : 0;
+  s.S = a.template take<char>((size_t)n_s * n_s * tsize);
   s.rhs = a.template take<char>((size_t)s.n_pad * tsize);
   s.zsol = a.template take<char>((size_t)s.n_pad * tsize);
-  s.Linv = a.template take<char>((size_t)s.n_pad * 64 * tsize);
+  s.Linv = a.template take<char>((size_t)n_s * 64 * tsize);
   s.Vinv = a.template take<char>((size_t)s.np * 6 * tsize);
   s.gpv = a.template take<char>((size_t)s.np * 3 * tsize);
-  s.Wbuf = a.template take<char>((size_t)s.no * (6 + s.k) * 3 * tsize);
-  s.What = a.template take<char>((size_t)s.no * (6 + s.k) * 3 * tsize);
   s.part_mcc = a.template take<double>(s.nb_pt);
   s.part_step_p = a.template take<double>(s.nb_pt);
   s.part_step_c = a.template take<double>(s.nb_cam);
@@ -656,7 +1209,7 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.scalars = a.template take<double>(8);
 }
 
-static void scan_offsets(gbba_handle* h, const uint32_t* counts, uint32_t* off, int64_t n, uint32_t* tmp_chunks,
+void scan_offsets(gbba_handle* h, const uint32_t* counts, uint32_t* off, int64_t n, uint32_t* tmp_chunks,
                          cudaStream_t st) {
   const int64_t nchunks = ceil_div(n, 1024);
   k_scan_chunks<<<(unsigned)nchunks, 1024, 0, st>>>(counts, off, tmp_chunks, n);
@@ -672,6 +1225,9 @@ static void copy_in(void* dst, const void* src, size_t bytes, int memory, cudaSt
   if (bytes == 0) return;
   GBBA_CUDA(cudaMemcpyAsync(dst, src, bytes, memory == GBBA_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
 }
+
+static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize);
+static void setup_atomic_path(gbba_handle* h, Solve& s, size_t tsize);
 
 static void copy_to_host(void* dst, const void* src, size_t bytes, int memory) {
   if (bytes == 0) return;
@@ -711,9 +1267,8 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   for (int64_t g = 0; g < ni; ++g) n_max += ic[g] ? 0 : free_i;
   s.n_red = n_max;
   s.n_pad = ceil_div(std::max<int64_t>(n_max, 1), 64) * 64;
-  const bool dense = o->linear_solver == GBBA_SOLVER_DENSE_SCHUR ||
-                     (o->linear_solver == GBBA_SOLVER_AUTO && s.n_pad <= (int64_t)o->dense_schur_max_size + 64);
-  GBBA_REQUIRE(dense, GBBA_ERROR_NOT_SUPPORTED, "iterative Schur solver selected but not built for this call");
+  s.dense = o->linear_solver == GBBA_SOLVER_DENSE_SCHUR ||
+            (o->linear_solver == GBBA_SOLVER_AUTO && s.n_pad <= (int64_t)o->dense_schur_max_size + 64);
   s.nb_obs = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(no, 1), 256), h->sm_count * 8));
   s.nb_pt = (int)std::max<int64_t>(1, ceil_div(np * 32, 128));
   s.nb_cam = 64;
@@ -798,8 +1353,290 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   GBBA_CUDA(cudaMemcpyAsync(s.intr_col, icol.data(), sizeof(int32_t) * icol.size(), cudaMemcpyHostToDevice, st));
   GBBA_CUDA(cudaMemcpyAsync(s.intr_var, ivar.data(), ni, cudaMemcpyHostToDevice, st));
   GBBA_CUDA(cudaStreamSynchronize(st));  // the host vectors above go out of scope
+  setup_pairs(h, s, tsize);
 }
 
+
+// Pair list and camera CSR of the atomic-free Schur build.  Applies when the
+// dense solver is used, every free intrinsic block is private to one camera
+// and every camera uses one intrinsic group; otherwise the point-major kernel
+// with atomics is used.
+static void setup_atomic_path(gbba_handle* h, Solve& s, size_t tsize) {
+  GBBA_REQUIRE(s.dense, GBBA_ERROR_NOT_SUPPORTED,
+               "the iterative Schur solver needs every free intrinsic block to belong to one camera");
+  s.pair_path = false;
+  Arena& A = h->pair_arena;
+  const size_t w = (size_t)s.no * (6 + s.k) * 3 * tsize;
+  A.reset();
+  A.reserve(2 * (w + 256) + 4096);
+  s.Wbuf = A.take<char>(w);
+  s.What = A.take<char>(w);
+}
+
+static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
+  s.pair_path = false;
+  const int64_t nc = s.nc, ni = s.ni, np = s.np, no = s.no;
+  const bool want_pairs = s.dense;
+  if ((std::getenv("GBBA_NO_PAIR_PATH") && s.dense) || nc > 0x7fffffffLL || no > 0x7fffffffLL ||
+      (want_pairs && (nc > 8192 || nc * nc > (int64_t)1 << 26))) {
+    setup_atomic_path(h, s, tsize);
+    return;
+  }
+  cudaStream_t st = s.st;
+  const int64_t nk = want_pairs ? nc * nc : 0;
+  const int64_t n_pcg = s.dense ? 0 : s.n_pad;
+  const int B = 6 + s.k;
+  size_t phase2_guess = 0;
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    Arena& A = h->pair_arena;
+    Planner p1;
+    p1.take<int32_t>(nc);
+    p1.take<uint32_t>(ni);
+    p1.take<int>(2);
+    p1.take<uint32_t>(nc + 1);
+    p1.take<uint32_t>(nc + 1);
+    p1.take<uint32_t>(nc + 1);
+    p1.take<uint32_t>(no);
+    p1.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
+    p1.take<uint32_t>(np + 1);
+    p1.take<uint32_t>(np + 1);
+    p1.take<char>((size_t)no * 9 * B * tsize);
+    // PCG vectors (x, r, z, p, q, b), point temporaries, camera blocks
+    p1.take<double>(6 * n_pcg);
+    p1.take<double>(3 * np);
+    p1.take<double>((size_t)nc * B * B);
+    p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
+    p1.take<double>(4096);
+    size_t cam_sort_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, cam_sort_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)no, 0, key_bits(nc));
+    p1.take<uint32_t>(no);  // sorted camera keys
+    p1.take<uint32_t>(no);  // iota
+    p1.take<char>(cam_sort_bytes);
+    A.reset();
+    A.reserve(p1.used + phase2_guess + 4096);
+    s.cam_group = A.take<int32_t>(nc);
+    uint32_t* group_cam = A.take<uint32_t>(ni);
+    int* conflict = A.take<int>(2);
+    uint32_t* cam_hist = A.take<uint32_t>(nc + 1);
+    s.cam_off = A.take<uint32_t>(nc + 1);
+    uint32_t* cam_fill = A.take<uint32_t>(nc + 1);
+    s.cam_obs = A.take<uint32_t>(no);
+    uint32_t* chunks = A.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
+    uint32_t* pcnt = A.take<uint32_t>(np + 1);
+    uint32_t* pair_off = A.take<uint32_t>(np + 1);
+    s.rec = A.take<char>((size_t)no * 9 * B * tsize);
+    s.pcg_x = A.take<double>(n_pcg);
+    s.pcg_r = A.take<double>(n_pcg);
+    s.pcg_z = A.take<double>(n_pcg);
+    s.pcg_p = A.take<double>(n_pcg);
+    s.pcg_q = A.take<double>(n_pcg);
+    s.pcg_b = A.take<double>(n_pcg);
+    s.pcg_y = A.take<double>(3 * np);
+    s.pcg_minv = A.take<double>((size_t)nc * B * B);
+    s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
+    s.pcg_part = A.take<double>(4096);
+    s.nb_pcg = 256;
+    uint32_t* cam_keys = A.take<uint32_t>(no);
+    uint32_t* iota = A.take<uint32_t>(no);
+    void* cam_sort_tmp = A.take<char>(cam_sort_bytes);
+    GBBA_CUDA(cudaMemsetAsync(s.cam_group, 0xff, sizeof(int32_t) * nc, st));
+    GBBA_CUDA(cudaMemsetAsync(group_cam, 0xff, sizeof(uint32_t) * ni, st));
+    GBBA_CUDA(cudaMemsetAsync(conflict, 0, sizeof(int) * 2, st));
+    GBBA_CUDA(cudaMemsetAsync(cam_hist, 0, sizeof(uint32_t) * (nc + 1), st));
+    GBBA_CUDA(cudaMemsetAsync(cam_fill, 0, sizeof(uint32_t) * (nc + 1), st));
+    const int grid = s.nb_obs;
+    k_cam_groups<<<grid, 256, 0, st>>>(s.cam, s.icam, no, s.intr_var, s.cam_group, group_cam, conflict, cam_hist);
+    check_launch(h);
+    k_pair_count<<<std::max(1, (int)std::min<int64_t>(ceil_div(np, 128), h->sm_count * 16)), 128, 0, st>>>(s.pt_off, s.cam, np, pcnt);
+    check_launch(h);
+    scan_offsets(h, pcnt, pair_off, np, chunks, st);
+    int hconf = 0;
+    uint32_t total = 0;
+    GBBA_CUDA(cudaMemcpyAsync(&hconf, conflict, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaMemcpyAsync(&total, pair_off + np, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    if (hconf) {
+      setup_atomic_path(h, s, tsize);
+      return;
+    }
+    Planner p2;
+    if (!want_pairs) total = 0;
+    size_t pair_sort_bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, pair_sort_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (const unsigned long long*)nullptr, (unsigned long long*)nullptr, (int)total, 0,
+                                    key_bits(nk));
+    p2.take<char>(pair_sort_bytes);
+    p2.take<uint32_t>(total);
+    p2.take<unsigned long long>(total);
+    p2.take<uint32_t>(total);
+    p2.take<uint32_t>(nk + 1);
+    p2.take<uint32_t>(nk + 1);
+    p2.take<uint32_t>(nk + 1);
+    p2.take<unsigned long long>(total);
+    p2.take<uint32_t>(nk);
+    p2.take<uint32_t>(1);
+    if (A.used + p2.used + 4096 > A.capacity) {  // grow and redo phase 1
+      phase2_guess = p2.used;
+      A.release();
+      continue;
+    }
+    // camera CSR: observation lists per camera in ascending (point) order, by a
+    // stable radix sort of the observations on their camera
+    scan_offsets(h, cam_hist, s.cam_off, nc, chunks, st);
+    k_iota<<<grid, 256, 0, st>>>(iota, no);
+    check_launch(h);
+    {
+      size_t bytes = cam_sort_bytes;
+      GBBA_CUDA(cub::DeviceRadixSort::SortPairs(cam_sort_tmp, bytes, s.cam, cam_keys, iota, s.cam_obs, (int)no, 0,
+                                                key_bits(nc), st));
+      count_launch(h, 4);
+    }
+    if (!want_pairs) {
+      s.pair_path = true;
+      s.n_blocks = 0;
+      return;
+    }
+    // pair list bucketed by camera pair
+    unsigned long long* tmp = A.take<unsigned long long>(total);
+    uint32_t* keys = A.take<uint32_t>(total);
+    uint32_t* hist = A.take<uint32_t>(nk + 1);
+    s.blk_off = A.take<uint32_t>(nk + 1);
+    uint32_t* fill = A.take<uint32_t>(nk + 1);
+    s.pairs = A.take<unsigned long long>(total);
+    s.blocks = A.take<uint32_t>(nk);
+    uint32_t* count = A.take<uint32_t>(1);
+    GBBA_CUDA(cudaMemsetAsync(hist, 0, sizeof(uint32_t) * (nk + 1), st));
+    GBBA_CUDA(cudaMemsetAsync(fill, 0, sizeof(uint32_t) * (nk + 1), st));
+    GBBA_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), st));
+    void* pair_sort_tmp = A.take<char>(pair_sort_bytes);
+    uint32_t* keys_sorted = A.take<uint32_t>(total);
+    k_pair_write<<<std::max(1, (int)std::min<int64_t>(ceil_div(np, 128), h->sm_count * 16)), 128, 0, st>>>(
+        s.pt_off, s.cam, np, nc, pair_off, tmp, keys, hist);
+    check_launch(h);
+    scan_offsets(h, hist, s.blk_off, nk, chunks, st);
+    if (total > 0) {  // stable: pairs stay in generation (point) order inside a block
+      size_t bytes = pair_sort_bytes;
+      GBBA_CUDA(cub::DeviceRadixSort::SortPairs(pair_sort_tmp, bytes, keys, keys_sorted, tmp, s.pairs, (int)total, 0,
+                                                key_bits(nk), st));
+      count_launch(h, 4);
+    }
+    k_nonempty<<<std::max(1, (int)std::min<int64_t>(ceil_div(nk, 256), h->sm_count * 8)), 256, 0, st>>>(s.blk_off, nk, s.blocks, count);
+    check_launch(h);
+    uint32_t hcount = 0;
+    GBBA_CUDA(cudaMemcpyAsync(&hcount, count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    s.n_blocks = hcount;
+    s.pair_path = true;
+    return;
+  }
+}
+
+// Restatement of ceres ConjugateGradientsSolver::Solve (internal/ceres/
+// conjugate_gradients_solver.cc:66-248) on the implicit Schur complement with
+// the block-Jacobi preconditioner: residual reset every 10 iterations (the
+// reset recomputes b - S x with FP64 accumulation), termination on the
+// q-tolerance zeta < eta; r_tolerance is disabled as in the LM strategy.
+template <int M, typename T>
+static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
+  gbba_handle* h = s.h;
+  cudaStream_t st = s.st;
+  constexpr int B = 6 + Model<M>::K;
+  const int64_t n = s.n_red;
+  const int nbv = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), s.nb_pcg));
+  const int gv = nbv;
+  std::vector<double> hp(2 * nbv);
+  auto dot2 = [&](const double* a1, const double* b1, const double* a2, const double* b2, double* d1, double* d2) {
+    k_dot2<<<nbv, 256, 0, st>>>(a1, b1, a2, b2, n, s.pcg_part);
+    check_launch(h);
+    GBBA_CUDA(cudaMemcpyAsync(hp.data(), s.pcg_part, sizeof(double) * 2 * nbv, cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    double t1 = 0.0, t2 = 0.0;
+    for (int i = 0; i < nbv; ++i) {
+      t1 += hp[i];
+      t2 += hp[nbv + i];
+    }
+    *d1 = t1;
+    if (d2) *d2 = t2;
+  };
+  auto spmv = [&](const double* x, double* out) {
+    if (s.np > 0) {
+      k_spmv_point<B, T><<<(unsigned)ceil_div(s.np * 32, 128), 128, 0, st>>>(
+          s.pt_off, s.cam, (const T*)s.rec, (const T*)s.Vinv, s.ext_col, s.intr_col, s.cam_group, s.k, s.np, x, s.pcg_y);
+      check_launch(h);
+    }
+    k_spmv_camera<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
+        s.cam_off, s.cam_obs, s.pt, (const T*)s.rec, (const T*)s.pcg_u, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc,
+        s.diag_c, s.radius, x, s.pcg_y, out);
+    check_launch(h);
+  };
+  T* zsol = (T*)s.zsol;
+  k_convert<T, double><<<gv, 256, 0, st>>>((const T*)s.rhs, s.pcg_b, n);
+  check_launch(h);
+  GBBA_CUDA(cudaMemsetAsync(s.pcg_x, 0, sizeof(double) * n, st));
+  double bb = 0.0;
+  dot2(s.pcg_b, s.pcg_b, nullptr, nullptr, &bb, nullptr);
+  if (!(bb > 0.0)) {
+    GBBA_CUDA(cudaMemsetAsync(zsol, 0, sizeof(T) * s.n_pad, st));
+    return;
+  }
+  GBBA_CUDA(cudaMemcpyAsync(s.pcg_r, s.pcg_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+  double rho = 1.0, Q0 = 0.0;
+  bool failure = false;
+  int it = 1;
+  for (;; ++it) {
+    k_precond<B><<<(unsigned)std::max<int64_t>(1, ceil_div(s.nc, 128)), 128, 0, st>>>(
+        s.pcg_minv, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.pcg_r, s.pcg_z);
+    check_launch(h);
+    const double last_rho = rho;
+    dot2(s.pcg_r, s.pcg_z, nullptr, nullptr, &rho, nullptr);
+    if (rho == 0.0 || std::isinf(rho) || std::isnan(rho)) {
+      failure = true;
+      break;
+    }
+    if (it == 1) {
+      GBBA_CUDA(cudaMemcpyAsync(s.pcg_p, s.pcg_z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    } else {
+      const double beta = rho / last_rho;
+      if (beta == 0.0 || std::isinf(beta) || std::isnan(beta)) {
+        failure = true;
+        break;
+      }
+      k_axpby<<<gv, 256, 0, st>>>(s.pcg_p, s.pcg_z, beta, n);
+      check_launch(h);
+    }
+    spmv(s.pcg_p, s.pcg_q);
+    double pq = 0.0;
+    dot2(s.pcg_p, s.pcg_q, nullptr, nullptr, &pq, nullptr);
+    if (pq <= 0.0 || std::isinf(pq) || std::isnan(pq)) break;  // no further progress
+    const double alpha = rho / pq;
+    if (std::isinf(alpha)) {
+      failure = true;
+      break;
+    }
+    const int reset = (it % 10 == 0) ? 1 : 0;
+    k_update_xr<<<gv, 256, 0, st>>>(s.pcg_x, s.pcg_r, s.pcg_p, s.pcg_q, s.pcg_b, alpha, reset, n);
+    check_launch(h);
+    if (reset) {
+      spmv(s.pcg_x, s.pcg_q);
+      k_sub<<<gv, 256, 0, st>>>(s.pcg_r, s.pcg_b, s.pcg_q, n);
+      check_launch(h);
+    }
+    k_add<<<gv, 256, 0, st>>>(s.pcg_z, s.pcg_b, s.pcg_r, n);
+    check_launch(h);
+    double xq = 0.0;
+    dot2(s.pcg_x, s.pcg_z, nullptr, nullptr, &xq, nullptr);
+    const double Q1 = -xq;
+    const double zeta = it * (Q1 - Q0) / Q1;
+    if (zeta < o->eta) break;
+    Q0 = Q1;
+    if (it >= o->max_linear_solver_iterations) break;
+  }
+  sum->linear_solver_iterations += it;
+  if (failure) GBBA_CUDA(cudaMemsetAsync(s.flag, 5, sizeof(int), st));
+  k_convert<double, T><<<gv, 256, 0, st>>>(s.pcg_x, zsol, n);
+  check_launch(h);
+}
 
 // ------------------------------------------------------------------ LM driver
 struct Scalars {
@@ -886,47 +1723,125 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   int invalid_steps = 0, iteration = 0;
   cudaEvent_t ev[6];
   for (int i = 0; i < 6; ++i) GBBA_CUDA(cudaEventCreate(&ev[i]));
+  // The launch sequence of one LM iteration, in five phases separated by the
+  // timing events.  Parameters are read from s.ext/s.intr/s.pts and the
+  // candidate is written to s.ext2/s.intr2/s.pts2 (an accepted candidate is
+  // copied back), so the sequence is invariant and is captured once into CUDA
+  // graphs that every iteration replays.
+  const Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
+  auto record_phase = [&](int ph) {
+    switch (ph) {
+      case 0:
+        if (s.dense) {
+          GBBA_CUDA(cudaMemsetAsync(S, 0, sizeof(T) * s.n_pad * s.n_pad, st));
+          k_schur_init<T><<<(unsigned)std::min<int64_t>(ceil_div(s.n_pad, 256), 1024), 256, 0, st>>>(
+              S, rhs, s.n_red, s.n_pad, s.diag_c, s.radius);
+          check_launch(h);
+        } else {
+          GBBA_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * s.n_pad, st));
+        }
+        break;
+      case 1:
+        if (s.np > 0 && s.pair_path) {
+          constexpr int B = 6 + Model<M>::K;
+          k_schur_point_rec<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, s.diag_p, s.radius, (T*)s.Vinv,
+                                                            (T*)s.gpv, (T*)s.rec, s.flag);
+          check_launch(h);
+          if (s.dense && s.n_blocks > 0) {
+            k_schur_pairs<B, T><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
+                s.blocks, s.n_blocks, s.blk_off, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k,
+                s.nc, S, s.n_pad);
+            check_launch(h);
+          }
+          k_rhs_camera<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
+              s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs);
+          check_launch(h);
+          if (!s.dense) {
+            k_cam_blocks<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
+                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.diag_c,
+                s.radius, (T*)s.pcg_u, s.pcg_minv, s.flag);
+            check_launch(h);
+          }
+        } else if (s.np > 0) {
+          k_schur_point<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, s.diag_p, s.radius, S, s.n_pad, rhs,
+                                                        (T*)s.Vinv, (T*)s.gpv, (T*)s.Wbuf, (T*)s.What, s.flag);
+          check_launch(h);
+        }
+        break;
+      case 2:
+        if (s.dense) dense_cholesky_solve<T>(h, S, s.n_pad, rhs, z, (T*)s.Linv, s.flag, st);
+        else pcg_solve<M, T>(s, o, sum);
+        break;
+      case 3:
+        if (s.np > 0) {
+          k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2,
+                                                    s.part_mcc, s.part_step_p, s.flag);
+          check_launch(h);
+        }
+        k_cam_candidate<T><<<s.nb_cam, 256, 0, st>>>(s.ext, s.intr, s.ext2, s.intr2, s.ext_col, s.intr_col, n_e, n_i, z,
+                                                     s.scale_c, s.part_step_c);
+        check_launch(h);
+        break;
+      default:
+        launch_cost(s.ext2, s.intr2, s.pts2);
+        k_reduce3<<<1, 256, 0, st>>>(s.part_mcc, s.np > 0 ? s.nb_pt : 0, s.part_step_p, s.np > 0 ? s.nb_pt : 0,
+                                     s.part_step_c, s.nb_cam, s.part_cost, s.nb_obs, s.scalars);
+        check_launch(h);
+        break;
+    }
+  };
+  int64_t phase_launches[5] = {0, 0, 0, 0, 0};
+  cudaGraphExec_t graphs[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  dense_cholesky_prepare<T>();
+  if (o->use_cuda_graphs) {
+    for (int ph = 0; ph < 5; ++ph) {
+      if (ph == 2 && !s.dense) continue;  // the PCG loop is host-driven
+      const int64_t l0 = h->launches;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        break;
+      }
+      record_phase(ph);
+      GBBA_CUDA(cudaStreamEndCapture(st, &g));
+      GBBA_CUDA(cudaGraphInstantiate(&graphs[ph], g, 0));
+      cudaGraphDestroy(g);
+      phase_launches[ph] = h->launches - l0;
+      h->launches = l0;  // captured, not yet run
+    }
+  }
+  auto run_phase = [&](int ph) {
+    if (graphs[ph]) {
+      GBBA_CUDA(cudaGraphLaunch(graphs[ph], st));
+      count_launch(h, (int)phase_launches[ph]);
+    } else {
+      const int64_t l0 = h->launches;
+      record_phase(ph);
+      phase_launches[ph] = h->launches - l0;
+    }
+  };
   while (term < 0) {
     if (iteration >= o->max_num_iterations) {
       term = GBBA_NO_CONVERGENCE;
       break;
     }
-    Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
     pin[2] = radius;
     GBBA_CUDA(cudaMemcpyAsync(s.radius, pin + 2, sizeof(double), cudaMemcpyHostToDevice, st));
     GBBA_CUDA(cudaMemsetAsync(s.flag, 0, sizeof(int), st));
     GBBA_CUDA(cudaMemsetAsync(s.nonfinite, 0, sizeof(int), st));
     GBBA_CUDA(cudaEventRecord(ev[0], st));
-    GBBA_CUDA(cudaMemsetAsync(S, 0, sizeof(T) * s.n_pad * s.n_pad, st));
-    k_schur_init<T><<<(unsigned)std::min<int64_t>(ceil_div(s.n_pad, 256), 1024), 256, 0, st>>>(S, rhs, s.n_red, s.n_pad,
-                                                                                            s.diag_c, s.radius);
-    check_launch(h);
+    run_phase(0);
     GBBA_CUDA(cudaEventRecord(ev[4], st));
-    if (s.np > 0) {
-      k_schur_point<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, s.diag_p, s.radius, S, s.n_pad, rhs,
-                                                    (T*)s.Vinv, (T*)s.gpv, (T*)s.Wbuf, (T*)s.What, s.flag);
-      check_launch(h);
-      ++sum->schur_kernel_launches;
-    }
+    run_phase(1);
     GBBA_CUDA(cudaEventRecord(ev[1], st));
-    const int64_t launches0 = h->launches;
-    dense_cholesky_solve<T>(h, S, s.n_pad, rhs, z, (T*)s.Linv, s.flag, st);
-    sum->factor_launches += (int32_t)(h->launches - launches0);
+    run_phase(2);
     GBBA_CUDA(cudaEventRecord(ev[5], st));
-    if (s.np > 0) {
-      k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2, s.part_mcc,
-                                                s.part_step_p, s.flag);
-      check_launch(h);
-    }
-    k_cam_candidate<T><<<s.nb_cam, 256, 0, st>>>(s.ext, s.intr, s.ext2, s.intr2, s.ext_col, s.intr_col, n_e, n_i, z,
-                                                 s.scale_c, s.part_step_c);
-    check_launch(h);
+    run_phase(3);
     GBBA_CUDA(cudaEventRecord(ev[2], st));
-    launch_cost(s.ext2, s.intr2, s.pts2);
-    k_reduce3<<<1, 256, 0, st>>>(s.part_mcc, s.np > 0 ? s.nb_pt : 0, s.part_step_p, s.np > 0 ? s.nb_pt : 0,
-                                 s.part_step_c, s.nb_cam, s.part_cost, s.nb_obs, s.scalars);
-    check_launch(h);
+    run_phase(4);
     GBBA_CUDA(cudaEventRecord(ev[3], st));
+    sum->schur_kernel_launches += phase_launches[1];
+    sum->factor_launches += (int32_t)phase_launches[2];
     Scalars* hs = reinterpret_cast<Scalars*>(pin + 8);
     GBBA_CUDA(cudaMemcpyAsync(hs, s.scalars, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaMemcpyAsync(&hs->flag, s.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -978,9 +1893,9 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       radius = radius / std::max(1.0 / 3.0, 1.0 - std::pow(2.0 * relative_decrease - 1.0, 3));
       radius = std::min(o->max_trust_region_radius, radius);
       decrease_factor = 2.0;
-      std::swap(s.ext, s.ext2);
-      std::swap(s.intr, s.intr2);
-      std::swap(s.pts, s.pts2);
+      GBBA_CUDA(cudaMemcpyAsync(s.ext, s.ext2, sizeof(double) * n_e, cudaMemcpyDeviceToDevice, st));
+      GBBA_CUDA(cudaMemcpyAsync(s.intr, s.intr2, sizeof(double) * n_i, cudaMemcpyDeviceToDevice, st));
+      GBBA_CUDA(cudaMemcpyAsync(s.pts, s.pts2, sizeof(double) * 3 * s.np, cudaMemcpyDeviceToDevice, st));
       const double tj = now_s();
       linearize(false, &gmax, &x_norm);
       sum->jacobian_time_s += now_s() - tj;
@@ -993,6 +1908,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     }
   }
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
+  for (int i = 0; i < 5; ++i)
+    if (graphs[i]) cudaGraphExecDestroy(graphs[i]);
   sum->termination_type = term;
   sum->usable = term != GBBA_FAILURE ? 1 : 0;
   sum->final_cost = cost;
@@ -1028,6 +1945,31 @@ gbba_status solve_impl(gbba_handle* h, const gbba_problem* P, const gbba_options
     copy_out(P->intrinsics, s.intr, sizeof(double) * s.k * s.ni, P->memory, s.st);
     copy_out(P->points, s.pts, sizeof(double) * 3 * s.np, P->memory, s.st);
     GBBA_CUDA(cudaStreamSynchronize(s.st));
+  }
+  // Mixed path: FP32 steps can end the LM early through ceres's stopping rule
+  // (a poor but accepted step with |dcost| <= 1e-6 cost).  When the mixed run
+  // reports convergence, a short plain-FP64 run from its solution, with
+  // tolerances 1000x tighter, finishes at the FP64 minimum.
+  if (st == GBBA_SUCCESS && sum->usable && sum->termination_type == GBBA_CONVERGENCE &&
+      o->precision == GBBA_PRECISION_MIXED && o->fp64_polish_iterations > 0) {
+    gbba_options o2 = *o;
+    o2.precision = GBBA_PRECISION_FP64;
+    o2.max_num_iterations = o->fp64_polish_iterations;
+    o2.function_tolerance = o->function_tolerance * 1e-3;
+    o2.parameter_tolerance = o->parameter_tolerance * 1e-3;
+    gbba_summary s2{};
+    const gbba_status st2 = solve_impl(h, P, &o2, &s2);
+    if (st2 == GBBA_SUCCESS && s2.usable) {
+      sum->final_cost = s2.final_cost;
+      sum->num_iterations += s2.num_iterations;
+      sum->num_successful_steps += s2.num_successful_steps;
+      sum->num_unsuccessful_steps += s2.num_unsuccessful_steps;
+      sum->termination_type = s2.termination_type;
+      sum->jacobian_time_s += s2.jacobian_time_s;
+      sum->linear_solver_time_s += s2.linear_solver_time_s;
+      sum->residual_time_s += s2.residual_time_s;
+      sum->linear_solver_iterations += s2.linear_solver_iterations;
+    }
   }
   sum->total_time_s = now_s() - t0;
   return st;

@@ -465,11 +465,40 @@ void out_back(gbba_handle* h, T* user, const T* dev, size_t count, int memory) {
   GBBA_CUDA(cudaMemcpyAsync(user, dev, count * sizeof(T), cudaMemcpyDeviceToHost, h->active));
 }
 
+// Device check of CSR offsets: offs[0] == 0, non-decreasing; returns the total
+// and the longest track.  info = {error, max_len, total_lo, total_hi}.
+template <typename Off>
+__global__ void k_check_offsets(const Off* offs, int64_t nt, unsigned int* info) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = (int64_t)offs[t], b = (int64_t)offs[t + 1];
+    if (b < a || (t == 0 && a != 0)) atomicExch(&info[0], 1u);
+    else atomicMax(&info[1], (unsigned int)(b - a > 0x7fffffff ? 0x7fffffff : b - a));
+    if (t == nt - 1) {
+      info[2] = (unsigned int)(b & 0xffffffff);
+      info[3] = (unsigned int)(b >> 32);
+    }
+  }
+}
+
 template <typename Off>
 void check_offsets(gbba_handle* h, const Off* offs, int64_t nt, int memory, int64_t* total, int* max_len) {
+  if (memory == GBBA_MEMORY_DEVICE) {
+    unsigned int* info = nullptr;
+    GBBA_CUDA(cudaMallocAsync((void**)&info, 4 * sizeof(unsigned int), h->active));
+    GBBA_CUDA(cudaMemsetAsync(info, 0, 4 * sizeof(unsigned int), h->active));
+    k_check_offsets<Off><<<std::max(1, std::min<int>((int)ceil_div(nt, 256), h->sm_count * 8)), 256, 0, h->active>>>(offs, nt, info);
+    check_launch(h);
+    unsigned int hi[4];
+    GBBA_CUDA(cudaMemcpyAsync(hi, info, sizeof(hi), cudaMemcpyDeviceToHost, h->active));
+    GBBA_CUDA(cudaFreeAsync(info, h->active));
+    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    GBBA_REQUIRE(hi[0] == 0, GBBA_ERROR_INVALID_ARGUMENT, "track_offsets must start at 0 and be non-decreasing");
+    *max_len = (int)hi[1];
+    *total = (int64_t)hi[2] | ((int64_t)hi[3] << 32);
+    return;
+  }
   std::vector<Off> ho(nt + 1);
-  if (memory == GBBA_MEMORY_HOST) std::memcpy(ho.data(), offs, sizeof(Off) * (nt + 1));
-  else GBBA_CUDA(cudaMemcpy(ho.data(), offs, sizeof(Off) * (nt + 1), cudaMemcpyDeviceToHost));
+  std::memcpy(ho.data(), offs, sizeof(Off) * (nt + 1));
   GBBA_REQUIRE(ho[0] == 0, GBBA_ERROR_INVALID_ARGUMENT, "track_offsets[0] must be 0");
   int ml = 0;
   for (int64_t t = 0; t < nt; ++t) {

@@ -174,8 +174,12 @@ def ring_scene(num_cameras=16, num_points=2000, seed=1, radius=10.0, extent=2.0,
 def medium_scene(num_cameras=500, num_points=200_000, seed=3, mean_views=8, sigma=0.7,
                  outlier_frac=0.05, huber=4.0, rot_sigma=0.01, t_sigma=0.05, x_sigma=0.05,
                  k_sigma=(0.05, 0.01, 0.01), radius=15.0, extent=3.0, model=abi.RADIAL_K3,
-                 geometric_views=False):
-    """Per-camera radial-K3 (or Brown-T2) scene with outliers under a Huber loss."""
+                 geometric_views=False, hold=(0,)):
+    """Per-camera radial-K3 (or Brown-T2) scene with outliers under a Huber loss.
+
+    `hold` lists the cameras whose extrinsics are held constant: camera 0 is
+    the reference's gauge; holding a second camera also fixes the scale, so
+    that the minimum is isolated instead of a flat valley."""
     rng = np.random.default_rng(seed)
     centers = radius * sphere_directions(num_cameras, rng)
     R, t = _cameras_facing_origin(centers)
@@ -207,11 +211,11 @@ def medium_scene(num_cameras=500, num_points=200_000, seed=3, mean_views=8, sigm
     pt, cam = pt[order], cam[order]
     intr_idx = cam.copy()
     obs, pred, depth = _observe(rng, model, ext_true, intr_true, X_true, cam, intr_idx, pt, sigma, outlier_frac)
-    ext, pts = _perturb(rng, ext_true.copy(), X_true, rot_sigma, t_sigma, x_sigma, fixed_cams=(0,))
+    ext, pts = _perturb(rng, ext_true.copy(), X_true, rot_sigma, t_sigma, x_sigma, fixed_cams=tuple(hold))
     intr = intr_true.copy()
     intr[:, 0] *= 1 + rng.normal(0, 0.002, num_cameras)
     cam_const = np.zeros(num_cameras, np.uint8)
-    cam_const[0] = 1
+    cam_const[list(hold)] = 1
     return _scene_dict(model, ext, intr, pts, obs, cam, intr_idx, pt,
                        camera_constant=cam_const, loss=abi.LOSS_HUBER, loss_scale=huber,
                        truth={"extrinsics": ext_true, "points": X_true, "intrinsics": intr_true},

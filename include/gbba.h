@@ -140,6 +140,10 @@ typedef struct gbba_options {
   int32_t refinement_interval;            /* mixed PCG: FP64 residual recompute every k steps: 8 */
   int32_t use_cuda_graphs;                /* 1: capture the per-iteration launch sequence */
   void* stream;                           /* cudaStream_t, or NULL for the handle's stream */
+  int32_t fp64_polish_iterations;         /* mixed path: after it stops, at most this many plain-FP64
+                                             LM iterations continue from its solution with function and
+                                             parameter tolerances 1000x tighter (0 = off): 10 */
+  int32_t reserved;
 } gbba_options;
 
 typedef struct gbba_summary {

@@ -185,3 +185,102 @@ def test_empty_and_all_constant_cameras(handle, abi, scenes):
              "intrinsic_index": np.zeros(0, np.uint32), "point_index": np.zeros(0, np.uint32)}
     s, _ = solve(handle, abi, empty, abi.default_options())
     assert s.initial_cost == 0.0 and s.usable
+
+
+def test_atomic_free_schur_matches_atomic_path(handle, abi, scenes, monkeypatch):
+    """The camera-pair (segmented, atomic-free) Schur build and the point-major
+    atomic build give the same solve (FP64, well-posed scene)."""
+    sc = scenes.medium_scene(num_cameras=25, num_points=1500, seed=101)
+    sc["camera_constant"][1] = 1
+    opts = scenes.ba_options_for(sc, max_num_iterations=15)
+    s_pair, p_pair = solve(handle, abi, sc, opts)
+    monkeypatch.setenv("GBBA_NO_PAIR_PATH", "1")
+    s_atom, p_atom = solve(handle, abi, sc, opts)
+    assert s_pair.num_iterations == s_atom.num_iterations
+    assert abs(s_pair.final_cost - s_atom.final_cost) <= 1e-10 * s_atom.final_cost
+    np.testing.assert_allclose(p_pair["points"], p_atom["points"], atol=1e-8)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_cuda_graph_replay_matches_eager_launches(precision, handle, abi, scenes):
+    sc = scenes.medium_scene(num_cameras=20, num_points=1000, seed=102)
+    sc["camera_constant"][1] = 1
+    a, pa = solve(handle, abi, sc, scenes.ba_options_for(sc, max_num_iterations=8, precision=precision,
+                                                         use_cuda_graphs=1))
+    b, pb = solve(handle, abi, sc, scenes.ba_options_for(sc, max_num_iterations=8, precision=precision,
+                                                         use_cuda_graphs=0))
+    # the column-norm reduction of the linearisation uses FP64 atomics, so two
+    # runs agree to rounding, not bit for bit
+    assert a.num_iterations == b.num_iterations
+    assert abs(a.final_cost - b.final_cost) <= 1e-12 * b.final_cost
+    np.testing.assert_allclose(pa["points"], pb["points"], rtol=0, atol=1e-9)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_iterative_schur_reaches_dense_minimum(precision, handle, abi, scenes):
+    """Block-Jacobi PCG on the implicit Schur complement (the large-problem
+    path) converges to the same minimum as the dense Cholesky."""
+    sc = scenes.medium_scene(num_cameras=30, num_points=3000, seed=103)
+    sc["camera_constant"][1] = 1
+    kw = dict(max_num_iterations=200, function_tolerance=1e-12, precision=precision)
+    d, _ = solve(handle, abi, sc, scenes.ba_options_for(sc, linear_solver=abi.SOLVER_DENSE_SCHUR, **kw))
+    i, _ = solve(handle, abi, sc, scenes.ba_options_for(sc, linear_solver=abi.SOLVER_ITERATIVE_SCHUR, **kw))
+    assert i.usable and i.linear_solver_iterations > 0
+    assert abs(i.final_cost - d.final_cost) <= 1e-7 * d.final_cost, (i.final_cost, d.final_cost)
+
+
+def batched_solve(handle, abi, scenes_list, opts):
+    hps = [abi.HostProblem(p) for p in scenes_list]
+    n = len(hps)
+    structs = (abi.GbbaProblem * n)(*[hp.struct() for hp in hps])
+    sums = (abi.GbbaSummary * n)()
+    st = handle.lib.gbba_solve_batched(handle.h, structs, n, C.byref(opts), sums)
+    return st, list(sums), [hp.params() for hp in hps]
+
+
+def local_problems(scenes, count, seed, cams=(5, 16), points=(200, 600)):
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        p = scenes.local_problem(rng, int(rng.integers(cams[0], cams[1] + 1)), int(rng.integers(points[0], points[1] + 1)))
+        p["camera_constant"][1] = 1  # isolate the minimum (see the golden fixtures)
+        out.append(p)
+    return out
+
+
+def test_batched_fp64_matches_individual_solves(handle, abi, scenes):
+    """One launch, one CTA per problem: each window follows the same LM as
+    gbba_solve and reaches the same final cost."""
+    probs = local_problems(scenes, 12, seed=111)
+    opts = abi.default_options(max_num_iterations=50)
+    st, bs, bp = batched_solve(handle, abi, probs, opts)
+    assert st == abi.SUCCESS
+    for p, s, prm in zip(probs, bs, bp):
+        si, pi = solve(handle, abi, p, opts)
+        assert s.usable and si.usable
+        assert abs(s.final_cost - si.final_cost) <= 1e-6 * si.final_cost, (s.final_cost, si.final_cost)
+        assert abs(s.initial_cost - si.initial_cost) <= 1e-12 * si.initial_cost
+        np.testing.assert_allclose(prm["points"], pi["points"], atol=1e-4)
+
+
+def test_batched_mixed_reaches_fp64_cost(handle, abi, scenes):
+    """Mixed-precision windows reach the FP64 minimum within 1e-6.  Some local
+    windows have flat valleys in which ceres's default stopping rule
+    (|dcost| <= 1e-6 cost) stops up to a few 1e-6 above the minimum, so the
+    FP64 reference here is run with a tight function tolerance."""
+    probs = local_problems(scenes, 16, seed=112, cams=(5, 40))
+    o64 = abi.default_options(max_num_iterations=300, function_tolerance=1e-12)
+    o32 = abi.default_options(max_num_iterations=100, precision=abi.PRECISION_MIXED)
+    st, b32, _ = batched_solve(handle, abi, probs, o32)
+    assert st == abi.SUCCESS
+    for p, s in zip(probs, b32):
+        si, _ = solve(handle, abi, p, o64)
+        assert s.usable and s.final_cost <= si.final_cost * (1 + 1e-6), (s.final_cost, si.final_cost)
+
+
+def test_batched_rejects_oversized_window(handle, abi, scenes):
+    probs = local_problems(scenes, 2, seed=113)
+    rng = np.random.default_rng(5)
+    probs.append(scenes.local_problem(rng, 60, 300))  # 59*6 + 8 unknowns > 256
+    st, _, _ = batched_solve(handle, abi, probs, abi.default_options(precision=abi.PRECISION_MIXED))
+    assert st == abi.ERROR_TOO_LARGE
