@@ -234,6 +234,11 @@ gbba_status gbba_create(int device, gbba_handle** out) {
   try {
     GBBA_CUDA(cudaSetDevice(device));
     GBBA_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    int least = 0;
+    GBBA_CUDA(cudaDeviceGetStreamPriorityRange(&least, &h->prio_hi));
+    GBBA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, least));
+    GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_main, cudaEventDisableTiming));
+    GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_side, cudaEventDisableTiming));
     GBBA_CUDA(cudaHostAlloc((void**)&h->pinned, 64 * sizeof(double), cudaHostAllocDefault));
     GBBA_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
   } catch (const Error& e) {
@@ -250,7 +255,12 @@ void gbba_destroy(gbba_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   h->arena.release();
   h->pair_arena.release();
+  h->item_arena.release();
   if (h->pinned) cudaFreeHost(h->pinned);
+  if (h->side) cudaStreamSynchronize(h->side);
+  if (h->ev_main) cudaEventDestroy(h->ev_main);
+  if (h->ev_side) cudaEventDestroy(h->ev_side);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }

@@ -86,12 +86,18 @@ struct gbba_handle {
   cudaStream_t stream = nullptr;
   gbba::Arena arena;
   gbba::Arena pair_arena;  // pair list + camera CSR of the atomic-free Schur build
+  gbba::Arena item_arena;  // work items and partial sums of the pair kernel
   // small pinned host buffer for per-iteration scalars
   double* pinned = nullptr;
   int64_t launches = 0;
   int sm_count = 0;
   cudaStream_t active = nullptr;  // stream of the current call
   cudaGraphExec_t graph_exec = nullptr;
+  // Dense factorisation look-ahead: the trailing update runs on `side` while
+  // the next panel is factored on the call's stream at priority `prio_hi`.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_main = nullptr, ev_side = nullptr;
+  int prio_hi = 0;
 };
 
 namespace gbba {

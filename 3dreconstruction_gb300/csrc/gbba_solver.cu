@@ -384,11 +384,12 @@ __global__ void __launch_bounds__(128) k_schur_point(Prob P, const double* __res
 // intrinsics, or intrinsics held): the camera-side columns of an observation
 // are then owned by its camera, so S splits into camera-pair blocks.
 //
-// Per-observation record of B' = 9B values (B = 6 + K):
-//   [ Jc (2 x B) | W = Jc^T Jp (B x 3) | W V^-1 (B x 3) | q = Jc^T r - W V^-1 g_p (B) ]
+// Per-observation record of 9B + 8 values (B = 6 + K):
+//   [ Jc (2 x B) | W = Jc^T Jp (B x 3) | W V^-1 (B x 3) | q = Jc^T r - W V^-1 g_p (B) | Jp (2 x 3) | r (2) ]
+// (scaled, corrected Jacobian blocks and residual of the current linearisation)
 template <int B>
 struct Rec {
-  static constexpr int kJc = 0, kW = 2 * B, kWh = 5 * B, kQ = 8 * B, kSize = 9 * B;
+  static constexpr int kJc = 0, kW = 2 * B, kWh = 5 * B, kQ = 8 * B, kJp = 9 * B, kR = 9 * B + 6, kSize = 9 * B + 8;
 };
 
 // Stage 1, one warp per point: V, V^-1, g_p and the observation records.
@@ -420,6 +421,13 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const double* _
 #pragma unroll
     for (int j = 0; j < 3; ++j) g[j] += J.Jp[0][j] * r0 + J.Jp[1][j] * r1;
     T* rc = rec + (int64_t)o * R::kSize;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      rc[R::kJp + j] = J.Jp[0][j];
+      rc[R::kJp + 3 + j] = J.Jp[1][j];
+    }
+    rc[R::kR] = r0;
+    rc[R::kR + 1] = r1;
 #pragma unroll
     for (int i = 0; i < B; ++i) {
       rc[R::kJc + i] = J.Jc[0][i];
@@ -484,32 +492,62 @@ __device__ __forceinline__ int cam_col(const int32_t* ext_col, const int32_t* in
   return g < 0 ? -1 : intr_col[K * (int64_t)g + (i - 6)];
 }
 
-// Stage 2, one warp per non-empty camera-pair block (ca >= cb): a segmented
-// reduction over the block's observation pairs (a, b) of
+// Stage 2, one warp per work item: a chunk of at most kPairChunk observation
+// pairs (a, b) of one camera-pair block (ca >= cb), reduced in order:
 //   U_a [a == b]  -  (W V^-1)_a  W_b^T
-// written once into S (lower triangle; entries that fall above the diagonal
-// are written transposed).  No atomics: each S entry has a single writer.
+// A block held by a single chunk is written once into S (lower triangle;
+// entries that fall above the diagonal are written transposed); the chunks of
+// a longer block (the diagonal blocks hold one pair per observation of the
+// camera) write partial sums that k_pair_merge adds in chunk order.  No
+// atomics: each S entry has a single writer.
+constexpr int kPairChunk = 64;
+struct PairItem {
+  uint32_t key, begin, end;
+  int32_t slot;  // -1: write S directly; else the partial-sum slot
+};
+struct PairMerge {
+  uint32_t key, first, count;
+};
+
 template <int B, typename T>
-__global__ void __launch_bounds__(128) k_schur_pairs(const uint32_t* __restrict__ blocks, int64_t nblocks,
-                                                     const uint32_t* __restrict__ blk_off,
+__device__ __forceinline__ void write_block(uint32_t ca, uint32_t cb, const T* acc, int lane,
+                                            const int32_t* __restrict__ ext_col, const int32_t* __restrict__ intr_col,
+                                            const int32_t* __restrict__ cam_group, int K, T* __restrict__ S,
+                                            int64_t ld) {
+  constexpr int E = (B * B + 31) / 32;
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int idx = lane + 32 * e;
+    if (idx >= B * B) continue;
+    const int i = idx / B, j = idx % B;
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, ca, i);
+    const int cj = cam_col(ext_col, intr_col, cam_group, K, cb, j);
+    if (ci < 0 || cj < 0) continue;
+    if (ca == cb && ci < cj) continue;
+    if (ci >= cj) S[(int64_t)ci * ld + cj] += acc[e];
+    else S[(int64_t)cj * ld + ci] += acc[e];
+  }
+}
+
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict__ items, int64_t nitems,
                                                      const unsigned long long* __restrict__ pairs,
                                                      const T* __restrict__ rec, const int32_t* __restrict__ ext_col,
                                                      const int32_t* __restrict__ intr_col,
                                                      const int32_t* __restrict__ cam_group, int K, int64_t nc,
-                                                     T* __restrict__ S, int64_t ld) {
+                                                     T* __restrict__ S, int64_t ld, T* __restrict__ partial) {
   using R = Rec<B>;
   constexpr int E = (B * B + 31) / 32;
   __shared__ T sh[4][8 * B];  // per warp: Wh_a (3B) | W_b (3B) | Jc_a (2B)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (w >= nblocks) return;
-  const uint32_t key = blocks[w];
-  const uint32_t ca = (uint32_t)(key / nc), cb = (uint32_t)(key % nc);
+  if (w >= nitems) return;
+  const PairItem it = items[w];
   T acc[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) acc[e] = T(0);
   T* sw = sh[warp];
-  for (uint32_t q = blk_off[key]; q < blk_off[key + 1]; ++q) {
+  for (uint32_t q = it.begin; q < it.end; ++q) {
     const unsigned long long pr = pairs[q];
     const uint32_t a = (uint32_t)(pr >> 32), b = (uint32_t)(pr & 0xffffffffu);
     const T* ra = rec + (int64_t)a * R::kSize;
@@ -534,18 +572,42 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const uint32_t* __restrict_
     }
     __syncwarp();
   }
+  if (it.slot >= 0) {
+    T* out = partial + (int64_t)it.slot * B * B;
 #pragma unroll
-  for (int e = 0; e < E; ++e) {
-    const int idx = lane + 32 * e;
-    if (idx >= B * B) continue;
-    const int i = idx / B, j = idx % B;
-    const int ci = cam_col(ext_col, intr_col, cam_group, K, ca, i);
-    const int cj = cam_col(ext_col, intr_col, cam_group, K, cb, j);
-    if (ci < 0 || cj < 0) continue;
-    if (ca == cb && ci < cj) continue;
-    if (ci >= cj) S[(int64_t)ci * ld + cj] += acc[e];
-    else S[(int64_t)cj * ld + ci] += acc[e];
+    for (int e = 0; e < E; ++e) {
+      const int idx = lane + 32 * e;
+      if (idx < B * B) out[idx] = acc[e];
+    }
+    return;
   }
+  write_block<B, T>((uint32_t)(it.key / nc), (uint32_t)(it.key % nc), acc, lane, ext_col, intr_col, cam_group, K, S, ld);
+}
+
+// Sum of a chunked block's partials in chunk order, written into S.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_pair_merge(const PairMerge* __restrict__ merges, int64_t nmerges,
+                                                    const T* __restrict__ partial, const int32_t* __restrict__ ext_col,
+                                                    const int32_t* __restrict__ intr_col,
+                                                    const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                    T* __restrict__ S, int64_t ld) {
+  constexpr int E = (B * B + 31) / 32;
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= nmerges) return;
+  const PairMerge m = merges[w];
+  T acc[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) acc[e] = T(0);
+  for (uint32_t c = 0; c < m.count; ++c) {
+    const T* in = partial + (int64_t)(m.first + c) * B * B;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int idx = lane + 32 * e;
+      if (idx < B * B) acc[e] += in[idx];
+    }
+  }
+  write_block<B, T>((uint32_t)(m.key / nc), (uint32_t)(m.key % nc), acc, lane, ext_col, intr_col, cam_group, K, S, ld);
 }
 
 // Stage 3, one warp per camera: rhs of the camera's columns = sum of q over
@@ -916,6 +978,91 @@ __global__ void k_cam_scatter(const uint32_t* cam, int64_t no, const uint32_t* o
   }
 }
 
+// Back substitution from the observation records (no projection is
+// recomputed): one warp per point,
+//   y_p = V^-1 (g_p - sum E'F z), step = -(z, y), m = J step,
+//   model_cost_change += -m.(r + m/2), candidate points.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ cam,
+                                                     const int32_t* __restrict__ ext_col,
+                                                     const int32_t* __restrict__ intr_col,
+                                                     const int32_t* __restrict__ cam_group, int K, int64_t np,
+                                                     const T* __restrict__ rec, const T* __restrict__ z,
+                                                     const T* __restrict__ Vinv, const T* __restrict__ gp,
+                                                     const double* __restrict__ scale_p, const double* __restrict__ pts,
+                                                     double* __restrict__ pts_new, double* __restrict__ part_mcc,
+                                                     double* __restrict__ part_step, int* __restrict__ flag) {
+  using R = Rec<B>;
+  __shared__ double smcc[4], sstep[4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  double mcc = 0.0, stp = 0.0;
+  if (p < np) {
+    const uint32_t ob = pt_off[p], oe = pt_off[p + 1];
+    T t[3] = {};
+    for (uint32_t o = ob + lane; o < oe; o += 32) {
+      const T* r = rec + (int64_t)o * R::kSize;
+      const uint32_t c = cam[o];
+      T fz0 = T(0), fz1 = T(0);
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
+        const T zi = ci >= 0 ? z[ci] : T(0);
+        fz0 += r[R::kJc + i] * zi;
+        fz1 += r[R::kJc + B + i] * zi;
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[j] += r[R::kJp + j] * fz0 + r[R::kJp + 3 + j] * fz1;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+    const T* vi = Vinv + 6 * p;
+    const T q0 = gp[3 * p] - t[0], q1 = gp[3 * p + 1] - t[1], q2 = gp[3 * p + 2] - t[2];
+    const T y[3] = {vi[0] * q0 + vi[1] * q1 + vi[2] * q2, vi[1] * q0 + vi[3] * q1 + vi[4] * q2,
+                    vi[2] * q0 + vi[4] * q1 + vi[5] * q2};
+    if (!isfinite((double)y[0]) || !isfinite((double)y[1]) || !isfinite((double)y[2])) {
+      if (lane == 0) atomicExch(flag, 3);
+    }
+    for (uint32_t o = ob + lane; o < oe; o += 32) {
+      const T* r = rec + (int64_t)o * R::kSize;
+      const uint32_t c = cam[o];
+      double m0 = 0.0, m1 = 0.0;
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
+        const double zi = ci >= 0 ? (double)z[ci] : 0.0;
+        m0 += (double)r[R::kJc + i] * zi;
+        m1 += (double)r[R::kJc + B + i] * zi;
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        m0 += (double)r[R::kJp + j] * (double)y[j];
+        m1 += (double)r[R::kJp + 3 + j] * (double)y[j];
+      }
+      m0 = -m0;
+      m1 = -m1;
+      const double r0 = (double)r[R::kR], r1 = (double)r[R::kR + 1];
+      mcc += -(m0 * (r0 + m0 / 2.0) + m1 * (r1 + m1 / 2.0));
+    }
+    if (lane < 3) {
+      const double d = -(double)y[lane] * scale_p[3 * p + lane];
+      pts_new[3 * p + lane] = pts[3 * p + lane] + d;
+      stp = d * d;
+    }
+  }
+  mcc = warp_sum(mcc);
+  stp = warp_sum(stp);
+  if (lane == 0) {
+    smcc[warp] = mcc;
+    sstep[warp] = stp;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    part_mcc[blockIdx.x] = smcc[0] + smcc[1] + smcc[2] + smcc[3];
+    part_step[blockIdx.x] = sstep[0] + sstep[1] + sstep[2] + sstep[3];
+  }
+}
+
 // Back substitution (one warp per point) + model cost change + candidate points.
 //   y_p = V^-1 (g_p - sum E'F z), step = -(z, y), m = J step,
 //   model_cost_change += -m.(r + m/2)
@@ -1131,7 +1278,11 @@ struct Solve {
   int nb_obs, nb_pt, nb_cam, nb_x;
   // atomic-free Schur build (pair list in the handle's pair arena)
   bool pair_path = false;
-  int64_t n_blocks = 0;
+  int64_t n_blocks = 0;  // work items of the pair kernel
+  int64_t n_merges = 0;
+  void* pair_items = nullptr;
+  void* pair_merges = nullptr;
+  void* pair_partial = nullptr;
   uint32_t *blocks = nullptr, *blk_off = nullptr, *cam_off = nullptr, *cam_obs = nullptr;
   unsigned long long* pairs = nullptr;
   int32_t* cam_group = nullptr;
@@ -1400,7 +1551,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p1.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
     p1.take<uint32_t>(np + 1);
     p1.take<uint32_t>(np + 1);
-    p1.take<char>((size_t)no * 9 * B * tsize);
+    p1.take<char>((size_t)no * (9 * B + 8) * tsize);
     // PCG vectors (x, r, z, p, q, b), point temporaries, camera blocks
     p1.take<double>(6 * n_pcg);
     p1.take<double>(3 * np);
@@ -1425,7 +1576,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     uint32_t* chunks = A.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
     uint32_t* pcnt = A.take<uint32_t>(np + 1);
     uint32_t* pair_off = A.take<uint32_t>(np + 1);
-    s.rec = A.take<char>((size_t)no * 9 * B * tsize);
+    s.rec = A.take<char>((size_t)no * (9 * B + 8) * tsize);
     s.pcg_x = A.take<double>(n_pcg);
     s.pcg_r = A.take<double>(n_pcg);
     s.pcg_z = A.take<double>(n_pcg);
@@ -1521,12 +1672,37 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
                                                 key_bits(nk), st));
       count_launch(h, 4);
     }
-    k_nonempty<<<std::max(1, (int)std::min<int64_t>(ceil_div(nk, 256), h->sm_count * 8)), 256, 0, st>>>(s.blk_off, nk, s.blocks, count);
-    check_launch(h);
-    uint32_t hcount = 0;
-    GBBA_CUDA(cudaMemcpyAsync(&hcount, count, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    // work items: chunks of at most kPairChunk pairs per camera-pair block
+    std::vector<uint32_t> hoff(nk + 1);
+    GBBA_CUDA(cudaMemcpyAsync(hoff.data(), s.blk_off, sizeof(uint32_t) * (nk + 1), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaStreamSynchronize(st));
-    s.n_blocks = hcount;
+    std::vector<PairItem> items;
+    std::vector<PairMerge> merges;
+    int32_t slots = 0;
+    for (int64_t key = 0; key < nk; ++key) {
+      const uint32_t b = hoff[key], e = hoff[key + 1];
+      if (e == b) continue;
+      const uint32_t nch = (e - b + kPairChunk - 1) / kPairChunk;
+      if (nch == 1) {
+        items.push_back(PairItem{(uint32_t)key, b, e, -1});
+        continue;
+      }
+      merges.push_back(PairMerge{(uint32_t)key, (uint32_t)slots, nch});
+      for (uint32_t c = 0; c < nch; ++c)
+        items.push_back(PairItem{(uint32_t)key, b + c * kPairChunk, std::min(e, b + (c + 1) * kPairChunk), slots++});
+    }
+    Arena& I = h->item_arena;
+    I.reset();
+    I.reserve(sizeof(PairItem) * items.size() + sizeof(PairMerge) * merges.size() + (size_t)slots * B * B * tsize +
+              4096);
+    s.pair_items = I.take<PairItem>(items.size());
+    s.pair_merges = I.take<PairMerge>(merges.size());
+    s.pair_partial = I.take<char>((size_t)slots * B * B * tsize);
+    GBBA_CUDA(cudaMemcpyAsync(s.pair_items, items.data(), sizeof(PairItem) * items.size(), cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaMemcpyAsync(s.pair_merges, merges.data(), sizeof(PairMerge) * merges.size(), cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    s.n_blocks = (int64_t)items.size();
+    s.n_merges = (int64_t)merges.size();
     s.pair_path = true;
     return;
   }
@@ -1749,9 +1925,15 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
           check_launch(h);
           if (s.dense && s.n_blocks > 0) {
             k_schur_pairs<B, T><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
-                s.blocks, s.n_blocks, s.blk_off, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k,
-                s.nc, S, s.n_pad);
+                (const PairItem*)s.pair_items, s.n_blocks, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col,
+                s.cam_group, s.k, s.nc, S, s.n_pad, (T*)s.pair_partial);
             check_launch(h);
+            if (s.n_merges > 0) {
+              k_pair_merge<B, T><<<(unsigned)ceil_div(s.n_merges * 32, 128), 128, 0, st>>>(
+                  (const PairMerge*)s.pair_merges, s.n_merges, (const T*)s.pair_partial, s.ext_col, s.intr_col,
+                  s.cam_group, s.k, s.nc, S, s.n_pad);
+              check_launch(h);
+            }
           }
           k_rhs_camera<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
               s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs);
@@ -1773,7 +1955,13 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
         else pcg_solve<M, T>(s, o, sum);
         break;
       case 3:
-        if (s.np > 0) {
+        if (s.np > 0 && s.pair_path) {
+          constexpr int B = 6 + Model<M>::K;
+          k_backsub_rec<B, T><<<s.nb_pt, 128, 0, st>>>(s.pt_off, s.cam, s.ext_col, s.intr_col, s.cam_group, s.k, s.np,
+                                                       (const T*)s.rec, z, (const T*)s.Vinv, (const T*)s.gpv,
+                                                       s.scale_p, s.pts, s.pts2, s.part_mcc, s.part_step_p, s.flag);
+          check_launch(h);
+        } else if (s.np > 0) {
           k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2,
                                                     s.part_mcc, s.part_step_p, s.flag);
           check_launch(h);

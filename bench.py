@@ -15,8 +15,12 @@ Metric: observations x LM iterations per second (higher is better).
   e2e        the same solve through the C ABI with pinned HOST buffers: the
              host->device upload, sort and the device->host write-back of the
              refined parameters are inside the timed region.
-  roofline   the Schur elimination kernel (the dominant HBM kernel): its
-             algorithmic bytes per launch / its event-timed duration.
+  roofline   the Schur elimination phase (the HBM-bound kernels that build
+             S: point records, camera-pair products, merges, camera rhs):
+             its algorithmic bytes per execution / its event-timed duration.
+  factor_roofline  the dense FP32 Cholesky of S (a latency-bound chain of
+             64-wide panels): n^3/3 flops / its event-timed duration against
+             the FP32 SIMT peak.
   time_to_cost  plain FP64 GPU path run to convergence gives C*; the mixed
              path (FP32 LM, then its FP64 polish of at most 10 iterations)
              is timed to its final cost and checked against (1+1e-6) C*.
@@ -47,18 +51,37 @@ UNIT = "obs*iter/s"
 
 
 def algorithmic_schur_bytes(no, np_, n_red, p_c, s):
-    """Compulsory DRAM bytes of one launch of the point-major Schur kernel.
+    """Compulsory DRAM bytes of one Schur-elimination phase (one LM iteration).
 
+    The phase is k_schur_point_rec (one warp per point: Jacobian, V, V^-1,
+    per-observation records), k_schur_pairs + k_pair_merge (the camera-pair
+    products W_a^T V^-1 W_b, summed in a fixed order) and k_rhs_camera.
     Reads: observations (x,y FP64 = 16 B) + camera/intrinsic/point index
     (3 x 4 B) per observation; point parameters (24 B), Jacobi scale and LM
     diagonal (2 x 3 x 8 B) and CSR offset (4 B) per point; camera-side
-    parameters once (p_c x 8 B per camera).  Writes: V^-1 (6 s) and g_p (3 s)
-    per point; the stored W and W V^-1 blocks (2 x p_c x 3 x s) per
-    observation; the lower triangle of S (n^2/2 x s) and rhs (n x s)."""
+    parameters (p_c x 8 B per camera).  Writes: the per-observation record
+    (Jc 2p_c, W 3p_c, W V^-1 3p_c, q p_c, Jp 6, r 2 values = 9p_c + 8) and
+    V^-1, g_p (9 values) per point; the lower triangle of S (n^2/2) and rhs
+    (n).  The pair products read W and W V^-1 of every observation once
+    (6 p_c values).  s = bytes per value of the phase's arithmetic type."""
     n_cam = n_red // p_c if p_c else 0
-    reads = no * (16 + 12) + np_ * (24 + 48 + 4) + n_cam * p_c * 8
-    writes = np_ * 9 * s + no * 2 * p_c * 3 * s + (n_red * n_red // 2) * s + n_red * s
+    reads = no * (16 + 12) + np_ * (24 + 48 + 4) + n_cam * p_c * 8 + no * 6 * p_c * s
+    writes = no * (9 * p_c + 8) * s + np_ * 9 * s + (n_red * n_red // 2) * s + n_red * s
     return reads + writes
+
+
+def factor_flops(n_red):
+    """Dense Cholesky of S (n^3/3) plus the two triangular solves (2 n^2)."""
+    return n_red ** 3 / 3.0 + 2.0 * n_red ** 2
+
+
+# DRAM bytes (read + write) of one Schur phase on the medium workload, from
+# ncu's dram__bytes_read.sum + dram__bytes_write.sum summed over the phase's
+# kernels (profiles/schur_phase_medium.md); None until captured.
+SCHUR_TRAFFIC_PER_PHASE = None
+
+# FP32 SIMT peak of a GB300: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz.
+FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
 
 
 def env_rank():
@@ -281,12 +304,14 @@ def run_ours(args):
     e1 = torch.cuda.Event(enable_timing=True)
     iters = 0
     schur_t = 0.0
-    schur_n = 0
+    factor_t = 0.0
+    phase_launches = 0
     e0.record(stream)
     for _ in range(args.steps):
         iters += step()
         schur_t += summ.schur_kernel_time_s
-        schur_n += summ.schur_kernel_launches
+        factor_t += summ.factor_time_s
+        phase_launches = summ.schur_kernel_launches // max(1, summ.num_iterations)
     e1.record(stream)
     barrier()
     clk = clocks.stop()
@@ -343,8 +368,10 @@ def run_ours(args):
         peak = float(peaks.get("hbm_gbs", 6800.0))
         p_c = 12
         alg = algorithmic_schur_bytes(no, len(scene["points"]), n_red, p_c, 4)
-        per_launch_s = schur_t / max(1, schur_n)
-        achieved = alg / per_launch_s / 1e9
+        per_phase_s = schur_t / max(1, iters)
+        achieved = alg / per_phase_s / 1e9
+        per_factor_s = factor_t / max(1, iters)
+        ff = factor_flops(n_red)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -358,11 +385,20 @@ def run_ours(args):
             "gpu_launches": int(launches),
             "clocks": clk,
             "e2e": e2e,
-            "roofline": {"kernel": "k_schur_point (Schur elimination, point-major)", "bound": "hbm",
-                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "roofline": {"kernel": "Schur elimination phase (k_schur_point_rec + k_schur_pairs + k_pair_merge"
+                                   " + k_rhs_camera), one execution per LM iteration",
+                         "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
                          "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
-                         "algorithmic_bytes_per_launch": alg, "launch_ms": per_launch_s * 1e3,
-                         "traffic": None},
+                         "algorithmic_bytes_per_launch": alg, "launch_ms": per_phase_s * 1e3,
+                         "kernel_launches_per_phase": int(phase_launches),
+                         "traffic": SCHUR_TRAFFIC_PER_PHASE},
+            "factor_roofline": {"kernel": "dense Cholesky of S + triangular solves (FP32, blocked, NB=64)",
+                                "bound": "fp32 simt", "achieved": ff / per_factor_s / 1e12,
+                                "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
+                                "frac": ff / per_factor_s / 1e12 / FP32_SIMT_TFLOPS,
+                                "peak_source": "nominal (152 SMs x 128 lanes x 2 x 2.07 GHz)",
+                                "flops_per_factorization": ff, "factor_ms": per_factor_s * 1e3},
         }
     # ---- time to cost: plain FP64 GPU to convergence (C*), mixed to (1+1e-6) C*
     if args.time_to_cost and rank == 0:
