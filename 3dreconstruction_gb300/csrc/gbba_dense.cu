@@ -40,12 +40,6 @@ __device__ __forceinline__ T* vec_at(int i) {
 template <typename T>
 constexpr size_t dense_smem_bytes() { return (size_t)2 * NB * (NB + 1) * sizeof(T) + 2 * NB * sizeof(T); }
 
-// Vector type for 16-byte tile loads (rows of S are 256-byte aligned: n_pad
-// and every tile origin are multiples of 64 elements).
-template <typename T> struct Vec16;
-template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
-template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
-
 // Copy the 64x64 tile at src (row stride ld) into a padded shared tile.  All
 // of a thread's global loads are issued before its shared stores so that
 // their latencies overlap.
@@ -65,33 +59,6 @@ __device__ __forceinline__ void load_tile(T (*dst)[NB + 1], const T* __restrict_
     const T* e = reinterpret_cast<const T*>(&v[it]);
 #pragma unroll
     for (int w = 0; w < W; ++w) dst[r][c + w] = e[w];
-  }
-}
-
-// Four consecutive values through 16-byte accesses (p 16-byte aligned).
-template <typename T>
-__device__ __forceinline__ void ld4(const T* p, T v[4]) {
-  using V = typename Vec16<T>::type;
-  constexpr int W = Vec16<T>::n;
-#pragma unroll
-  for (int q = 0; q < 4 / W; ++q) {
-    const V x = reinterpret_cast<const V*>(p)[q];
-    const T* e = reinterpret_cast<const T*>(&x);
-#pragma unroll
-    for (int w = 0; w < W; ++w) v[q * W + w] = e[w];
-  }
-}
-template <typename T>
-__device__ __forceinline__ void st4(T* p, const T v[4]) {
-  using V = typename Vec16<T>::type;
-  constexpr int W = Vec16<T>::n;
-#pragma unroll
-  for (int q = 0; q < 4 / W; ++q) {
-    V x;
-    T* e = reinterpret_cast<T*>(&x);
-#pragma unroll
-    for (int w = 0; w < W; ++w) e[w] = v[q * W + w];
-    reinterpret_cast<V*>(p)[q] = x;
   }
 }
 

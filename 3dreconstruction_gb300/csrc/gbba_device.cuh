@@ -86,17 +86,11 @@ __device__ __forceinline__ void rotate(const T w[3], const T X[3], T p[3], T R[3
   }
 }
 
-// Residual (and Jacobian blocks when kJac) of one observation.
-//   Je [2][6]: d r / d(w, t);  Jk [2][K]: d r / d intrinsics;  Jx [2][3]: d r / d X
+// Camera model applied to the camera-frame point p: residual, and with kJac
+// the intrinsic block Jk and D = d r / d p.
 template <int M, typename T, bool kJac>
-__device__ __forceinline__ void residual(const T* __restrict__ Kp, const T E[6], const T X[3], T ox, T oy,
-                                         T r[2], T Je[2][6], T Jk[2][Model<M>::K], T Jx[2][3], T* depth) {
-  T p[3], R[3][3], dpdw[3][3];
-  rotate<T, kJac>(E, X, p, R, dpdw);
-  p[0] += E[3];
-  p[1] += E[4];
-  p[2] += E[5];
-  if (depth) *depth = p[2];
+__device__ __forceinline__ void camera_residual(const T* __restrict__ Kp, const T p[3], T ox, T oy, T r[2],
+                                                T Jk[2][Model<M>::K], T D[2][3]) {
   const T iz = T(1) / p[2];
   const T x = p[0] * iz, y = p[1] * iz;
   T A[2][2];  // d r / d(x, y)
@@ -148,13 +142,29 @@ __device__ __forceinline__ void residual(const T* __restrict__ Kp, const T E[6],
   }
   if (kJac) {
     // d r / d p = A . [[iz, 0, -x iz], [0, iz, -y iz]]
-    T D[2][3];
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       D[i][0] = A[i][0] * iz;
       D[i][1] = A[i][1] * iz;
       D[i][2] = -(A[i][0] * x + A[i][1] * y) * iz;
     }
+  }
+}
+
+// Residual (and Jacobian blocks when kJac) of one observation.
+//   Je [2][6]: d r / d(w, t);  Jk [2][K]: d r / d intrinsics;  Jx [2][3]: d r / d X
+template <int M, typename T, bool kJac>
+__device__ __forceinline__ void residual(const T* __restrict__ Kp, const T E[6], const T X[3], T ox, T oy,
+                                         T r[2], T Je[2][6], T Jk[2][Model<M>::K], T Jx[2][3], T* depth) {
+  T p[3], R[3][3], dpdw[3][3];
+  rotate<T, kJac>(E, X, p, R, dpdw);
+  p[0] += E[3];
+  p[1] += E[4];
+  p[2] += E[5];
+  if (depth) *depth = p[2];
+  T D[2][3];
+  camera_residual<M, T, kJac>(Kp, p, ox, oy, r, Jk, D);
+  if (kJac) {
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
@@ -165,6 +175,45 @@ __device__ __forceinline__ void residual(const T* __restrict__ Kp, const T E[6],
       }
     }
   }
+}
+
+// Camera pose as 12 values: R(w) row-major (the matrix form of the rotation
+// that rotate() applies, with the same first-order branch) and t.
+template <typename T>
+__device__ __forceinline__ void pose_matrix(const T E[6], T pose[12]) {
+  const T w[3] = {E[0], E[1], E[2]};
+  const T th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  if (th2 > T(DBL_EPSILON)) {
+    const T th = dsqrt(th2);
+    T s, c;
+    dsincos(th, &s, &c);
+    const T ith = T(1) / th;
+    const T u[3] = {w[0] * ith, w[1] * ith, w[2] * ith};
+    const T omc = T(1) - c;
+    pose[0] = c + omc * u[0] * u[0];        pose[1] = -s * u[2] + omc * u[0] * u[1]; pose[2] = s * u[1] + omc * u[0] * u[2];
+    pose[3] = s * u[2] + omc * u[1] * u[0]; pose[4] = c + omc * u[1] * u[1];        pose[5] = -s * u[0] + omc * u[1] * u[2];
+    pose[6] = -s * u[1] + omc * u[2] * u[0]; pose[7] = s * u[0] + omc * u[2] * u[1]; pose[8] = c + omc * u[2] * u[2];
+  } else {
+    pose[0] = T(1);  pose[1] = -w[2]; pose[2] = w[1];
+    pose[3] = w[2];  pose[4] = T(1);  pose[5] = -w[0];
+    pose[6] = -w[1]; pose[7] = w[0];  pose[8] = T(1);
+  }
+  pose[9] = E[3];
+  pose[10] = E[4];
+  pose[11] = E[5];
+}
+
+// Residual only, from a precomputed pose: p = R X + t.  Equal to residual()
+// up to rounding (the rotation is applied as a matrix instead of through
+// the Rodrigues terms), without a sine or cosine per observation.
+template <int M, typename T>
+__device__ __forceinline__ void residual_pose(const T* __restrict__ Kp, const T* __restrict__ pose, const T X[3], T ox,
+                                              T oy, T r[2]) {
+  T p[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) p[i] = pose[3 * i] * X[0] + pose[3 * i + 1] * X[1] + pose[3 * i + 2] * X[2] + pose[9 + i];
+  T Jk[2][Model<M>::K], D[2][3];
+  camera_residual<M, T, false>(Kp, p, ox, oy, r, Jk, D);
 }
 
 // Huber / squared loss: returns the cost 1/2 rho(s) and the Corrector scale sqrt(rho').

@@ -111,4 +111,37 @@ inline void check_launch(gbba_handle* h) {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Vector type of 16-byte loads and stores.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec16<double> { using type = double2; static constexpr int n = 2; };
+
+// Four consecutive values through 16-byte accesses (p 16-byte aligned).
+template <typename T>
+__device__ __forceinline__ void ld4(const T* p, T v[4]) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::n;
+#pragma unroll
+  for (int q = 0; q < 4 / W; ++q) {
+    const V x = reinterpret_cast<const V*>(p)[q];
+    const T* e = reinterpret_cast<const T*>(&x);
+#pragma unroll
+    for (int w = 0; w < W; ++w) v[q * W + w] = e[w];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void st4(T* p, const T v[4]) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::n;
+#pragma unroll
+  for (int q = 0; q < 4 / W; ++q) {
+    V x;
+    T* e = reinterpret_cast<T*>(&x);
+#pragma unroll
+    for (int w = 0; w < W; ++w) e[w] = v[q * W + w];
+    reinterpret_cast<V*>(p)[q] = x;
+  }
+}
+
+
 }  // namespace gbba

@@ -147,6 +147,9 @@ struct Prob {
   int64_t nc, ni, np, no;
   int loss_type;
   double loss_a;
+  // FP64 camera poses (pose_matrix, 12 per camera) of ext, or null: the
+  // mixed path evaluates its FP64 residuals from them.
+  const double* pose;
 };
 
 template <int M, typename T>
@@ -179,8 +182,12 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
   if constexpr (sizeof(T) == 8) {
     residual<M, T, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (T*)nullptr);
   } else {
-    double dJe[2][6], dJk[2][K], dJx[2][3];
-    residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    if (P.pose) {
+      residual_pose<M, double>(Kd, P.pose + 12 * (int64_t)c, Xd, ob.x, ob.y, r);
+    } else {
+      double dJe[2][6], dJk[2][K], dJx[2][3];
+      residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    }
     T Ef[6], Kf[K], Xf[3], rf[2];
 #pragma unroll
     for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
@@ -392,9 +399,78 @@ struct Rec {
   static constexpr int kJc = 0, kW = 2 * B, kWh = 5 * B, kQ = 8 * B, kJp = 9 * B, kR = 9 * B + 6, kSize = 9 * B + 8;
 };
 
-// Stage 1, one warp per point: V, V^-1, g_p and the observation records.
+// (V + D_p^2 / radius)^-1 of one point by a 3x3 Cholesky; v = upper
+// triangle of V (00 01 02 11 12 22).  Returns false on a non-positive pivot
+// or a non-finite inverse.
+template <typename T>
+__device__ __forceinline__ bool point_vinv(const T v[6], const double* __restrict__ dp, double rad, T vi[6]) {
+  const T a00 = v[0] + (T)(dp[0] / rad), a11 = v[3] + (T)(dp[1] / rad), a22 = v[5] + (T)(dp[2] / rad);
+  const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
+  const T d1 = a11 - l10 * l10;
+  const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
+  const T d2 = a22 - l20 * l20 - l21 * l21;
+  const T l22 = sqrt(d2);
+  const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
+  const T i10 = -l10 * i00 * i11, i21 = -l21 * i11 * i22, i20 = -(l20 * i00 + l21 * i10) * i22;
+  vi[0] = i00 * i00 + i10 * i10 + i20 * i20;
+  vi[1] = i10 * i11 + i20 * i21;
+  vi[2] = i20 * i22;
+  vi[3] = i11 * i11 + i21 * i21;
+  vi[4] = i21 * i22;
+  vi[5] = i22 * i22;
+  return a00 > T(0) && d1 > T(0) && d2 > T(0) && isfinite(vi[0]) && isfinite(vi[3]) && isfinite(vi[5]);
+}
+
+// V and g_p contributions of one observation (upper triangle of Jp^T Jp, Jp^T r).
 template <int M, typename T>
-__global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const double* __restrict__ scale_c,
+__device__ __forceinline__ void point_terms(const ObsJac<M, T>& J, T v[6], T g[3]) {
+  const T r0 = (T)J.r[0], r1 = (T)J.r[1];
+  v[0] = J.Jp[0][0] * J.Jp[0][0] + J.Jp[1][0] * J.Jp[1][0];
+  v[1] = J.Jp[0][0] * J.Jp[0][1] + J.Jp[1][0] * J.Jp[1][1];
+  v[2] = J.Jp[0][0] * J.Jp[0][2] + J.Jp[1][0] * J.Jp[1][2];
+  v[3] = J.Jp[0][1] * J.Jp[0][1] + J.Jp[1][1] * J.Jp[1][1];
+  v[4] = J.Jp[0][1] * J.Jp[0][2] + J.Jp[1][1] * J.Jp[1][2];
+  v[5] = J.Jp[0][2] * J.Jp[0][2] + J.Jp[1][2] * J.Jp[1][2];
+#pragma unroll
+  for (int j = 0; j < 3; ++j) g[j] = J.Jp[0][j] * r0 + J.Jp[1][j] * r1;
+}
+
+// Points are processed in groups: consecutive points whose observations fit
+// one warp (at most 32 in total) share a warp, one observation per lane; a
+// point with no observation or with more than 32 has a warp of its own.
+// pt_grp[i] is the first point of group i (pt_grp[n_groups] = np).
+constexpr int kGroupChunk = 256;  // points per thread of the greedy packing
+
+// Greedy packing over chunks of kGroupChunk points (a chunk always starts a
+// new group): with write = 0 counts the groups of each chunk into out[chunk],
+// with write = 1 writes their first points at out[goff[chunk]...].
+__global__ void k_pt_groups(const uint32_t* __restrict__ pt_off, int64_t np, const uint32_t* __restrict__ goff,
+                            uint32_t* __restrict__ out, int write) {
+  const int64_t ch = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nch = (np + kGroupChunk - 1) / kGroupChunk;
+  if (ch >= nch) return;
+  const int64_t p_end = min(np, (ch + 1) * kGroupChunk);
+  uint32_t ng = 0, cur = 0;
+  uint32_t* dst = write ? out + goff[ch] : nullptr;
+  for (int64_t p = ch * kGroupChunk; p < p_end; ++p) {
+    const uint32_t n = pt_off[p + 1] - pt_off[p];
+    const bool alone = n == 0 || n > 32;
+    if (alone || cur == 0 || cur + n > 32) {
+      if (write) dst[ng] = (uint32_t)p;
+      ++ng;
+      cur = alone ? 33u : n;  // 33 closes the group
+    } else {
+      cur += n;
+    }
+  }
+  if (!write) out[ch] = ng;
+  else if (ch == nch - 1) out[goff[nch]] = (uint32_t)np;
+}
+
+// Stage 1, one warp per point group: V, V^-1, g_p and the observation records.
+template <int M, typename T>
+__global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
+                                                         const double* __restrict__ scale_c,
                                                          const double* __restrict__ scale_p,
                                                          const double* __restrict__ diag_p,
                                                          const double* __restrict__ radius, T* __restrict__ Vinv,
@@ -403,23 +479,133 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const double* _
   constexpr int B = ObsJac<M, T>::B;
   using R = Rec<B>;
   const int lane = threadIdx.x & 31;
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (p >= P.np) return;
-  const uint32_t ob = P.pt_off[p], oe = P.pt_off[p + 1];
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (w >= n_groups) return;
+  const uint32_t p0 = pt_grp[w], p1 = pt_grp[w + 1];
+  const uint32_t o0 = P.pt_off[p0], o1 = P.pt_off[p1];
+  const double rad = *radius;
+  if (p1 - p0 > 1 || (o1 - o0 >= 1 && o1 - o0 <= 32)) {
+    // ---- packed: lane i holds observation o0 + i
+    const uint32_t o = o0 + lane;
+    const bool valid = o < o1;
+    ObsJac<M, T> J;
+    T v[6] = {}, g[3] = {};
+    uint32_t p = 0;
+    int head = lane, tail = lane;
+    if (valid) {
+      double cost;
+      obs_jacobian<M, T, true>(P, o, scale_c, scale_p, J, &cost);
+      point_terms<M, T>(J, v, g);
+      p = P.pt[o];
+      head = (int)(P.pt_off[p] - o0);
+      tail = (int)(P.pt_off[p + 1] - o0) - 1;
+    }
+    // segmented inclusive scan over the point's lanes, then the total from its last lane
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const bool take = lane - d >= head;
+#pragma unroll
+      for (int i = 0; i < 6; ++i) {
+        const T y = __shfl_up_sync(0xffffffffu, v[i], d);
+        if (take) v[i] += y;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const T y = __shfl_up_sync(0xffffffffu, g[i], d);
+        if (take) g[i] += y;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) v[i] = __shfl_sync(0xffffffffu, v[i], tail);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] = __shfl_sync(0xffffffffu, g[i], tail);
+    if (!valid) return;
+    T vi[6];
+    const bool ok = point_vinv<T>(v, diag_p + 3 * (int64_t)p, rad, vi);
+    if (lane == head) {
+      if (!ok) atomicExch(flag, 2);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) gp[3 * (int64_t)p + i] = g[i];
+    }
+    const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
+    const T r0 = (T)J.r[0], r1 = (T)J.r[1];
+    T* rc = rec + (int64_t)o * R::kSize;
+    if constexpr (B % 4 == 0) {
+      // every field starts on a 16-byte boundary: write the record in 16-byte pieces
+#pragma unroll
+      for (int c4 = 0; c4 < 2 * B; c4 += 4) {
+        T t4[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) t4[e] = c4 + e < B ? J.Jc[0][c4 + e] : J.Jc[1][c4 + e - B];
+        st4<T>(rc + R::kJc + c4, t4);
+      }
+#pragma unroll
+      for (int i0 = 0; i0 < B; i0 += 4) {
+        T wc[12], yc[12], qc[4];
+#pragma unroll
+        for (int ii = 0; ii < 4; ++ii) {
+          const int i = i0 + ii;
+#pragma unroll
+          for (int j = 0; j < 3; ++j) wc[3 * ii + j] = J.Jc[0][i] * J.Jp[0][j] + J.Jc[1][i] * J.Jp[1][j];
+#pragma unroll
+          for (int j = 0; j < 3; ++j)
+            yc[3 * ii + j] = wc[3 * ii] * Vf[0][j] + wc[3 * ii + 1] * Vf[1][j] + wc[3 * ii + 2] * Vf[2][j];
+          qc[ii] = (J.Jc[0][i] * r0 + J.Jc[1][i] * r1) -
+                   (yc[3 * ii] * g[0] + yc[3 * ii + 1] * g[1] + yc[3 * ii + 2] * g[2]);
+        }
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+          st4<T>(rc + R::kW + 3 * i0 + 4 * e, wc + 4 * e);
+          st4<T>(rc + R::kWh + 3 * i0 + 4 * e, yc + 4 * e);
+        }
+        st4<T>(rc + R::kQ + i0, qc);
+      }
+      const T t8[8] = {J.Jp[0][0], J.Jp[0][1], J.Jp[0][2], J.Jp[1][0], J.Jp[1][1], J.Jp[1][2], r0, r1};
+      st4<T>(rc + R::kJp, t8);
+      st4<T>(rc + R::kJp + 4, t8 + 4);
+      return;
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      rc[R::kJp + j] = J.Jp[0][j];
+      rc[R::kJp + 3 + j] = J.Jp[1][j];
+    }
+    rc[R::kR] = r0;
+    rc[R::kR + 1] = r1;
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      rc[R::kJc + i] = J.Jc[0][i];
+      rc[R::kJc + B + i] = J.Jc[1][i];
+      T wr[3], y[3];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) wr[j] = J.Jc[0][i] * J.Jp[0][j] + J.Jc[1][i] * J.Jp[1][j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) y[j] = wr[0] * Vf[0][j] + wr[1] * Vf[1][j] + wr[2] * Vf[2][j];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        rc[R::kW + i * 3 + j] = wr[j];
+        rc[R::kWh + i * 3 + j] = y[j];
+      }
+      rc[R::kQ + i] = (J.Jc[0][i] * r0 + J.Jc[1][i] * r1) - (y[0] * g[0] + y[1] * g[1] + y[2] * g[2]);
+    }
+    return;
+  }
+  // ---- one point (no observation, or more than 32): lanes stride its observations
+  const uint32_t p = p0;
   T v[6] = {}, g[3] = {};
-  for (uint32_t o = ob + lane; o < oe; o += 32) {
+  for (uint32_t o = o0 + lane; o < o1; o += 32) {
     ObsJac<M, T> J;
     double cost;
     obs_jacobian<M, T, true>(P, o, scale_c, scale_p, J, &cost);
-    const T r0 = (T)J.r[0], r1 = (T)J.r[1];
-    v[0] += J.Jp[0][0] * J.Jp[0][0] + J.Jp[1][0] * J.Jp[1][0];
-    v[1] += J.Jp[0][0] * J.Jp[0][1] + J.Jp[1][0] * J.Jp[1][1];
-    v[2] += J.Jp[0][0] * J.Jp[0][2] + J.Jp[1][0] * J.Jp[1][2];
-    v[3] += J.Jp[0][1] * J.Jp[0][1] + J.Jp[1][1] * J.Jp[1][1];
-    v[4] += J.Jp[0][1] * J.Jp[0][2] + J.Jp[1][1] * J.Jp[1][2];
-    v[5] += J.Jp[0][2] * J.Jp[0][2] + J.Jp[1][2] * J.Jp[1][2];
+    T dv[6], dg[3];
+    point_terms<M, T>(J, dv, dg);
 #pragma unroll
-    for (int j = 0; j < 3; ++j) g[j] += J.Jp[0][j] * r0 + J.Jp[1][j] * r1;
+    for (int i = 0; i < 6; ++i) v[i] += dv[i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) g[i] += dg[i];
+    const T r0 = (T)J.r[0], r1 = (T)J.r[1];
     T* rc = rec + (int64_t)o * R::kSize;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -441,35 +627,17 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const double* _
   for (int i = 0; i < 6; ++i) v[i] = warp_sum(v[i]);
 #pragma unroll
   for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
-  const double rad = *radius;
-  const T a00 = v[0] + (T)(diag_p[3 * p] / rad), a11 = v[3] + (T)(diag_p[3 * p + 1] / rad),
-          a22 = v[5] + (T)(diag_p[3 * p + 2] / rad);
-  const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
-  const T d1 = a11 - l10 * l10;
-  const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
-  const T d2 = a22 - l20 * l20 - l21 * l21;
-  const T l22 = sqrt(d2);
-  const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
-  const T i10 = -l10 * i00 * i11, i21 = -l21 * i11 * i22, i20 = -(l20 * i00 + l21 * i10) * i22;
   T vi[6];
-  vi[0] = i00 * i00 + i10 * i10 + i20 * i20;
-  vi[1] = i10 * i11 + i20 * i21;
-  vi[2] = i20 * i22;
-  vi[3] = i11 * i11 + i21 * i21;
-  vi[4] = i21 * i22;
-  vi[5] = i22 * i22;
-  if (!(a00 > T(0)) || !(d1 > T(0)) || !(d2 > T(0)) || !isfinite((double)vi[0]) || !isfinite((double)vi[3]) ||
-      !isfinite((double)vi[5])) {
-    if (lane == 0) atomicExch(flag, 2);
-  }
+  const bool ok = point_vinv<T>(v, diag_p + 3 * (int64_t)p, rad, vi);
   if (lane == 0) {
+    if (!ok) atomicExch(flag, 2);
 #pragma unroll
-    for (int i = 0; i < 6; ++i) Vinv[6 * p + i] = vi[i];
+    for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) gp[3 * p + i] = g[i];
+    for (int i = 0; i < 3; ++i) gp[3 * (int64_t)p + i] = g[i];
   }
   const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
-  for (uint32_t o = ob + lane; o < oe; o += 32) {
+  for (uint32_t o = o0 + lane; o < o1; o += 32) {
     T* rc = rec + (int64_t)o * R::kSize;
 #pragma unroll
     for (int i = 0; i < B; ++i) {
@@ -500,7 +668,7 @@ __device__ __forceinline__ int cam_col(const int32_t* ext_col, const int32_t* in
 // a longer block (the diagonal blocks hold one pair per observation of the
 // camera) write partial sums that k_pair_merge adds in chunk order.  No
 // atomics: each S entry has a single writer.
-constexpr int kPairChunk = 64;
+constexpr int kPairChunk = 128;
 struct PairItem {
   uint32_t key, begin, end;
   int32_t slot;  // -1: write S directly; else the partial-sum slot
@@ -529,6 +697,32 @@ __device__ __forceinline__ void write_block(uint32_t ca, uint32_t cb, const T* a
   }
 }
 
+// Register tiling of one B x B camera-pair block over a warp: lane t of a
+// group owns the 3x3 output tile (ti, tj) = (t / TPD, t % TPD).  When the
+// block needs at most 16 tiles the warp splits into two groups of 16 lanes
+// that take alternate pairs (their sums are added in group order at the end).
+// Staged operands are padded so that a tile's three rows are 16-byte loads:
+// W V^-1 and W as TPD groups of 12 values (3 rows x 3 + 3 padding), Jc as
+// 2 rows x TPD groups of 4 values (3 + 1 padding).
+template <int B>
+struct PairTile {
+  static constexpr int TPD = (B + 2) / 3;
+  static constexpr int NT = TPD * TPD;
+  static constexpr int G = NT <= 16 ? 2 : 1;
+  static constexpr int LPG = NT <= 16 ? 16 : 32;
+  static constexpr int WSZ = TPD * 12;
+  static constexpr int JSZ = 2 * TPD * 4;
+  static constexpr int PSZ = 2 * WSZ + JSZ;
+  static constexpr int VALS = 8 * B;                  // staged values per pair
+  static constexpr int SLOTS = (VALS + 31) / 32;       // per lane
+};
+
+template <typename T>
+__device__ __forceinline__ void lds12(const T* p, T v[12]) {
+#pragma unroll
+  for (int q = 0; q < 3; ++q) ld4<T>(p + 4 * q, v + 4 * q);
+}
+
 template <int B, typename T>
 __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict__ items, int64_t nitems,
                                                      const unsigned long long* __restrict__ pairs,
@@ -537,51 +731,139 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
                                                      const int32_t* __restrict__ cam_group, int K, int64_t nc,
                                                      T* __restrict__ S, int64_t ld, T* __restrict__ partial) {
   using R = Rec<B>;
-  constexpr int E = (B * B + 31) / 32;
-  __shared__ T sh[4][8 * B];  // per warp: Wh_a (3B) | W_b (3B) | Jc_a (2B)
+  using PT = PairTile<B>;
+  constexpr int ST = sizeof(T) == 4 ? 16 : 8;  // pairs per stage
+  __shared__ __align__(16) T sh[4][ST * PT::PSZ];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (w >= nitems) return;
   const PairItem it = items[w];
-  T acc[E];
-#pragma unroll
-  for (int e = 0; e < E; ++e) acc[e] = T(0);
   T* sw = sh[warp];
-  for (uint32_t q = it.begin; q < it.end; ++q) {
-    const unsigned long long pr = pairs[q];
-    const uint32_t a = (uint32_t)(pr >> 32), b = (uint32_t)(pr & 0xffffffffu);
-    const T* ra = rec + (int64_t)a * R::kSize;
-    const T* rb = rec + (int64_t)b * R::kSize;
-    for (int i = lane; i < 3 * B; i += 32) {
-      sw[i] = ra[R::kWh + i];
-      sw[3 * B + i] = rb[R::kW + i];
-    }
-    const bool same = a == b;
-    if (same)
-      for (int i = lane; i < 2 * B; i += 32) sw[6 * B + i] = ra[R::kJc + i];
-    __syncwarp();
+  // this lane's staging slots: source offset in the a- or b-record, destination
+  int src[PT::SLOTS], dst[PT::SLOTS], kind[PT::SLOTS];  // kind: 0 = a (W V^-1), 1 = b (W), 2 = a (Jc), 3 = none
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int idx = lane + 32 * e;
-      if (idx < B * B) {
-        const int i = idx / B, j = idx % B;
-        T v = -(sw[3 * i] * sw[3 * B + 3 * j] + sw[3 * i + 1] * sw[3 * B + 3 * j + 1] + sw[3 * i + 2] * sw[3 * B + 3 * j + 2]);
-        if (same) v += sw[6 * B + i] * sw[6 * B + j] + sw[7 * B + i] * sw[7 * B + j];
-        acc[e] += v;
+  for (int u = 0; u < PT::SLOTS; ++u) {
+    const int f = lane + 32 * u;
+    if (f < 3 * B) {
+      const int i = f / 3, k = f % 3;
+      kind[u] = 0;
+      src[u] = R::kWh + f;
+      dst[u] = (i / 3) * 12 + (i % 3) * 3 + k;
+    } else if (f < 6 * B) {
+      const int g = f - 3 * B, i = g / 3, k = g % 3;
+      kind[u] = 1;
+      src[u] = R::kW + g;
+      dst[u] = PT::WSZ + (i / 3) * 12 + (i % 3) * 3 + k;
+    } else if (f < 8 * B) {
+      const int g = f - 6 * B, r = g / B, i = g % B;
+      kind[u] = 2;
+      src[u] = R::kJc + g;
+      dst[u] = 2 * PT::WSZ + r * PT::TPD * 4 + (i / 3) * 4 + i % 3;
+    } else {
+      kind[u] = 3;
+      src[u] = 0;
+      dst[u] = 0;
+    }
+  }
+  const int grp = lane / PT::LPG, t = lane % PT::LPG;
+  const bool active = grp < PT::G && t < PT::NT;
+  const int ti = active ? t / PT::TPD : 0, tj = active ? t % PT::TPD : 0;
+  T acc[3][3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[r][c] = T(0);
+  // Software pipeline: the loads of stage s+1 are issued before stage s is
+  // multiplied out of shared memory.
+  T v[ST][PT::SLOTS];
+  auto stage_load = [&](uint32_t q0) {
+    const int n = (int)min((uint32_t)ST, it.end - q0);
+#pragma unroll
+    for (int q = 0; q < ST; ++q) {
+      if (q < n) {
+        const unsigned long long pr = pairs[q0 + q];
+        const uint32_t a = (uint32_t)(pr >> 32), b = (uint32_t)(pr & 0xffffffffu);
+        const T* ra = rec + (int64_t)a * R::kSize;
+        const T* rb = rec + (int64_t)b * R::kSize;
+#pragma unroll
+        for (int u = 0; u < PT::SLOTS; ++u) {
+          if (kind[u] == 0 || (kind[u] == 2 && a == b)) v[q][u] = ra[src[u]];
+          else if (kind[u] == 1) v[q][u] = rb[src[u]];
+        }
       }
     }
-    __syncwarp();
-  }
-  if (it.slot >= 0) {
-    T* out = partial + (int64_t)it.slot * B * B;
+  };
+  auto stage_store = [&](uint32_t q0) {
+    const int n = (int)min((uint32_t)ST, it.end - q0);
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int idx = lane + 32 * e;
-      if (idx < B * B) out[idx] = acc[e];
+    for (int q = 0; q < ST; ++q)
+      if (q < n) {
+#pragma unroll
+        for (int u = 0; u < PT::SLOTS; ++u)
+          if (kind[u] != 3) sw[q * PT::PSZ + dst[u]] = v[q][u];
+      }
+  };
+  if (it.begin < it.end) stage_load(it.begin);
+  for (uint32_t q0 = it.begin; q0 < it.end; q0 += ST) {
+    const int n = (int)min((uint32_t)ST, it.end - q0);
+    __syncwarp();
+    stage_store(q0);
+    __syncwarp();
+    if (q0 + ST < it.end) stage_load(q0 + ST);
+    if (active) {
+      for (int q = grp; q < n; q += PT::G) {
+        const unsigned long long pr = pairs[q0 + q];
+        const T* sp = sw + q * PT::PSZ;
+        T A[12], Bv[12];
+        lds12<T>(sp + ti * 12, A);
+        lds12<T>(sp + PT::WSZ + tj * 12, Bv);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int c = 0; c < 3; ++c)
+            acc[r][c] -= A[3 * r] * Bv[3 * c] + A[3 * r + 1] * Bv[3 * c + 1] + A[3 * r + 2] * Bv[3 * c + 2];
+        if ((uint32_t)(pr >> 32) == (uint32_t)(pr & 0xffffffffu)) {
+          T ja0[4], ja1[4], jb0[4], jb1[4];
+          ld4<T>(sp + 2 * PT::WSZ + ti * 4, ja0);
+          ld4<T>(sp + 2 * PT::WSZ + PT::TPD * 4 + ti * 4, ja1);
+          ld4<T>(sp + 2 * PT::WSZ + tj * 4, jb0);
+          ld4<T>(sp + 2 * PT::WSZ + PT::TPD * 4 + tj * 4, jb1);
+#pragma unroll
+          for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) acc[r][c] += ja0[r] * jb0[c] + ja1[r] * jb1[c];
+        }
+      }
     }
-    return;
   }
-  write_block<B, T>((uint32_t)(it.key / nc), (uint32_t)(it.key % nc), acc, lane, ext_col, intr_col, cam_group, K, S, ld);
+  if (PT::G == 2) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[r][c] += __shfl_down_sync(0xffffffffu, acc[r][c], 16);
+  }
+  if (!active || grp != 0) return;
+  const uint32_t ca = (uint32_t)(it.key / nc), cb = (uint32_t)(it.key % nc);
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    const int i = 3 * ti + r;
+    if (i >= B) continue;
+    const int ci = it.slot >= 0 ? 0 : cam_col(ext_col, intr_col, cam_group, K, ca, i);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int j = 3 * tj + c;
+      if (j >= B) continue;
+      if (it.slot >= 0) {
+        partial[(int64_t)it.slot * B * B + i * B + j] = acc[r][c];
+        continue;
+      }
+      const int cj = cam_col(ext_col, intr_col, cam_group, K, cb, j);
+      if (ci < 0 || cj < 0) continue;
+      if (ca == cb && ci < cj) continue;
+      if (ci >= cj) S[(int64_t)ci * ld + cj] += acc[r][c];
+      else S[(int64_t)cj * ld + ci] += acc[r][c];
+    }
+  }
 }
 
 // Sum of a chunked block's partials in chunk order, written into S.
@@ -983,10 +1265,12 @@ __global__ void k_cam_scatter(const uint32_t* cam, int64_t no, const uint32_t* o
 //   y_p = V^-1 (g_p - sum E'F z), step = -(z, y), m = J step,
 //   model_cost_change += -m.(r + m/2), candidate points.
 template <int B, typename T>
-__global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ cam,
+__global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ pt,
+                                                     const uint32_t* __restrict__ pt_grp, int64_t n_groups,
+                                                     const uint32_t* __restrict__ cam,
                                                      const int32_t* __restrict__ ext_col,
                                                      const int32_t* __restrict__ intr_col,
-                                                     const int32_t* __restrict__ cam_group, int K, int64_t np,
+                                                     const int32_t* __restrict__ cam_group, int K,
                                                      const T* __restrict__ rec, const T* __restrict__ z,
                                                      const T* __restrict__ Vinv, const T* __restrict__ gp,
                                                      const double* __restrict__ scale_p, const double* __restrict__ pts,
@@ -995,59 +1279,112 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
   using R = Rec<B>;
   __shared__ double smcc[4], sstep[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   double mcc = 0.0, stp = 0.0;
-  if (p < np) {
-    const uint32_t ob = pt_off[p], oe = pt_off[p + 1];
-    T t[3] = {};
-    for (uint32_t o = ob + lane; o < oe; o += 32) {
+  // F z of one observation: the camera block's part of J step
+  auto fz = [&](const T* r, uint32_t c, T& f0, T& f1) {
+    f0 = T(0);
+    f1 = T(0);
+#pragma unroll
+    for (int i = 0; i < B; ++i) {
+      const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
+      const T zi = ci >= 0 ? z[ci] : T(0);
+      f0 += r[R::kJc + i] * zi;
+      f1 += r[R::kJc + B + i] * zi;
+    }
+  };
+  // model cost change of one observation, m = -(F z + E y): m in the compute
+  // type (the Jacobian's own precision), -m.(r + m/2) in FP64
+  auto obs_mcc = [&](const T* r, uint32_t c, const T y[3]) {
+    T f0, f1;
+    fz(r, c, f0, f1);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      f0 += r[R::kJp + j] * y[j];
+      f1 += r[R::kJp + 3 + j] * y[j];
+    }
+    const double m0 = -(double)f0, m1 = -(double)f1;
+    const double r0 = (double)r[R::kR], r1 = (double)r[R::kR + 1];
+    return -(m0 * (r0 + m0 / 2.0) + m1 * (r1 + m1 / 2.0));
+  };
+  // y_p = V^-1 (g_p - E^T F z) and the candidate point
+  auto point_step = [&](uint32_t p, const T t[3], T y[3]) {
+    const T* vi = Vinv + 6 * (int64_t)p;
+    const T q0 = gp[3 * (int64_t)p] - t[0], q1 = gp[3 * (int64_t)p + 1] - t[1], q2 = gp[3 * (int64_t)p + 2] - t[2];
+    y[0] = vi[0] * q0 + vi[1] * q1 + vi[2] * q2;
+    y[1] = vi[1] * q0 + vi[3] * q1 + vi[4] * q2;
+    y[2] = vi[2] * q0 + vi[4] * q1 + vi[5] * q2;
+  };
+  if (w < n_groups) {
+    const uint32_t p0 = pt_grp[w], p1 = pt_grp[w + 1];
+    const uint32_t o0 = pt_off[p0], o1 = pt_off[p1];
+    if (p1 - p0 > 1 || (o1 - o0 >= 1 && o1 - o0 <= 32)) {
+      // packed: lane i holds observation o0 + i
+      const uint32_t o = o0 + lane;
+      const bool valid = o < o1;
+      T t[3] = {T(0), T(0), T(0)};
+      uint32_t p = 0, c = 0;
+      int head = lane, tail = lane;
       const T* r = rec + (int64_t)o * R::kSize;
-      const uint32_t c = cam[o];
-      T fz0 = T(0), fz1 = T(0);
+      if (valid) {
+        c = cam[o];
+        p = pt[o];
+        head = (int)(pt_off[p] - o0);
+        tail = (int)(pt_off[p + 1] - o0) - 1;
+        T f0, f1;
+        fz(r, c, f0, f1);
 #pragma unroll
-      for (int i = 0; i < B; ++i) {
-        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
-        const T zi = ci >= 0 ? z[ci] : T(0);
-        fz0 += r[R::kJc + i] * zi;
-        fz1 += r[R::kJc + B + i] * zi;
+        for (int j = 0; j < 3; ++j) t[j] = r[R::kJp + j] * f0 + r[R::kJp + 3 + j] * f1;
       }
 #pragma unroll
-      for (int j = 0; j < 3; ++j) t[j] += r[R::kJp + j] * fz0 + r[R::kJp + 3 + j] * fz1;
-    }
+      for (int d = 1; d < 32; d <<= 1) {
+        const bool take = lane - d >= head;
 #pragma unroll
-    for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
-    const T* vi = Vinv + 6 * p;
-    const T q0 = gp[3 * p] - t[0], q1 = gp[3 * p + 1] - t[1], q2 = gp[3 * p + 2] - t[2];
-    const T y[3] = {vi[0] * q0 + vi[1] * q1 + vi[2] * q2, vi[1] * q0 + vi[3] * q1 + vi[4] * q2,
-                    vi[2] * q0 + vi[4] * q1 + vi[5] * q2};
-    if (!isfinite((double)y[0]) || !isfinite((double)y[1]) || !isfinite((double)y[2])) {
-      if (lane == 0) atomicExch(flag, 3);
-    }
-    for (uint32_t o = ob + lane; o < oe; o += 32) {
-      const T* r = rec + (int64_t)o * R::kSize;
-      const uint32_t c = cam[o];
-      double m0 = 0.0, m1 = 0.0;
-#pragma unroll
-      for (int i = 0; i < B; ++i) {
-        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
-        const double zi = ci >= 0 ? (double)z[ci] : 0.0;
-        m0 += (double)r[R::kJc + i] * zi;
-        m1 += (double)r[R::kJc + B + i] * zi;
+        for (int j = 0; j < 3; ++j) {
+          const T y = __shfl_up_sync(0xffffffffu, t[j], d);
+          if (take) t[j] += y;
+        }
       }
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        m0 += (double)r[R::kJp + j] * (double)y[j];
-        m1 += (double)r[R::kJp + 3 + j] * (double)y[j];
+      for (int j = 0; j < 3; ++j) t[j] = __shfl_sync(0xffffffffu, t[j], tail);
+      if (valid) {
+        T y[3];
+        point_step(p, t, y);
+        mcc = obs_mcc(r, c, y);
+        if (lane == head) {
+          if (!isfinite(y[0]) || !isfinite(y[1]) || !isfinite(y[2])) atomicExch(flag, 3);
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            const double d = -(double)y[j] * scale_p[3 * (int64_t)p + j];
+            pts_new[3 * (int64_t)p + j] = pts[3 * (int64_t)p + j] + d;
+            stp += d * d;
+          }
+        }
       }
-      m0 = -m0;
-      m1 = -m1;
-      const double r0 = (double)r[R::kR], r1 = (double)r[R::kR + 1];
-      mcc += -(m0 * (r0 + m0 / 2.0) + m1 * (r1 + m1 / 2.0));
-    }
-    if (lane < 3) {
-      const double d = -(double)y[lane] * scale_p[3 * p + lane];
-      pts_new[3 * p + lane] = pts[3 * p + lane] + d;
-      stp = d * d;
+    } else {
+      // one point (no observation, or more than 32)
+      const uint32_t p = p0;
+      T t[3] = {T(0), T(0), T(0)};
+      for (uint32_t o = o0 + lane; o < o1; o += 32) {
+        const T* r = rec + (int64_t)o * R::kSize;
+        T f0, f1;
+        fz(r, cam[o], f0, f1);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] += r[R::kJp + j] * f0 + r[R::kJp + 3 + j] * f1;
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+      T y[3];
+      point_step(p, t, y);
+      if (!isfinite(y[0]) || !isfinite(y[1]) || !isfinite(y[2])) {
+        if (lane == 0) atomicExch(flag, 3);
+      }
+      for (uint32_t o = o0 + lane; o < o1; o += 32) mcc += obs_mcc(rec + (int64_t)o * R::kSize, cam[o], y);
+      if (lane < 3) {
+        const double d = -(double)y[lane] * scale_p[3 * (int64_t)p + lane];
+        pts_new[3 * (int64_t)p + lane] = pts[3 * (int64_t)p + lane] + d;
+        stp = d * d;
+      }
     }
   }
   mcc = warp_sum(mcc);
@@ -1173,6 +1510,18 @@ __global__ void k_cam_candidate(const double* ext, const double* intr, double* e
   }
 }
 
+// FP64 camera poses of ext (one thread per camera).
+__global__ void k_cam_pose(const double* __restrict__ ext, int64_t nc, double* __restrict__ pose) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double E[6], q[12];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) E[i] = ext[6 * c + i];
+  pose_matrix<double>(E, q);
+#pragma unroll
+  for (int i = 0; i < 12; ++i) pose[12 * c + i] = q[i];
+}
+
 // FP64 robustified cost 1/2 sum rho(|r|^2) at (ext, intr, pts); per-block partials.
 template <int M>
 __global__ void __launch_bounds__(256) k_cost(Prob P, const double* ext, const double* intr, const double* pts,
@@ -1190,8 +1539,12 @@ __global__ void __launch_bounds__(256) k_cost(Prob P, const double* ext, const d
 #pragma unroll
     for (int i = 0; i < 3; ++i) X[i] = __ldg(&pts[3 * (int64_t)p + i]);
     const double2 ob = P.obs[o];
-    double dJe[2][6], dJk[2][K], dJx[2][3];
-    residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    if (P.pose) {
+      residual_pose<M, double>(Kp, P.pose + 12 * (int64_t)c, X, ob.x, ob.y, r);
+    } else {
+      double dJe[2][6], dJk[2][K], dJx[2][3];
+      residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    }
     double sr1;
     const double cst = robust<double>(P.loss_type, P.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
     if (!isfinite(cst)) atomicExch(nonfinite, 1);
@@ -1265,6 +1618,10 @@ struct Solve {
   int precision;
   // device arrays
   double *ext, *intr, *pts, *ext2, *intr2, *pts2;
+  double *pose = nullptr, *pose2 = nullptr;  // FP64 poses of ext / ext2 (mixed path)
+  uint32_t *pt_grp = nullptr, *pgrp_cnt = nullptr, *pgrp_off = nullptr;  // point groups (k_pt_groups)
+  int64_t n_pgrp = 0;
+  int nb_pgrp = 1;  // blocks of the per-group kernels (4 groups per block)
   double2* obs;
   uint32_t *cam, *icam, *pt, *pt_off;
   int32_t *ext_col, *intr_col;
@@ -1313,6 +1670,7 @@ static Prob make_prob(const Solve& s, const double* ext, const double* intr, con
   P.no = s.no;
   P.loss_type = o ? o->loss_type : 0;
   P.loss_a = o ? o->loss_scale : 1.0;
+  P.pose = nullptr;
   return P;
 }
 
@@ -1323,6 +1681,8 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.intr = a.template take<double>(s.k * s.ni);
   s.pts = a.template take<double>(3 * s.np);
   s.ext2 = a.template take<double>(6 * s.nc);
+  s.pose = a.template take<double>(12 * s.nc);
+  s.pose2 = a.template take<double>(12 * s.nc);
   s.intr2 = a.template take<double>(s.k * s.ni);
   s.pts2 = a.template take<double>(3 * s.np);
   s.obs = a.template take<double2>(s.no);
@@ -1330,6 +1690,9 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.icam = a.template take<uint32_t>(s.no);
   s.pt = a.template take<uint32_t>(s.no);
   s.pt_off = a.template take<uint32_t>(s.np + 1);
+  s.pt_grp = a.template take<uint32_t>(s.np + 1);
+  s.pgrp_cnt = a.template take<uint32_t>(ceil_div(s.np, kGroupChunk) + 1);
+  s.pgrp_off = a.template take<uint32_t>(ceil_div(s.np, kGroupChunk) + 1);
   s.ext_col = a.template take<int32_t>(6 * s.nc);
   s.intr_col = a.template take<int32_t>(s.k * s.ni);
   s.intr_var = a.template take<uint8_t>(s.ni);
@@ -1497,6 +1860,21 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   check_launch(h);
   k_gather<<<grid, 256, 0, st>>>(perm, no, obs_in, idx_in, idx_in + no, idx_in + 2 * no, s.obs, s.cam, s.icam, s.pt);
   check_launch(h);
+  // point groups of the Schur point kernel
+  if (np > 0) {
+    const int64_t nch = ceil_div(np, kGroupChunk);
+    const unsigned gb = (unsigned)ceil_div(nch, 128);
+    k_pt_groups<<<gb, 128, 0, st>>>(s.pt_off, np, nullptr, s.pgrp_cnt, 0);
+    check_launch(h);
+    scan_offsets(h, s.pgrp_cnt, s.pgrp_off, nch, chunks, st);
+    k_pt_groups<<<gb, 128, 0, st>>>(s.pt_off, np, s.pgrp_off, s.pt_grp, 1);
+    check_launch(h);
+    uint32_t ng = 0;
+    GBBA_CUDA(cudaMemcpyAsync(&ng, s.pgrp_off + nch, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    s.n_pgrp = ng;
+    s.nb_pgrp = (int)std::max<int64_t>(1, ceil_div(s.n_pgrp * 32, 128));
+  }
   copy_in(s.ext, P->extrinsics, sizeof(double) * 6 * nc, P->memory, st);
   copy_in(s.intr, P->intrinsics, sizeof(double) * s.k * ni, P->memory, st);
   copy_in(s.pts, P->points, sizeof(double) * 3 * np, P->memory, st);
@@ -1832,14 +2210,29 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   double* pin = h->pinned;
   const int gx = s.nb_x;
 
+  // The mixed path evaluates its FP64 residuals from per-camera FP64 poses
+  // (a 3x3 product per observation instead of the Rodrigues sine/cosine):
+  // s.pose for the current parameters, s.pose2 for the evaluated ones.
+  constexpr bool kPose = sizeof(T) == 4;
+  const unsigned nb_cam_pose = (unsigned)std::max<int64_t>(1, ceil_div(s.nc, 128));
   auto launch_cost = [&](const double* e, const double* i, const double* p) {
     Prob Pc = make_prob(s, e, i, p, o);
+    if (kPose && s.nc > 0) {
+      k_cam_pose<<<nb_cam_pose, 128, 0, st>>>(e, s.nc, s.pose2);
+      check_launch(h);
+      Pc.pose = s.pose2;
+    }
     k_cost<M><<<s.nb_obs, 256, 0, st>>>(Pc, e, i, p, s.part_cost, s.nonfinite);
     check_launch(h);
   };
   // gradient max norm and x norm at the current point; scale on first use
   auto linearize = [&](bool first, double* gmax, double* xnorm) {
     Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
+    if (kPose && s.nc > 0) {
+      k_cam_pose<<<nb_cam_pose, 128, 0, st>>>(s.ext, s.nc, s.pose);
+      check_launch(h);
+      P.pose = s.pose;
+    }
     GBBA_CUDA(cudaMemsetAsync(s.cn_c, 0, sizeof(double) * (s.n_red + 1), st));
     GBBA_CUDA(cudaMemsetAsync(s.g_c, 0, sizeof(double) * (s.n_red + 1), st));
     GBBA_CUDA(cudaMemsetAsync(s.cn_p, 0, sizeof(double) * 3 * s.np, st));
@@ -1904,7 +2297,9 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   // candidate is written to s.ext2/s.intr2/s.pts2 (an accepted candidate is
   // copied back), so the sequence is invariant and is captured once into CUDA
   // graphs that every iteration replays.
-  const Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
+  Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
+  if (kPose && s.nc > 0) P.pose = s.pose;
+  const int nb_back = s.pair_path ? s.nb_pgrp : s.nb_pt;  // blocks (partials) of the back substitution  // refreshed by linearize() after every accepted step
   auto record_phase = [&](int ph) {
     switch (ph) {
       case 0:
@@ -1920,7 +2315,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       case 1:
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
-          k_schur_point_rec<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, s.diag_p, s.radius, (T*)s.Vinv,
+          k_schur_point_rec<M, T><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
+              P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, s.radius, (T*)s.Vinv,
                                                             (T*)s.gpv, (T*)s.rec, s.flag);
           check_launch(h);
           if (s.dense && s.n_blocks > 0) {
@@ -1957,9 +2353,10 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       case 3:
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
-          k_backsub_rec<B, T><<<s.nb_pt, 128, 0, st>>>(s.pt_off, s.cam, s.ext_col, s.intr_col, s.cam_group, s.k, s.np,
-                                                       (const T*)s.rec, z, (const T*)s.Vinv, (const T*)s.gpv,
-                                                       s.scale_p, s.pts, s.pts2, s.part_mcc, s.part_step_p, s.flag);
+          k_backsub_rec<B, T><<<s.nb_pgrp, 128, 0, st>>>(s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, s.ext_col,
+                                                         s.intr_col, s.cam_group, s.k, (const T*)s.rec, z,
+                                                         (const T*)s.Vinv, (const T*)s.gpv, s.scale_p, s.pts, s.pts2,
+                                                         s.part_mcc, s.part_step_p, s.flag);
           check_launch(h);
         } else if (s.np > 0) {
           k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2,
@@ -1972,7 +2369,7 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
         break;
       default:
         launch_cost(s.ext2, s.intr2, s.pts2);
-        k_reduce3<<<1, 256, 0, st>>>(s.part_mcc, s.np > 0 ? s.nb_pt : 0, s.part_step_p, s.np > 0 ? s.nb_pt : 0,
+        k_reduce3<<<1, 256, 0, st>>>(s.part_mcc, s.np > 0 ? nb_back : 0, s.part_step_p, s.np > 0 ? nb_back : 0,
                                      s.part_step_c, s.nb_cam, s.part_cost, s.nb_obs, s.scalars);
         check_launch(h);
         break;
