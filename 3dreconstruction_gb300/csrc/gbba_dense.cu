@@ -62,112 +62,254 @@ __device__ __forceinline__ void load_tile(T (*dst)[NB + 1], const T* __restrict_
   }
 }
 
+// Reciprocal of a pivot.  Single precision uses the fast hardware reciprocal
+// (__fdividef, within 2 ulp for normal pivots): it sits on the elimination's
+// critical path, and the FP32 factor only feeds LM steps whose acceptance is
+// decided on the FP64 cost.  Double precision divides exactly.
+__device__ __forceinline__ float pivot_rcp(float d) { return __fdividef(1.0f, d); }
+__device__ __forceinline__ double pivot_rcp(double d) { return 1.0 / d; }
+
 // Factor the diagonal tile: S_kk = L L^T (written back into S's lower
 // triangle, zeros above), L^-1 (into Linv_all), and y_k = L^-1 b_k.
 //
-// Outer-product LDL^T elimination with the same row operations applied to an
-// identity block E, so that at the end A = L_u D L_u^T and E = L_u^-1 (one
-// pass of 64 pivot steps yields both the factor and its inverse).  Thread
-// (ty, tx) holds rows 4ty..4ty+3 x columns 4tx..4tx+3 of A and of E in
-// registers.  At pivot j the owners of column j publish it with zeros at and
-// above the pivot, the owners of row j of E publish that row (exactly zero
-// right of the diagonal), and the diagonal owner publishes 1/d_j; every
-// thread then applies a_il -= (c_i/d_j) c_l and e_il -= (c_i/d_j) E_jl to its
-// whole block, with no predicates: the zeros leave finished columns, rows
-// above the pivot and the zero part of E unchanged.
+// Blocked right-looking factorisation of the 64 x 64 tile in shared memory
+// over four 16-column panels p (offset o = 16p):
+//   1. warp 0 factors the 16 x 16 diagonal block: outer-product LDL^T with
+//      the same row operations applied to an identity block E (so that
+//      E = L_u^-1 at the end); lane (r, h) holds row r, columns 8h..8h+7 of
+//      both in registers, pivots are broadcast through shared memory with
+//      only __syncwarp between steps;
+//   2. panel solve  L_ip = A_ip L_pp^-T  for the rows below (all threads);
+//   3. trailing update  A_il -= L_ip L_lp^T  inside the tile (all threads);
+// then the off-diagonal 16 x 16 blocks of L^-1 by increasing distance from
+// the diagonal,  Li_IJ = -Li_II sum_{K=J..I-1} L_IK Li_KJ,  and y = L^-1 b.
+// A non-positive (or non-finite) pivot is replaced by 1 and sets *flag.
+constexpr int kPotrfThreads = 256;
+constexpr int kTileLd = NB + 4;  // 16-byte aligned rows
 template <typename T>
-__global__ void __launch_bounds__(256) k_potrf_diag(T* __restrict__ S, int64_t ld, int kb, T* __restrict__ Linv_all,
-                                                    T* __restrict__ b, int* __restrict__ flag) {
-  constexpr int BS = NB + 4;  // 16-byte aligned broadcast rows
-  T* colbuf = &tile_at<T>(1)[0][0];  // [2][BS]: column j of A (double-buffered)
-  T* rowbuf = colbuf + 2 * BS;       // [2][BS]: row j of E
-  T* rpiv = rowbuf + 2 * BS;         // [2]: 1 / d_j
-  T* part = &tile_at<T>(0)[0][0];    // 64 x 16 partial sums of L^-1 b
-  T* yb = vec_at<T>(0);
-  T* dv = vec_at<T>(1);
-  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+constexpr size_t potrf_smem_bytes() {
+  return sizeof(T) * ((size_t)2 * NB * kTileLd   // A / L, L^-1
+                      + 3 * 16 * 16              // scratch of the inverse blocks
+                      + 4 * 16 + 4               // warp-0 broadcast buffers
+                      + 2 * NB);                 // b, pivots
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPotrfThreads) k_potrf_diag(T* __restrict__ S, int64_t ld, int kb,
+                                                              T* __restrict__ Linv_all, T* __restrict__ b,
+                                                              int* __restrict__ flag) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* A = reinterpret_cast<T*>(smem_raw);  // [64][kTileLd]: A, overwritten by L
+  T* Li = A + NB * kTileLd;               // [64][kTileLd]: L^-1
+  T* scr = Li + NB * kTileLd;             // [3][16][16]
+  T* bc = scr + 3 * 256;                  // [2][16] pivot column
+  T* br = bc + 32;                        // [2][16] row of E
+  T* rp = br + 32;                        // [2] 1/d (+2 padding)
+  T* yb = rp + 4;                         // [64]
+  T* dv = yb + NB;                        // [64] pivots of the current panel
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t off = (int64_t)kb * NB;
-  T a[4][4], e[4][4];
+  // load the tile (lower part is what is used), clear L^-1, load b
 #pragma unroll
-  for (int ii = 0; ii < 4; ++ii) {
-    ld4<T>(S + (off + ty * 4 + ii) * ld + off + tx * 4, a[ii]);
-#pragma unroll
-    for (int jj = 0; jj < 4; ++jj) e[ii][jj] = (ty * 4 + ii == tx * 4 + jj) ? T(1) : T(0);
+  for (int it = 0; it < NB * NB / 4 / kPotrfThreads; ++it) {
+    const int idx = tid + it * kPotrfThreads, r = idx >> 4, c = (idx & 15) * 4;
+    T v[4];
+    ld4<T>(S + (off + r) * ld + off + c, v);
+    st4<T>(A + r * kTileLd + c, v);
+    const T z[4] = {T(0), T(0), T(0), T(0)};
+    st4<T>(Li + r * kTileLd + c, z);
   }
   if (tid < NB) yb[tid] = b[off + tid];
-  for (int j4 = 0; j4 < NB; j4 += 4) {
-    const bool col_owner = tx == (j4 >> 2), row_owner = ty == (j4 >> 2);
+  __syncthreads();
+
+  for (int p = 0; p < 4; ++p) {
+    const int o = 16 * p;
+    // ---- 1. diagonal 16 x 16 block, warp 0
+    if (warp == 0) {
+      const int r = lane & 15, h = lane >> 4;
+      T a[8], e[8];
+      ld4<T>(A + (o + r) * kTileLd + o + 8 * h, a);
+      ld4<T>(A + (o + r) * kTileLd + o + 8 * h + 4, a + 4);
 #pragma unroll
-    for (int jc = 0; jc < 4; ++jc) {
-      const int j = j4 + jc;
-      T* cb = colbuf + (j & 1) * BS;
-      T* rb = rowbuf + (j & 1) * BS;
-      if (col_owner) {
-        T c[4];
+      for (int q = 0; q < 8; ++q) e[q] = (r == 8 * h + q) ? T(1) : T(0);
+      // pivot j: lane (i, h') holds a_ij in a[j & 7] when h' = j >> 3, and
+      // row j of E lives in lanes (j, 0) and (j, 1); everything a lane needs
+      // is fetched with independent shuffles (no shared-memory round trip)
 #pragma unroll
-        for (int ii = 0; ii < 4; ++ii) c[ii] = (ty * 4 + ii > j) ? a[ii][jc] : T(0);
-        st4<T>(cb + ty * 4, c);
-        if (row_owner) {
-          T d = a[jc][jc];
-          if (!(d > T(0)) || !isfinite(d)) {
-            d = T(1);
-            atomicExch(flag, 1);
+      for (int j = 0; j < 16; ++j) {
+        const int hs = 16 * (j >> 3);  // lane offset of the owners of column j
+        T d = __shfl_sync(0xffffffffu, a[j & 7], j + hs);
+        const T cr = __shfl_sync(0xffffffffu, a[j & 7], r + hs);
+        T cl[8], rl[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          cl[q] = __shfl_sync(0xffffffffu, a[j & 7], 8 * h + q + hs);
+          rl[q] = __shfl_sync(0xffffffffu, e[q], j + 16 * h);
+        }
+        if (!(d > T(0) && d - d == T(0))) {  // non-positive, NaN or infinite pivot
+          d = T(1);
+          if (lane == 0) atomicExch(flag, 1);
+        }
+        if (lane == 0) dv[o + j] = d;
+        const T m = (r > j) ? cr * pivot_rcp(d) : T(0);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const T c = (8 * h + q > j) ? cl[q] : T(0);
+          a[q] -= m * c;
+          e[q] -= m * rl[q];
+        }
+      }
+      __syncwarp();
+      // L_pp = L_u D^1/2, L_pp^-1 = D^-1/2 E: sqrt(d) and 1/sqrt(d) once per
+      // pivot (lanes 0..15 in parallel), then products only
+      T* sqd = bc;       // [16] sqrt(d), reusing the broadcast buffers
+      T* rsd = bc + 16;  // [16] 1/sqrt(d)
+      if (lane < 16) {
+        const T sd = sqrt(dv[o + lane]);
+        sqd[lane] = sd;
+        rsd[lane] = T(1) / sd;
+      }
+      __syncwarp();
+      const T rr = rsd[r];
+      T rl8[8];
+      ld4<T>(rsd + 8 * h, rl8);
+      ld4<T>(rsd + 8 * h + 4, rl8 + 4);
+      T lv[8], iv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int l = 8 * h + q;
+        lv[q] = (l < r) ? a[q] * rl8[q] : (l == r ? sqd[r] : T(0));
+        iv[q] = (l <= r) ? e[q] * rr : T(0);
+      }
+      st4<T>(A + (o + r) * kTileLd + o + 8 * h, lv);
+      st4<T>(A + (o + r) * kTileLd + o + 8 * h + 4, lv + 4);
+      st4<T>(Li + (o + r) * kTileLd + o + 8 * h, iv);
+      st4<T>(Li + (o + r) * kTileLd + o + 8 * h + 4, iv + 4);
+    }
+    __syncthreads();
+    if (p == 3) break;
+    // ---- 2. panel solve: rows o+16..63, L_ic = sum_k A_ik Li_pp[c][k]
+    const int rows = NB - o - 16;
+    T pv[3];
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int idx = tid + u * kPotrfThreads;
+      pv[u] = T(0);
+      if (idx < rows * 16) {
+        const int i = o + 16 + (idx >> 4), c = idx & 15;
+        T s4[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+        for (int k4 = 0; k4 < 16; k4 += 4) {
+          T av[4], lv[4];
+          ld4<T>(A + i * kTileLd + o + k4, av);
+          ld4<T>(Li + (o + c) * kTileLd + o + k4, lv);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) s4[k] += av[k] * lv[k];
+        }
+        pv[u] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+      const int idx = tid + u * kPotrfThreads;
+      if (idx < rows * 16) A[(o + 16 + (idx >> 4)) * kTileLd + o + (idx & 15)] = pv[u];
+    }
+    __syncthreads();
+    // ---- 3. trailing update inside the tile: 4 x 4 output blocks, lower blocks only
+    {
+      const int nbk = rows / 4;  // 4-row blocks of the trailing part
+      for (int t = tid; t < nbk * nbk; t += kPotrfThreads) {
+        const int bi = t / nbk, bl = t % nbk;
+        if (bl > bi) continue;
+        const int i0 = o + 16 + 4 * bi, l0 = o + 16 + 4 * bl;
+        T acc[4][4] = {};
+#pragma unroll
+        for (int k4 = 0; k4 < 16; k4 += 4) {
+          T xi[4][4], xl[4][4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            ld4<T>(A + (i0 + q) * kTileLd + o + k4, xi[q]);
+            ld4<T>(A + (l0 + q) * kTileLd + o + k4, xl[q]);
           }
-          dv[j] = d;
-          rpiv[j & 1] = T(1) / d;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
+#pragma unroll
+              for (int k = 0; k < 4; ++k) acc[q][w] += xi[q][k] * xl[w][k];
         }
-      }
-      if (row_owner) st4<T>(rb + tx * 4, e[jc]);
-      __syncthreads();
-      const T r = rpiv[j & 1];
-      T ci[4], cl[4], rl[4];
-      ld4<T>(cb + ty * 4, ci);
-      ld4<T>(cb + tx * 4, cl);
-      ld4<T>(rb + tx * 4, rl);
 #pragma unroll
-      for (int ii = 0; ii < 4; ++ii) {
-        const T m = ci[ii] * r;
+        for (int q = 0; q < 4; ++q) {
+          T v[4];
+          ld4<T>(A + (i0 + q) * kTileLd + l0, v);
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          a[ii][jj] -= m * cl[jj];
-          e[ii][jj] -= m * rl[jj];
+          for (int w = 0; w < 4; ++w) v[w] -= acc[q][w];
+          st4<T>(A + (i0 + q) * kTileLd + l0, v);
         }
       }
     }
+    __syncthreads();
   }
-  __syncthreads();
-  if (tid < NB) dv[tid] = sqrt(dv[tid]);
-  __syncthreads();
-  // L_il = a_il / sqrt(d_l) (l < i), L_ii = sqrt(d_i); L^-1 = D^-1/2 E.
-  T sl[4];
-  ld4<T>(dv + tx * 4, sl);
-  T yp[4] = {T(0), T(0), T(0), T(0)};
-  T yv[4];
-  ld4<T>(yb + tx * 4, yv);
+
+  // ---- off-diagonal blocks of L^-1, by distance from the diagonal
+  for (int dist = 1; dist < 4; ++dist) {
+    const int nblk = 4 - dist;  // blocks (J + dist, J), J = 0..nblk-1
+    // T_IJ = sum_{K=J}^{I-1} L_IK Li_KJ
+    for (int idx = tid; idx < nblk * 256; idx += kPotrfThreads) {
+      const int J = idx >> 8, I = J + dist, r = (idx >> 4) & 15, c = idx & 15;
+      T s4[4] = {T(0), T(0), T(0), T(0)};
+      for (int K = J; K < I; ++K) {
+        const T* ar = A + (16 * I + r) * kTileLd + 16 * K;
 #pragma unroll
-  for (int ii = 0; ii < 4; ++ii) {
-    const int i = ty * 4 + ii;
-    const T si = dv[i];
-    T lv[4], iv[4];
+        for (int k4 = 0; k4 < 16; k4 += 4) {
+          T av[4];
+          ld4<T>(ar + k4, av);
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) {
-      const int l = tx * 4 + jj;
-      lv[jj] = (l < i) ? a[ii][jj] / sl[jj] : (l == i ? si : T(0));
-      iv[jj] = (l <= i) ? e[ii][jj] / si : T(0);
-      yp[ii] += iv[jj] * yv[jj];
+          for (int k = 0; k < 4; ++k) s4[k] += av[k] * Li[(16 * K + k4 + k) * kTileLd + 16 * J + c];
+        }
+      }
+      scr[idx] = (s4[0] + s4[1]) + (s4[2] + s4[3]);
     }
-    st4<T>(S + (off + i) * ld + off + tx * 4, lv);
-    st4<T>(Linv_all + (int64_t)kb * NB * NB + i * NB + tx * 4, iv);
+    __syncthreads();
+    // Li_IJ = -Li_II T_IJ
+    for (int idx = tid; idx < nblk * 256; idx += kPotrfThreads) {
+      const int J = idx >> 8, I = J + dist, r = (idx >> 4) & 15, c = idx & 15;
+      T s4[4] = {T(0), T(0), T(0), T(0)};
+      const T* lr = Li + (16 * I + r) * kTileLd + 16 * I;
+#pragma unroll
+      for (int k4 = 0; k4 < 16; k4 += 4) {
+        T lv[4];
+        ld4<T>(lr + k4, lv);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) s4[k] += lv[k] * scr[(J << 8) + (k4 + k) * 16 + c];
+      }
+      Li[(16 * I + r) * kTileLd + 16 * J + c] = -((s4[0] + s4[1]) + (s4[2] + s4[3]));
+    }
+    __syncthreads();
   }
-  // y = L^-1 b: thread (ty, tx) holds the partial sums of its 4x4 block
+
+  // ---- y = L^-1 b (4 threads per row), then write L and L^-1
+  {
+    const int r = tid >> 2, q = tid & 3;
+    T s = T(0);
 #pragma unroll
-  for (int ii = 0; ii < 4; ++ii) part[(ty * 4 + ii) * 16 + tx] = yp[ii];
-  __syncthreads();
-  if (tid < NB) {
-    T y = T(0);
+    for (int c = 0; c < 16; ++c) s += Li[r * kTileLd + 16 * q + c] * yb[16 * q + c];
+    s += __shfl_xor_sync(0xffffffffu, s, 1);
+    s += __shfl_xor_sync(0xffffffffu, s, 2);
+    if (q == 0) b[off + r] = s;
+  }
 #pragma unroll
-    for (int t = 0; t < 16; ++t) y += part[tid * 16 + t];
-    b[off + tid] = y;
+  for (int it = 0; it < NB * NB / 4 / kPotrfThreads; ++it) {
+    const int idx = tid + it * kPotrfThreads, r = idx >> 4, c = (idx & 15) * 4;
+    T v[4], w[4];
+    ld4<T>(A + r * kTileLd + c, v);
+    ld4<T>(Li + r * kTileLd + c, w);
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+      if (c + e > r) v[e] = T(0);
+    st4<T>(S + (off + r) * ld + off + c, v);
+    st4<T>(Linv_all + (int64_t)kb * NB * NB + r * NB + c, w);
   }
 }
 
@@ -258,6 +400,97 @@ __global__ void __launch_bounds__(256) k_syrk(T* __restrict__ S, int64_t ld, int
     }
 }
 
+// Trailing update over 128 x 128 output tiles (2 x 2 tiles of 64):
+// S_IJ -= L_Ik L_Jk^T, K = 64 (panel kb).  blockIdx.x enumerates the lower
+// triangle of 128-tiles over the 64-tiles first..nb-1; at the matrix edge a
+// 128-tile holds one 64-tile row or column (the missing half is zero-filled
+// and not stored), and the quarter of a diagonal 128-tile above the diagonal
+// is not stored.  Operands are staged k-major (X^T, row stride 132) so that a
+// thread's 8 rows and 8 columns at one k are 16-byte shared loads; thread
+// (ty, tx) owns rows 8ty..8ty+7 x columns 8tx..8tx+7 of the output tile.
+constexpr int kWideLd = 2 * NB + 4;
+template <typename T>
+constexpr size_t wide_smem_bytes() { return (size_t)2 * NB * kWideLd * sizeof(T); }
+
+template <typename T>
+__device__ __forceinline__ void load_panel_t(T* __restrict__ dst, const T* __restrict__ S, int64_t ld, int64_t row0,
+                                             int64_t col0, int valid_rows, int tid) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::n, ITER = 2 * NB * NB / W / 256;
+  V v[ITER];
+#pragma unroll
+  for (int it = 0; it < ITER; ++it) {
+    const int idx = tid + it * 256, kv = idx / (2 * NB), r = idx % (2 * NB);
+    if (r < valid_rows) v[it] = *reinterpret_cast<const V*>(S + (row0 + r) * ld + col0 + kv * W);
+    else {
+      T* z = reinterpret_cast<T*>(&v[it]);
+#pragma unroll
+      for (int w = 0; w < W; ++w) z[w] = T(0);
+    }
+  }
+#pragma unroll
+  for (int it = 0; it < ITER; ++it) {
+    const int idx = tid + it * 256, kv = idx / (2 * NB), r = idx % (2 * NB);
+    const T* e = reinterpret_cast<const T*>(&v[it]);
+#pragma unroll
+    for (int w = 0; w < W; ++w) dst[(kv * W + w) * kWideLd + r] = e[w];
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_syrk_wide(T* __restrict__ S, int64_t ld, int kb, int first, int nb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* XiT = reinterpret_cast<T*>(smem_raw);
+  T* XjT = XiT + NB * kWideLd;
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int64_t t = blockIdx.x;
+  int64_t R = (int64_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while ((R + 1) * (R + 2) / 2 <= t) ++R;
+  while (R * (R + 1) / 2 > t) --R;
+  const int64_t C = t - R * (R + 1) / 2;
+  const int64_t ib0 = first + 2 * R, jb0 = first + 2 * C;
+  const int rows_i = ib0 + 1 < nb ? 2 * NB : NB, rows_j = jb0 + 1 < nb ? 2 * NB : NB;
+  const int64_t c0 = (int64_t)kb * NB;
+  load_panel_t<T>(XiT, S, ld, ib0 * NB, c0, rows_i, tid);
+  load_panel_t<T>(XjT, S, ld, jb0 * NB, c0, rows_j, tid);
+  __syncthreads();
+  // rows {4ty+i, 64+4ty+i} x columns {4tx+j, 64+4tx+j}: the 16-byte shared
+  // loads of a quarter warp cover 128 contiguous bytes (no bank conflicts)
+  T acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+#pragma unroll 4
+  for (int k = 0; k < NB; ++k) {
+    T xa[8], xb[8];
+    ld4<T>(XiT + k * kWideLd + ty * 4, xa);
+    ld4<T>(XiT + k * kWideLd + NB + ty * 4, xa + 4);
+    ld4<T>(XjT + k * kWideLd + tx * 4, xb);
+    ld4<T>(XjT + k * kWideLd + NB + tx * 4, xb + 4);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] += xa[i] * xb[j];
+  }
+#pragma unroll
+  for (int qi = 0; qi < 2; ++qi)
+#pragma unroll
+    for (int qj = 0; qj < 2; ++qj) {
+      const int64_t rb = ib0 + qi, cb = jb0 + qj;
+      if (rb >= nb || cb >= nb || rb < cb) continue;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        T* p = S + (rb * NB + ty * 4 + i) * ld + cb * NB + tx * 4;
+        T v[4];
+        ld4<T>(p, v);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] -= acc[4 * qi + i][4 * qj + j];
+        st4<T>(p, v);
+      }
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64_t ld, int kb, const T* __restrict__ Linv_all,
                                                   T* __restrict__ b, T* __restrict__ x) {
@@ -305,10 +538,13 @@ void dense_cholesky_prepare() {
   static bool configured = false;
   if (configured) return;
   const int sm = (int)dense_smem_bytes<T>();
-  GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)potrf_smem_bytes<T>()));
   GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   GBBA_CUDA(cudaFuncSetAttribute(k_syrk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+  GBBA_CUDA(cudaFuncSetAttribute(k_syrk_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)wide_smem_bytes<T>()));
   configured = true;
 }
 
@@ -316,10 +552,11 @@ void dense_cholesky_prepare() {
 // attribute is kept when the launch is captured into a graph), so that the
 // one-CTA diagonal factor is scheduled ahead of the trailing update's CTAs.
 template <typename... Exp, typename... Act>
-void launch_hi(gbba_handle* h, void (*k)(Exp...), unsigned grid, size_t smem, cudaStream_t st, Act... args) {
+void launch_hi(gbba_handle* h, void (*k)(Exp...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+               Act... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(256);
+  cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
   cudaLaunchAttribute at[1];
@@ -346,8 +583,8 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
   const int nb = (int)(n_pad / NB);
   const size_t sm = dense_smem_bytes<T>();
   dense_cholesky_prepare<T>();
-  launch_hi(h, k_potrf_diag<T>, 1, sm, st, S, n_pad, 0, Linv_all, b, flag);
-  if (nb > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(nb - 1), sm, st, S, n_pad, 0, (const T*)Linv_all, b);
+  launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, potrf_smem_bytes<T>(), st, S, n_pad, 0, Linv_all, b, flag);
+  if (nb > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(nb - 1), 256, sm, st, S, n_pad, 0, (const T*)Linv_all, b);
   bool side_pending = false;
   for (int k = 0; k + 1 < nb; ++k) {
     const int rem = nb - k - 1;  // tiles below the diagonal in column k
@@ -358,15 +595,15 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
     if (rem > 1) {
       GBBA_CUDA(cudaEventRecord(h->ev_main, st));
       GBBA_CUDA(cudaStreamWaitEvent(h->side, h->ev_main, 0));
-      const int64_t tiles = (int64_t)(rem - 1) * rem / 2;
-      k_syrk<T><<<(unsigned)tiles, 256, sm, h->side>>>(S, n_pad, k, k + 2, 0);
+      const int64_t tw = (rem - 1 + 1) / 2;  // 128-tiles per side over the 64-tiles k+2..nb-1
+      k_syrk_wide<T><<<(unsigned)(tw * (tw + 1) / 2), 256, wide_smem_bytes<T>(), h->side>>>(S, n_pad, k, k + 2, nb);
       check_launch(h);
       GBBA_CUDA(cudaEventRecord(h->ev_side, h->side));
       side_pending = true;
     }
-    launch_hi(h, k_syrk<T>, (unsigned)rem, sm, st, S, n_pad, k, k + 1, 1);
-    launch_hi(h, k_potrf_diag<T>, 1, sm, st, S, n_pad, k + 1, Linv_all, b, flag);
-    if (rem > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(rem - 1), sm, st, S, n_pad, k + 1, (const T*)Linv_all, b);
+    launch_hi(h, k_syrk<T>, (unsigned)rem, 256, sm, st, S, n_pad, k, k + 1, 1);
+    launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, potrf_smem_bytes<T>(), st, S, n_pad, k + 1, Linv_all, b, flag);
+    if (rem > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(rem - 1), 256, sm, st, S, n_pad, k + 1, (const T*)Linv_all, b);
   }
   if (side_pending) GBBA_CUDA(cudaStreamWaitEvent(st, h->ev_side, 0));
   for (int kb = nb - 1; kb >= 0; --kb) {
