@@ -97,7 +97,7 @@ constexpr size_t potrf_smem_bytes() {
 template <typename T>
 __global__ void __launch_bounds__(kPotrfThreads) k_potrf_diag(T* __restrict__ S, int64_t ld, int kb,
                                                               T* __restrict__ Linv_all, T* __restrict__ b,
-                                                              int* __restrict__ flag) {
+                                                              int* __restrict__ flag, int upd) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* A = reinterpret_cast<T*>(smem_raw);  // [64][kTileLd]: A, overwritten by L
   T* Li = A + NB * kTileLd;               // [64][kTileLd]: L^-1
@@ -109,17 +109,57 @@ __global__ void __launch_bounds__(kPotrfThreads) k_potrf_diag(T* __restrict__ S,
   T* dv = yb + NB;                        // [64] pivots of the current panel
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t off = (int64_t)kb * NB;
-  // load the tile (lower part is what is used), clear L^-1, load b
+  // load the tile (lower part is what is used) and b; with upd, also the
+  // previous panel's block P = L_{kb,kb-1} (staged in the L^-1 buffer)
 #pragma unroll
   for (int it = 0; it < NB * NB / 4 / kPotrfThreads; ++it) {
     const int idx = tid + it * kPotrfThreads, r = idx >> 4, c = (idx & 15) * 4;
     T v[4];
     ld4<T>(S + (off + r) * ld + off + c, v);
     st4<T>(A + r * kTileLd + c, v);
+    if (upd) {
+      ld4<T>(S + (off + r) * ld + off - NB + c, v);
+      st4<T>(Li + r * kTileLd + c, v);
+    }
+  }
+  if (tid < NB) yb[tid] = b[off + tid];
+  __syncthreads();
+  if (upd) {
+    // A -= P P^T (thread: rows 4(tid>>4).., columns 4(tid&15)..)
+    const int r0 = 4 * (tid >> 4), l0 = 4 * (tid & 15);
+    T acc[4][4] = {};
+#pragma unroll 4
+    for (int k4 = 0; k4 < NB; k4 += 4) {
+      T xi[4][4], xl[4][4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        ld4<T>(Li + (r0 + q) * kTileLd + k4, xi[q]);
+        ld4<T>(Li + (l0 + q) * kTileLd + k4, xl[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int w = 0; w < 4; ++w)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[q][w] += xi[q][k] * xl[w][k];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      T v[4];
+      ld4<T>(A + (r0 + q) * kTileLd + l0, v);
+#pragma unroll
+      for (int w = 0; w < 4; ++w) v[w] -= acc[q][w];
+      st4<T>(A + (r0 + q) * kTileLd + l0, v);
+    }
+    __syncthreads();
+  }
+  // clear L^-1
+#pragma unroll
+  for (int it = 0; it < NB * NB / 4 / kPotrfThreads; ++it) {
+    const int idx = tid + it * kPotrfThreads, r = idx >> 4, c = (idx & 15) * 4;
     const T z[4] = {T(0), T(0), T(0), T(0)};
     st4<T>(Li + r * kTileLd + c, z);
   }
-  if (tid < NB) yb[tid] = b[off + tid];
   __syncthreads();
 
   for (int p = 0; p < 4; ++p) {
@@ -331,16 +371,39 @@ __device__ __forceinline__ void tile_xyt(const T (*X)[NB + 1], const T (*Y)[NB +
   }
 }
 
+// Panel solve of block column kb: for tile ib = kb + 1 + blockIdx.x,
+//   (with upd) S_ib,kb -= L_ib,kb-1 L_kb,kb-1^T   (the previous panel's
+//                                                  update of this tile)
+//   L_ib,kb = S_ib,kb L_kb,kb^-T,   b_ib -= L_ib,kb y_kb
+// (the forward substitution is fused into the panel solve).
 template <typename T>
 __global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t ld, int kb, const T* __restrict__ Linv_all,
-                                                    T* __restrict__ b) {
+                                                    T* __restrict__ b, int upd) {
   T(*A)[NB + 1] = tile_at<T>(0);
   T(*Li)[NB + 1] = tile_at<T>(1);
   T* y = vec_at<T>(0);
   const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
   const int64_t ib = kb + 1 + blockIdx.x;
   const int64_t r0 = ib * NB, c0 = (int64_t)kb * NB;
-  load_tile<T>(A, S + r0 * ld + c0, ld, tid);
+  T a[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) ld4<T>(S + (r0 + ty * 4 + i) * ld + c0 + tx * 4, a[i]);
+  if (upd) {
+    load_tile<T>(A, S + r0 * ld + c0 - NB, ld, tid);
+    load_tile<T>(Li, S + c0 * ld + c0 - NB, ld, tid);
+    __syncthreads();
+    T acc[4][4] = {};
+    tile_xyt<T>(A, Li, ty, tx, acc);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) a[i][j] -= acc[i][j];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) A[ty * 4 + i][tx * 4 + j] = a[i][j];
   load_tile<T>(Li, Linv_all + (int64_t)kb * NB * NB, NB, tid);
   if (tid < NB) y[tid] = b[c0 + tid];
   __syncthreads();
@@ -348,56 +411,22 @@ __global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t l
   tile_xyt<T>(A, Li, ty, tx, acc);
   __syncthreads();
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 4; ++i) {
+    st4<T>(S + (r0 + ty * 4 + i) * ld + c0 + tx * 4, acc[i]);
 #pragma unroll
     for (int j = 0; j < 4; ++j) A[ty * 4 + i][tx * 4 + j] = acc[i][j];
+  }
   __syncthreads();
-  for (int idx = tid; idx < NB * NB; idx += 256) {
-    const int r = idx / NB, c = idx % NB;
-    S[(r0 + r) * ld + c0 + c] = A[r][c];
-  }
-  if (tid < NB) {
-    T s = T(0);
-    for (int c = 0; c < NB; ++c) s += A[tid][c] * y[c];
-    b[r0 + tid] -= s;
-  }
-}
-
-// Trailing update by panel kb: S_ij -= L_ik L_jk^T.  With one_col the tiles
-// are (first + blockIdx.x, first) (one block column); otherwise blockIdx.x
-// enumerates the lower triangle of tiles first <= jb <= ib.
-template <typename T>
-__global__ void __launch_bounds__(256) k_syrk(T* __restrict__ S, int64_t ld, int kb, int first, int one_col) {
-  T(*Xi)[NB + 1] = tile_at<T>(0);
-  T(*Xj)[NB + 1] = tile_at<T>(1);
-  const int tid = threadIdx.x, ty = tid / 16, tx = tid % 16;
-  int64_t ib, jb;
-  if (one_col) {
-    ib = first + (int64_t)blockIdx.x;
-    jb = first;
-  } else {
-    // triangular decode of blockIdx.x -> (row >= col)
-    const int64_t t = blockIdx.x;
-    int64_t row = (int64_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-    while ((row + 1) * (row + 2) / 2 <= t) ++row;
-    while (row * (row + 1) / 2 > t) --row;
-    const int64_t col = t - row * (row + 1) / 2;
-    ib = first + row;
-    jb = first + col;
-  }
-  const int64_t c0 = (int64_t)kb * NB;
-  load_tile<T>(Xi, S + ib * NB * ld + c0, ld, tid);
-  load_tile<T>(Xj, S + jb * NB * ld + c0, ld, tid);
-  __syncthreads();
-  T acc[4][4] = {};
-  tile_xyt<T>(Xi, Xj, ty, tx, acc);
+  // b_ib -= L y: 4 threads per row, 16 columns each
+  {
+    const int r = tid >> 2, q = tid & 3;
+    T s4 = T(0);
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      T* p = &S[(ib * NB + ty * 4 + i) * ld + jb * NB + tx * 4 + j];
-      *p -= acc[i][j];
-    }
+    for (int c = 0; c < 16; ++c) s4 += A[r][16 * q + c] * y[16 * q + c];
+    s4 += __shfl_xor_sync(0xffffffffu, s4, 1);
+    s4 += __shfl_xor_sync(0xffffffffu, s4, 2);
+    if (q == 0) b[r0 + r] -= s4;
+  }
 }
 
 // Trailing update over 128 x 128 output tiles (2 x 2 tiles of 64):
@@ -541,7 +570,6 @@ void dense_cholesky_prepare() {
   GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)potrf_smem_bytes<T>()));
   GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-  GBBA_CUDA(cudaFuncSetAttribute(k_syrk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
   GBBA_CUDA(cudaFuncSetAttribute(k_syrk_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)wide_smem_bytes<T>()));
@@ -570,24 +598,28 @@ void launch_hi(gbba_handle* h, void (*k)(Exp...), unsigned grid, unsigned block,
 
 // Solve S x = b in place of (S -> L, b -> y); x receives the solution.
 //
-// Look-ahead by one panel: after panel k is solved, the update of block
-// column k+1 (the next panel) runs on the call's stream followed by that
-// panel's diagonal factor and panel solve, while the update of the remaining
-// columns k+2.. runs on the side stream.  The two touch disjoint tiles; the
-// call's stream waits for the side stream's update of step k-1 before it
-// updates column k+1 (both write that column), and the side stream starts
-// step k only after panel k is solved.  The side stream is joined back
-// before the backward substitution, so the sequence can be captured.
+// Right-looking, 64-wide panels, look-ahead by one panel.  Per step k the
+// call's stream runs two kernels:
+//   potrf(k+1): applies panel k's update to diagonal tile k+1, factors it
+//               (L, L^-1, y_{k+1});
+//   trsm(k+1):  applies panel k's update to the tiles below it in block
+//               column k+1, then solves them (and updates b);
+// while the side stream applies panel k's update to block columns k+2..
+// (128-wide tiles).  The two streams touch disjoint tiles; the call's stream
+// waits for the side stream's step k-1 before step k (that step wrote block
+// column k+1), and the side stream starts step k once panel k is solved.
+// The side stream is joined back before the backward substitution, so the
+// sequence can be captured.
 template <typename T>
 void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st) {
   const int nb = (int)(n_pad / NB);
-  const size_t sm = dense_smem_bytes<T>();
+  const size_t sm = dense_smem_bytes<T>(), psm = potrf_smem_bytes<T>();
   dense_cholesky_prepare<T>();
-  launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, potrf_smem_bytes<T>(), st, S, n_pad, 0, Linv_all, b, flag);
-  if (nb > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(nb - 1), 256, sm, st, S, n_pad, 0, (const T*)Linv_all, b);
+  launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, 0, Linv_all, b, flag, 0);
+  if (nb > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(nb - 1), 256, sm, st, S, n_pad, 0, (const T*)Linv_all, b, 0);
   bool side_pending = false;
   for (int k = 0; k + 1 < nb; ++k) {
-    const int rem = nb - k - 1;  // tiles below the diagonal in column k
+    const int rem = nb - k - 1;  // tiles in block column k+1, diagonal included
     if (side_pending) {
       GBBA_CUDA(cudaStreamWaitEvent(st, h->ev_side, 0));
       side_pending = false;
@@ -595,15 +627,15 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
     if (rem > 1) {
       GBBA_CUDA(cudaEventRecord(h->ev_main, st));
       GBBA_CUDA(cudaStreamWaitEvent(h->side, h->ev_main, 0));
-      const int64_t tw = (rem - 1 + 1) / 2;  // 128-tiles per side over the 64-tiles k+2..nb-1
+      const int64_t tw = rem / 2;  // 128-tiles per side over the 64-tiles k+2..nb-1
       k_syrk_wide<T><<<(unsigned)(tw * (tw + 1) / 2), 256, wide_smem_bytes<T>(), h->side>>>(S, n_pad, k, k + 2, nb);
       check_launch(h);
       GBBA_CUDA(cudaEventRecord(h->ev_side, h->side));
       side_pending = true;
     }
-    launch_hi(h, k_syrk<T>, (unsigned)rem, 256, sm, st, S, n_pad, k, k + 1, 1);
-    launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, potrf_smem_bytes<T>(), st, S, n_pad, k + 1, Linv_all, b, flag);
-    if (rem > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(rem - 1), 256, sm, st, S, n_pad, k + 1, (const T*)Linv_all, b);
+    launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, k + 1, Linv_all, b, flag, 1);
+    if (rem > 1)
+      launch_hi(h, k_trsm_panel<T>, (unsigned)(rem - 1), 256, sm, st, S, n_pad, k + 1, (const T*)Linv_all, b, 1);
   }
   if (side_pending) GBBA_CUDA(cudaStreamWaitEvent(st, h->ev_side, 0));
   for (int kb = nb - 1; kb >= 0; --kb) {
