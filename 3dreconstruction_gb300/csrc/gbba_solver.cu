@@ -150,6 +150,10 @@ struct Prob {
   // FP64 camera poses (pose_matrix, 12 per camera) of ext, or null: the
   // mixed path evaluates its FP64 residuals from them.
   const double* pose;
+  // FP32 copies of the parameters and of the Jacobi scales, or null: the
+  // mixed path's FP32 Jacobian reads them instead of converting per
+  // observation (conversions and FP64 products run on GB300's FP64 pipe).
+  const float *ext_f, *intr_f, *pts_f, *scale_cf, *scale_pf;
 };
 
 template <int M, typename T>
@@ -170,9 +174,7 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
   constexpr int K = Model<M>::K;
   const uint32_t c = P.cam[o], g = P.icam[o], p = P.pt[o];
   const double2 ob = P.obs[o];
-  double Ed[6], Kd[K], Xd[3];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) Ed[i] = __ldg(&P.ext[6 * (int64_t)c + i]);
+  double Kd[K], Xd[3];
 #pragma unroll
   for (int i = 0; i < K; ++i) Kd[i] = __ldg(&P.intr[K * (int64_t)g + i]);
 #pragma unroll
@@ -180,21 +182,35 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
   T Je[2][6], Jk[2][K], Jx[2][3];
   double r[2];
   if constexpr (sizeof(T) == 8) {
+    double Ed[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Ed[i] = __ldg(&P.ext[6 * (int64_t)c + i]);
     residual<M, T, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (T*)nullptr);
   } else {
+    T Ef[6], Kf[K], Xf[3], rf[2];
     if (P.pose) {
       residual_pose<M, double>(Kd, P.pose + 12 * (int64_t)c, Xd, ob.x, ob.y, r);
     } else {
-      double dJe[2][6], dJk[2][K], dJx[2][3];
+      double Ed[6], dJe[2][6], dJk[2][K], dJx[2][3];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) Ed[i] = __ldg(&P.ext[6 * (int64_t)c + i]);
       residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
     }
-    T Ef[6], Kf[K], Xf[3], rf[2];
+    if (P.ext_f) {
 #pragma unroll
-    for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
+      for (int i = 0; i < 6; ++i) Ef[i] = __ldg(&P.ext_f[6 * (int64_t)c + i]);
 #pragma unroll
-    for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
+      for (int i = 0; i < K; ++i) Kf[i] = __ldg(&P.intr_f[K * (int64_t)g + i]);
 #pragma unroll
-    for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
+      for (int i = 0; i < 3; ++i) Xf[i] = __ldg(&P.pts_f[3 * (int64_t)p + i]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 6; ++i) Ef[i] = (T)__ldg(&P.ext[6 * (int64_t)c + i]);
+#pragma unroll
+      for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
+    }
     residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
   }
   double sr1;
@@ -209,13 +225,18 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
 #pragma unroll
   for (int j = 0; j < ObsJac<M, T>::B; ++j) {
     T sc = s;
-    if (kScale) sc = J.col[j] >= 0 ? (T)(scale_c[J.col[j]] * sr1) : T(0);
+    if (kScale) {
+      if (sizeof(T) == 4 && P.scale_cf) sc = J.col[j] >= 0 ? (T)P.scale_cf[J.col[j]] * s : T(0);
+      else sc = J.col[j] >= 0 ? (T)(scale_c[J.col[j]] * sr1) : T(0);
+    }
 #pragma unroll
     for (int i = 0; i < 2; ++i) J.Jc[i][j] = (j < 6 ? Je[i][j] : Jk[i][j - 6]) * sc;
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    const T sc = kScale ? (T)(scale_p[3 * (int64_t)p + j] * sr1) : s;
+    const T sc = !kScale ? s
+                 : (sizeof(T) == 4 && P.scale_pf) ? (T)P.scale_pf[3 * (int64_t)p + j] * s
+                                                 : (T)(scale_p[3 * (int64_t)p + j] * sr1);
 #pragma unroll
     for (int i = 0; i < 2; ++i) J.Jp[i][j] = Jx[i][j] * sc;
   }
@@ -732,7 +753,10 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
                                                      T* __restrict__ S, int64_t ld, T* __restrict__ partial) {
   using R = Rec<B>;
   using PT = PairTile<B>;
-  constexpr int ST = sizeof(T) == 4 ? 16 : 8;  // pairs per stage
+  // Pairs per stage: small stages keep registers and shared memory low, so
+  // that many warps have loads in flight (measured on the medium workload,
+  // 2 pairs per stage beat 4, 8 and 16).
+  constexpr int ST = 2;
   __shared__ __align__(16) T sh[4][ST * PT::PSZ];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -773,6 +797,20 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
   for (int r = 0; r < 3; ++r)
 #pragma unroll
     for (int c = 0; c < 3; ++c) acc[r][c] = T(0);
+  // The item's pair list (at most kPairChunk = 128 entries) is loaded once,
+  // four per lane; pair q of the item is then a shuffle away.
+  static_assert(kPairChunk <= 128, "pair list held in four registers per lane");
+  unsigned long long pidx[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const uint32_t qi = it.begin + lane + 32 * j;
+    pidx[j] = qi < it.end ? pairs[qi] : 0ull;
+  }
+  auto pair_at = [&](uint32_t q) {  // q relative to it.begin; uniform over the warp's 16-pair stage
+    const uint32_t j = q >> 5;
+    const unsigned long long v = j == 0 ? pidx[0] : j == 1 ? pidx[1] : j == 2 ? pidx[2] : pidx[3];
+    return __shfl_sync(0xffffffffu, v, (int)(q & 31));
+  };
   // Software pipeline: the loads of stage s+1 are issued before stage s is
   // multiplied out of shared memory.
   T v[ST][PT::SLOTS];
@@ -781,7 +819,7 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
 #pragma unroll
     for (int q = 0; q < ST; ++q) {
       if (q < n) {
-        const unsigned long long pr = pairs[q0 + q];
+        const unsigned long long pr = pair_at(q0 - it.begin + q);
         const uint32_t a = (uint32_t)(pr >> 32), b = (uint32_t)(pr & 0xffffffffu);
         const T* ra = rec + (int64_t)a * R::kSize;
         const T* rb = rec + (int64_t)b * R::kSize;
@@ -810,9 +848,17 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
     stage_store(q0);
     __syncwarp();
     if (q0 + ST < it.end) stage_load(q0 + ST);
+    // pair q of this stage is a diagonal pair (same observation) when bit q is set
+    uint32_t same_bits = 0;
+#pragma unroll
+    for (int q = 0; q < ST; ++q) {
+      if (q < n) {
+        const unsigned long long pr = pair_at(q0 - it.begin + q);
+        if ((uint32_t)(pr >> 32) == (uint32_t)(pr & 0xffffffffu)) same_bits |= 1u << q;
+      }
+    }
     if (active) {
       for (int q = grp; q < n; q += PT::G) {
-        const unsigned long long pr = pairs[q0 + q];
         const T* sp = sw + q * PT::PSZ;
         T A[12], Bv[12];
         lds12<T>(sp + ti * 12, A);
@@ -822,7 +868,7 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
 #pragma unroll
           for (int c = 0; c < 3; ++c)
             acc[r][c] -= A[3 * r] * Bv[3 * c] + A[3 * r + 1] * Bv[3 * c + 1] + A[3 * r + 2] * Bv[3 * c + 2];
-        if ((uint32_t)(pr >> 32) == (uint32_t)(pr & 0xffffffffu)) {
+        if (same_bits & (1u << q)) {
           T ja0[4], ja1[4], jb0[4], jb1[4];
           ld4<T>(sp + 2 * PT::WSZ + ti * 4, ja0);
           ld4<T>(sp + 2 * PT::WSZ + PT::TPD * 4 + ti * 4, ja1);
@@ -892,35 +938,43 @@ __global__ void __launch_bounds__(128) k_pair_merge(const PairMerge* __restrict_
   write_block<B, T>((uint32_t)(m.key / nc), (uint32_t)(m.key % nc), acc, lane, ext_col, intr_col, cam_group, K, S, ld);
 }
 
-// Stage 3, one warp per camera: rhs of the camera's columns = sum of q over
-// the camera's observations (fixed order: the camera CSR).
+// Stage 3, one block of 256 threads per camera: rhs of the camera's columns =
+// sum of q over the camera's observations.  Thread t sums observations
+// t, t+256, ... of the camera CSR; the per-thread sums are reduced by a warp
+// butterfly and then over the eight warps in order (a fixed order).
+constexpr int kRhsThreads = 256;
 template <int B, typename T>
-__global__ void __launch_bounds__(128) k_rhs_camera(const uint32_t* __restrict__ cam_off,
-                                                    const uint32_t* __restrict__ cam_obs, const T* __restrict__ rec,
-                                                    const int32_t* __restrict__ ext_col,
-                                                    const int32_t* __restrict__ intr_col,
-                                                    const int32_t* __restrict__ cam_group, int K, int64_t nc,
-                                                    T* __restrict__ rhs) {
+__global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __restrict__ cam_off,
+                                                            const uint32_t* __restrict__ cam_obs,
+                                                            const T* __restrict__ rec,
+                                                            const int32_t* __restrict__ ext_col,
+                                                            const int32_t* __restrict__ intr_col,
+                                                            const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                            T* __restrict__ rhs) {
   using R = Rec<B>;
-  const int lane = threadIdx.x & 31;
-  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (c >= nc) return;
+  __shared__ T part[kRhsThreads / 32][B];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t c = blockIdx.x;
   T acc[B];
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = T(0);
-  for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+  for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
     const T* r = rec + (int64_t)cam_obs[q] * R::kSize + R::kQ;
 #pragma unroll
     for (int i = 0; i < B; ++i) acc[i] += r[i];
   }
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
-  if (lane < B) {
-    T v = acc[0];
+  if (lane == 0) {
 #pragma unroll
-    for (int i = 1; i < B; ++i)
-      if (lane == i) v = acc[i];
-    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
+    for (int i = 0; i < B; ++i) part[warp][i] = acc[i];
+  }
+  __syncthreads();
+  if (threadIdx.x < B) {
+    T v = T(0);
+#pragma unroll
+    for (int w = 0; w < kRhsThreads / 32; ++w) v += part[w][threadIdx.x];
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, threadIdx.x);
     if (ci >= 0) rhs[ci] = v;
   }
 }
@@ -1619,6 +1673,8 @@ struct Solve {
   // device arrays
   double *ext, *intr, *pts, *ext2, *intr2, *pts2;
   double *pose = nullptr, *pose2 = nullptr;  // FP64 poses of ext / ext2 (mixed path)
+  float *ext_f = nullptr, *intr_f = nullptr, *pts_f = nullptr;  // FP32 copies of ext, intr, pts (mixed path)
+  float *scale_cf = nullptr, *scale_pf = nullptr;               // FP32 copies of the Jacobi scales
   uint32_t *pt_grp = nullptr, *pgrp_cnt = nullptr, *pgrp_off = nullptr;  // point groups (k_pt_groups)
   int64_t n_pgrp = 0;
   int nb_pgrp = 1;  // blocks of the per-group kernels (4 groups per block)
@@ -1671,6 +1727,7 @@ static Prob make_prob(const Solve& s, const double* ext, const double* intr, con
   P.loss_type = o ? o->loss_type : 0;
   P.loss_a = o ? o->loss_scale : 1.0;
   P.pose = nullptr;
+  P.ext_f = P.intr_f = P.pts_f = P.scale_cf = P.scale_pf = nullptr;
   return P;
 }
 
@@ -1683,6 +1740,11 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.ext2 = a.template take<double>(6 * s.nc);
   s.pose = a.template take<double>(12 * s.nc);
   s.pose2 = a.template take<double>(12 * s.nc);
+  s.ext_f = a.template take<float>(6 * s.nc);
+  s.intr_f = a.template take<float>((int64_t)s.k * s.ni);
+  s.pts_f = a.template take<float>(3 * s.np);
+  s.scale_cf = a.template take<float>(s.n_red + 1);
+  s.scale_pf = a.template take<float>(3 * s.np);
   s.intr2 = a.template take<double>(s.k * s.ni);
   s.pts2 = a.template take<double>(3 * s.np);
   s.obs = a.template take<double2>(s.no);
@@ -2215,6 +2277,11 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   // s.pose for the current parameters, s.pose2 for the evaluated ones.
   constexpr bool kPose = sizeof(T) == 4;
   const unsigned nb_cam_pose = (unsigned)std::max<int64_t>(1, ceil_div(s.nc, 128));
+  auto to_float = [&](const double* src, float* dst, int64_t n) {
+    if (n <= 0) return;
+    k_convert<double, float><<<(unsigned)std::min<int64_t>(ceil_div(n, 256), 1024), 256, 0, st>>>(src, dst, n);
+    check_launch(h);
+  };
   auto launch_cost = [&](const double* e, const double* i, const double* p) {
     Prob Pc = make_prob(s, e, i, p, o);
     if (kPose && s.nc > 0) {
@@ -2233,6 +2300,14 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       check_launch(h);
       P.pose = s.pose;
     }
+    if (kPose) {
+      to_float(s.ext, s.ext_f, 6 * s.nc);
+      to_float(s.intr, s.intr_f, (int64_t)s.k * s.ni);
+      to_float(s.pts, s.pts_f, 3 * s.np);
+      P.ext_f = s.ext_f;
+      P.intr_f = s.intr_f;
+      P.pts_f = s.pts_f;
+    }
     GBBA_CUDA(cudaMemsetAsync(s.cn_c, 0, sizeof(double) * (s.n_red + 1), st));
     GBBA_CUDA(cudaMemsetAsync(s.g_c, 0, sizeof(double) * (s.n_red + 1), st));
     GBBA_CUDA(cudaMemsetAsync(s.cn_p, 0, sizeof(double) * 3 * s.np, st));
@@ -2250,6 +2325,10 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
         3 * s.np, s.cn_p, s.g_p, s.scale_p, s.diag_p, first ? 1 : 0, o->jacobi_scaling, o->min_lm_diagonal,
         o->max_lm_diagonal, s.gmax_bits);
     check_launch(h);
+    if (kPose && first) {
+      to_float(s.scale_c, s.scale_cf, s.n_red);
+      to_float(s.scale_p, s.scale_pf, 3 * s.np);
+    }
     k_xnorm<<<gx, 256, 0, st>>>(s.ext, s.ext_col, n_e, s.intr, s.intr_var, s.k, n_i, s.pts, 3 * s.np, s.part_x);
     check_launch(h);
     k_reduce3<<<1, 256, 0, st>>>(s.part_x, gx, s.part_x, 0, s.part_x, 0, s.part_x, 0, s.scalars + 4);
@@ -2298,8 +2377,15 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   // copied back), so the sequence is invariant and is captured once into CUDA
   // graphs that every iteration replays.
   Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
-  if (kPose && s.nc > 0) P.pose = s.pose;
-  const int nb_back = s.pair_path ? s.nb_pgrp : s.nb_pt;  // blocks (partials) of the back substitution  // refreshed by linearize() after every accepted step
+  if (kPose && s.nc > 0) P.pose = s.pose;  // refreshed by linearize() after every accepted step
+  if (kPose) {
+    P.ext_f = s.ext_f;
+    P.intr_f = s.intr_f;
+    P.pts_f = s.pts_f;
+    P.scale_cf = s.scale_cf;
+    P.scale_pf = s.scale_pf;
+  }
+  const int nb_back = s.pair_path ? s.nb_pgrp : s.nb_pt;  // blocks (partials) of the back substitution
   auto record_phase = [&](int ph) {
     switch (ph) {
       case 0:
@@ -2331,9 +2417,11 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
               check_launch(h);
             }
           }
-          k_rhs_camera<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
-              s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs);
-          check_launch(h);
+          if (s.nc > 0) {
+            k_rhs_camera<B, T><<<(unsigned)s.nc, kRhsThreads, 0, st>>>(
+                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs);
+            check_launch(h);
+          }
           if (!s.dense) {
             k_cam_blocks<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
                 s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.diag_c,
