@@ -40,6 +40,29 @@ __device__ __forceinline__ T* vec_at(int i) {
 template <typename T>
 constexpr size_t dense_smem_bytes() { return (size_t)2 * NB * (NB + 1) * sizeof(T) + 2 * NB * sizeof(T); }
 
+// Copy the contiguous 64x64 tile at src (row stride 64) with L2-only loads
+// (ld.global.cg): for data written by a kernel that may still have been
+// running when this kernel started (programmatic dependent launch), so that
+// no line cached in L1 before that kernel finished can be read.
+template <typename T>
+__device__ __forceinline__ void load_tile_cg(T (*dst)[NB + 1], const T* src, int tid) {
+  using V = typename Vec16<T>::type;
+  constexpr int W = Vec16<T>::n, PER_ROW = NB / W, ITER = NB * PER_ROW / 256;
+  V v[ITER];
+#pragma unroll
+  for (int it = 0; it < ITER; ++it) {
+    const int idx = tid + it * 256, r = idx / PER_ROW, c = (idx % PER_ROW) * W;
+    v[it] = __ldcg(reinterpret_cast<const V*>(src + r * NB + c));
+  }
+#pragma unroll
+  for (int it = 0; it < ITER; ++it) {
+    const int idx = tid + it * 256, r = idx / PER_ROW, c = (idx % PER_ROW) * W;
+    const T* e = reinterpret_cast<const T*>(&v[it]);
+#pragma unroll
+    for (int w = 0; w < W; ++w) dst[r][c + w] = e[w];
+  }
+}
+
 // Copy the 64x64 tile at src (row stride ld) into a padded shared tile.  All
 // of a thread's global loads are issued before its shared stores so that
 // their latencies overlap.
@@ -109,6 +132,9 @@ __global__ void __launch_bounds__(kPotrfThreads) k_potrf_diag(T* __restrict__ S,
   T* dv = yb + NB;                        // [64] pivots of the current panel
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int64_t off = (int64_t)kb * NB;
+  // the panel solve of this block column may start now: it reads L^-1 and y
+  // only after griddepcontrol.wait, i.e. after this kernel has completed
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   // load the tile (lower part is what is used) and b; with upd, also the
   // previous panel's block P = L_{kb,kb-1} (staged in the L^-1 buffer)
 #pragma unroll
@@ -377,8 +403,8 @@ __device__ __forceinline__ void tile_xyt(const T (*X)[NB + 1], const T (*Y)[NB +
 //   L_ib,kb = S_ib,kb L_kb,kb^-T,   b_ib -= L_ib,kb y_kb
 // (the forward substitution is fused into the panel solve).
 template <typename T>
-__global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t ld, int kb, const T* __restrict__ Linv_all,
-                                                    T* __restrict__ b, int upd) {
+__global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t ld, int kb, const T* Linv_all, T* b,
+                                                    int upd) {
   T(*A)[NB + 1] = tile_at<T>(0);
   T(*Li)[NB + 1] = tile_at<T>(1);
   T* y = vec_at<T>(0);
@@ -404,8 +430,11 @@ __global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t l
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) A[ty * 4 + i][tx * 4 + j] = a[i][j];
-  load_tile<T>(Li, Linv_all + (int64_t)kb * NB * NB, NB, tid);
-  if (tid < NB) y[tid] = b[c0 + tid];
+  // L^-1 and y_kb come from the diagonal factor launched just before this
+  // kernel (programmatic dependent launch): wait for its completion
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  load_tile_cg<T>(Li, Linv_all + (int64_t)kb * NB * NB, tid);
+  if (tid < NB) y[tid] = __ldcg(b + c0 + tid);
   __syncthreads();
   T acc[4][4] = {};
   tile_xyt<T>(A, Li, ty, tx, acc);
@@ -425,7 +454,7 @@ __global__ void __launch_bounds__(256) k_trsm_panel(T* __restrict__ S, int64_t l
     for (int c = 0; c < 16; ++c) s4 += A[r][16 * q + c] * y[16 * q + c];
     s4 += __shfl_xor_sync(0xffffffffu, s4, 1);
     s4 += __shfl_xor_sync(0xffffffffu, s4, 2);
-    if (q == 0) b[r0 + r] -= s4;
+    if (q == 0) b[r0 + r] = __ldcg(b + r0 + r) - s4;
   }
 }
 
@@ -579,19 +608,25 @@ void dense_cholesky_prepare() {
 // Launch on the panel chain at the device's greatest stream priority (the
 // attribute is kept when the launch is captured into a graph), so that the
 // one-CTA diagonal factor is scheduled ahead of the trailing update's CTAs.
+//
+// With pdl the launch may begin while the previous kernel on the stream is
+// still running (programmatic dependent launch): the kernel must execute
+// griddepcontrol.wait before it touches anything the previous kernel writes.
 template <typename... Exp, typename... Act>
-void launch_hi(gbba_handle* h, void (*k)(Exp...), unsigned grid, unsigned block, size_t smem, cudaStream_t st,
-               Act... args) {
+void launch_hi(gbba_handle* h, bool pdl, void (*k)(Exp...), unsigned grid, unsigned block, size_t smem,
+               cudaStream_t st, Act... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(block);
   cfg.dynamicSmemBytes = smem;
   cfg.stream = st;
-  cudaLaunchAttribute at[1];
+  cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributePriority;
   at[0].val.priority = h->prio_hi;
+  at[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[1].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = pdl ? 2 : 1;
   GBBA_CUDA(cudaLaunchKernelEx(&cfg, k, args...));
   count_launch(h);
 }
@@ -615,8 +650,9 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
   const int nb = (int)(n_pad / NB);
   const size_t sm = dense_smem_bytes<T>(), psm = potrf_smem_bytes<T>();
   dense_cholesky_prepare<T>();
-  launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, 0, Linv_all, b, flag, 0);
-  if (nb > 1) launch_hi(h, k_trsm_panel<T>, (unsigned)(nb - 1), 256, sm, st, S, n_pad, 0, (const T*)Linv_all, b, 0);
+  launch_hi(h, false, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, 0, Linv_all, b, flag, 0);
+  if (nb > 1)
+    launch_hi(h, true, k_trsm_panel<T>, (unsigned)(nb - 1), 256, sm, st, S, n_pad, 0, (const T*)Linv_all, b, 0);
   bool side_pending = false;
   for (int k = 0; k + 1 < nb; ++k) {
     const int rem = nb - k - 1;  // tiles in block column k+1, diagonal included
@@ -633,9 +669,10 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
       GBBA_CUDA(cudaEventRecord(h->ev_side, h->side));
       side_pending = true;
     }
-    launch_hi(h, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, k + 1, Linv_all, b, flag, 1);
+    launch_hi(h, false, k_potrf_diag<T>, 1, kPotrfThreads, psm, st, S, n_pad, k + 1, Linv_all, b, flag, 1);
     if (rem > 1)
-      launch_hi(h, k_trsm_panel<T>, (unsigned)(rem - 1), 256, sm, st, S, n_pad, k + 1, (const T*)Linv_all, b, 1);
+      launch_hi(h, true, k_trsm_panel<T>, (unsigned)(rem - 1), 256, sm, st, S, n_pad, k + 1, (const T*)Linv_all,
+                b, 1);
   }
   if (side_pending) GBBA_CUDA(cudaStreamWaitEvent(st, h->ev_side, 0));
   for (int kb = nb - 1; kb >= 0; --kb) {

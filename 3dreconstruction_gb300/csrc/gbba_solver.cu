@@ -2468,7 +2468,12 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   dense_cholesky_prepare<T>();
   if (o->use_cuda_graphs) {
     for (int ph = 0; ph < 5; ++ph) {
-      if (ph == 2 && !s.dense) continue;  // the PCG loop is host-driven
+      // Phase 2 (the linear solve) is launched directly every iteration: the
+      // PCG loop is host-driven, and the dense factorisation relies on the
+      // per-launch stream priority of its panel chain, which a graph replay
+      // does not reproduce (medium workload: 4.59 ms replayed, 4.50 ms
+      // launched directly).
+      if (ph == 2) continue;
       const int64_t l0 = h->launches;
       cudaGraph_t g = nullptr;
       if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
