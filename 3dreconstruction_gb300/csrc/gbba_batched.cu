@@ -7,10 +7,16 @@
 // levenberg_marquardt_strategy.cc).  Local windows are small (<= 40 cameras,
 // reduced camera system <= 256 unknowns), so one CTA owns one problem for its
 // whole solve:
-//   - the lower triangle of S, rhs, the step and the camera-side scaling live
-//     in shared memory (S: n(n+1)/2 values, <= 131.6 KB in FP32);
-//   - points are processed one warp per point (V, V^-1, g_p, W, W V^-1), the
-//     pair products are accumulated into shared-memory S with shared atomics;
+//   - in FP32 the lower triangle of S lives in shared memory (n(n+1)/2
+//     values, <= 131.6 KB) and the pair products are accumulated into it
+//     with shared atomics;
+//   - in FP64 (the plain FP64 path and the mixed path's FP64 polish) S lives
+//     in a per-CTA slice of global memory (L2-resident), accumulated with
+//     native global FP64 reductions: shared memory has no FP64 add, and an
+//     FP64 S of n = 256 would not fit it;
+//   - the camera column norms and gradient are accumulated in the same
+//     global slice (FP64 reductions);
+//   - points are processed one warp per point (V, V^-1, g_p, W, W V^-1);
 //   - the Cholesky factorisation and both triangular solves run in shared
 //     memory; the accept / reject decision is taken by thread 0.
 // CTAs never wait on each other, so the launch cannot deadlock; the hardware
@@ -37,9 +43,9 @@ namespace {
 constexpr int kThreads = 512;
 constexpr int kWarps = kThreads / 32;
 
-template <typename T> struct NMax;
-template <> struct NMax<float> { static constexpr int v = 256; };
-template <> struct NMax<double> { static constexpr int v = 176; };
+constexpr int kNMax = 256;  // largest reduced camera system of a batched problem
+// doubles of a CTA's global scratch slice: column norms, gradient, rhs, S
+constexpr int64_t kGlobalSlice = 3 * kNMax + kNMax * (kNMax + 1) / 2;
 
 struct BProb {
   uint32_t o0, o1;  // observations (sorted by point)
@@ -65,6 +71,7 @@ struct BArgs {
   const uint8_t* intr_var;
   double *scale_p, *diag_p;
   void *Vinv, *gp, *wscratch;  // compute type
+  double* gscr;                // kGlobalSlice doubles per CTA
   int max_views;
   BOut* out;
   // options
@@ -72,18 +79,24 @@ struct BArgs {
   double loss_a, ftol, gtol, ptol, r0, rmax, rmin, min_rel, dmin, dmax;
 };
 
-template <typename T, int N>
+// NS: values of S held in shared memory (1 when S lives in global memory).
+constexpr int kPoseCams = 64;  // windows with more cameras evaluate residuals by Rodrigues
+template <typename T, int NS, int N>
 struct Shared {
-  T S[N * (N + 1) / 2];
+  double pose[2][kPoseCams * 12];  // FP64 poses of ext (0) and of the candidate ext2 (1)
+  T S[NS];
   T rhs[N];
   T z[N];
   double scale_c[N];
   double diag_c[N];
-  double acc_c[N];  // column norms during linearisation
-  double g_c[N];
   double red[kWarps];
   double bcast[8];
   int flag;
+};
+template <typename SS>
+struct SharedOf {
+  static constexpr bool kGlobalS = sizeof(SS) == 8;
+  using type = Shared<SS, kGlobalS ? 1 : kNMax * (kNMax + 1) / 2, kNMax>;
 };
 
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
@@ -119,10 +132,14 @@ __device__ __forceinline__ double block_max(double v, double* red, double* out) 
 }
 
 // Residual (FP64), corrected Jacobian blocks (compute type) of observation o.
+// With pose (FP64 pose_matrix of the problem's cameras, indexed from the
+// problem's first camera c0), the FP32 path takes its FP64 residual from it
+// instead of the Rodrigues sine / cosine per observation.
 template <int M, typename T>
 __device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, const double* intr, const double* pts,
                                            int64_t o, uint32_t p, double r[2], T Jc[2][6 + Model<M>::K], T Jp[2][3],
-                                           int col[6 + Model<M>::K]) {
+                                           int col[6 + Model<M>::K], const double* pose = nullptr,
+                                           uint32_t c0 = 0) {
   constexpr int K = Model<M>::K;
   const uint32_t c = a.cam[o], g = a.icam[o];
   const double2 ob = a.obs[o];
@@ -137,8 +154,12 @@ __device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, co
   if constexpr (sizeof(T) == 8) {
     residual<M, double, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (double*)nullptr);
   } else {
-    double dJe[2][6], dJk[2][K], dJx[2][3];
-    residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    if (pose) {
+      residual_pose<M, double>(Kd, pose + 12 * (c - c0), Xd, ob.x, ob.y, r);
+    } else {
+      double dJe[2][6], dJk[2][K], dJx[2][3];
+      residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+    }
     T Ef[6], Kf[K], Xf[3], rf[2];
 #pragma unroll
     for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
@@ -174,19 +195,63 @@ template <int M, typename T, typename SS>
 __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   constexpr int K = Model<M>::K;
   constexpr int B = 6 + K;
-  constexpr int N = NMax<SS>::v;
+  constexpr bool kGS = SharedOf<SS>::kGlobalS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  Shared<SS, N>& sh = *reinterpret_cast<Shared<SS, N>*>(smem_raw);
+  typename SharedOf<SS>::type& sh = *reinterpret_cast<typename SharedOf<SS>::type*>(smem_raw);
   const uint32_t pid = a.order[blockIdx.x];
   const BProb P = a.probs[pid];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = (int)P.n;
   T* Vinv = (T*)a.Vinv;
   T* gpv = (T*)a.gp;
-  // per-warp scratch: W and W V^-1 of the warp's current point
-  T* wsc = (T*)a.wscratch + ((int64_t)blockIdx.x * kWarps + warp) * (int64_t)a.max_views * 6 * B;
+  // per-warp scratch, one slot per observation of the warp's current point:
+  // W and W V^-1 (6B values), then (one intrinsic group) the observation's
+  // U_kk lower triangle and intrinsic rhs (KK + K values); one more slot
+  // holds per-point sums
+  constexpr int KK = K * (K + 1) / 2;
+  constexpr int SLOT = 6 * B + KK + K;
+  T* wsc = (T*)a.wscratch + ((int64_t)blockIdx.x * kWarps + warp) * (int64_t)(a.max_views + 1) * SLOT;
+  // global slice: column norms [kNMax], gradient [kNMax], rhs [kNMax], S (FP64)
+  double* gsl = a.gscr + (int64_t)blockIdx.x * kGlobalSlice;
+  double* g_acc = gsl;
+  double* g_grad = gsl + kNMax;
+  double* g_rhs = gsl + 2 * kNMax;
+  double* g_S = gsl + 3 * kNMax;
+  // S and rhs accessors: shared memory in FP32, the global slice (through L2:
+  // global reductions do not update L1) in FP64
+  auto Sld = [&](int i) -> SS {
+    if constexpr (kGS) return (SS)__ldcg(g_S + i);
+    else return sh.S[i];
+  };
+  auto Sst = [&](int i, SS v) {
+    if constexpr (kGS) __stcg(g_S + i, (double)v);
+    else sh.S[i] = v;
+  };
+  auto Sadd = [&](int i, SS v) {
+    if constexpr (kGS) atomicAdd(g_S + i, (double)v);
+    else atomicAdd(&sh.S[i], v);
+  };
+  auto Radd = [&](int i, SS v) {
+    if constexpr (kGS) atomicAdd(g_rhs + i, (double)v);
+    else atomicAdd(&sh.rhs[i], v);
+  };
 
+  const bool use_pose = P.nc <= (uint32_t)kPoseCams;
+  // poses of ext (slot 0) or ext2 (slot 1); the barrier makes them visible
+  auto make_poses = [&](const double* ext, int slot) {
+    if (use_pose) {
+      for (uint32_t c = tid; c < P.nc; c += kThreads) {
+        double E[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) E[i] = ext[6 * ((int64_t)P.c0 + c) + i];
+        pose_matrix<double>(E, &sh.pose[slot][12 * c]);
+      }
+    }
+    __syncthreads();
+  };
+  const double* pose_x = use_pose ? sh.pose[0] : nullptr;
   auto cost_at = [&](const double* ext, const double* intr, const double* pts, bool* finite) -> double {
+    const double* pz = !use_pose ? nullptr : ext == a.ext ? sh.pose[0] : sh.pose[1];
     double acc = 0.0;
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       // obs of point p are [pt_off[p], pt_off[p+1])
@@ -197,7 +262,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         for (int i = 0; i < K; ++i) Kp[i] = intr[K * (int64_t)g + i];
         for (int i = 0; i < 3; ++i) X[i] = pts[3 * (int64_t)p + i];
         const double2 ob = a.obs[o];
-        residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+        if (pz) residual_pose<M, double>(Kp, pz + 12 * (c - P.c0), X, ob.x, ob.y, r);
+        else residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
         double sr1;
         acc += robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
       }
@@ -210,8 +276,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   // gradient max norm, x norm; scale (first) and LM diagonal
   auto linearize = [&](bool first, double* gmax, double* xnorm) {
     for (int i = tid; i < n; i += kThreads) {
-      sh.acc_c[i] = 0.0;
-      sh.g_c[i] = 0.0;
+      __stcg(g_acc + i, 0.0);
+      __stcg(g_grad + i, 0.0);
     }
     __syncthreads();
     double gm = 0.0;
@@ -221,13 +287,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
           const double x0 = Jc[0][j], x1 = Jc[1][j];
-          atomicAdd(&sh.acc_c[col[j]], x0 * x0 + x1 * x1);
-          atomicAdd(&sh.g_c[col[j]], x0 * r[0] + x1 * r[1]);
+          atomicAdd(g_acc + col[j], x0 * x0 + x1 * x1);
+          atomicAdd(g_grad + col[j], x0 * r[0] + x1 * r[1]);
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -251,10 +317,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
-      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(sh.acc_c[i])) : 1.0;
+      const double acc = __ldcg(g_acc + i);
+      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(acc)) : 1.0;
       const double sc = sh.scale_c[i];
-      sh.diag_c[i] = fmin(fmax(sh.acc_c[i] * sc * sc, a.dmin), a.dmax);
-      gm = fmax(gm, fabs(sh.g_c[i]));
+      sh.diag_c[i] = fmin(fmax(acc * sc * sc, a.dmin), a.dmax);
+      gm = fmax(gm, fabs(__ldcg(g_grad + i)));
     }
     *gmax = block_max(gm, sh.red, &sh.bcast[1]);
     double xs = 0.0;
@@ -274,6 +341,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   };
 
   bool finite = true;
+  make_poses(a.ext, 0);
   double cost = cost_at(a.ext, a.intr, a.pts, &finite);
   BOut res;
   res.initial_cost = cost;
@@ -300,12 +368,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       break;
     }
     // ---- S = diag(D_c^2) + sum F'F - sum (F'E) V^-1 (E'F), rhs
-    for (int i = tid; i < n * (n + 1) / 2; i += kThreads) sh.S[i] = SS(0);
-    for (int i = tid; i < n; i += kThreads) sh.rhs[i] = SS(0);
+    for (int i = tid; i < n * (n + 1) / 2; i += kThreads) Sst(i, SS(0));
+    for (int i = tid; i < n; i += kThreads) {
+      if constexpr (kGS) __stcg(g_rhs + i, 0.0);
+      else sh.rhs[i] = SS(0);
+    }
     if (tid == 0) sh.flag = 0;
     __syncthreads();
-    for (int i = tid; i < n; i += kThreads) sh.S[tri(i, i)] = (SS)(sh.diag_c[i] / radius);
+    for (int i = tid; i < n; i += kThreads) Sst(tri(i, i), (SS)(sh.diag_c[i] / radius));
     __syncthreads();
+    // One intrinsic group per window (the local-BA case): the intrinsic
+    // columns are common to every observation, so their terms factor through
+    // per-point sums (no observation pairs) and per-lane accumulators:
+    //   S_kk -= (sum_x W_kx V^-1)(sum_y W_ky)^T,  S_k,c(y) -= (sum_x W_kx V^-1) W_ey^T,
+    //   U_kk += sum_o J_ko^T J_ko (per lane, flushed once), rhs_k likewise;
+    // only the 6x6 extrinsic blocks need the observation pairs (camera a > b,
+    // or the diagonal block of a single observation).
+    const bool one_group = P.ni == 1;
+    const int32_t* kcol = a.intr_col + K * (int64_t)P.g0;  // the group's columns (-1 = held)
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1], m = oe - ob;
       T v[6] = {}, g[3] = {};
@@ -313,7 +393,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           const T s = col[j] >= 0 ? (T)sh.scale_c[col[j]] : T(0);
@@ -335,19 +415,37 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         v[5] += Jp[0][2] * Jp[0][2] + Jp[1][2] * Jp[1][2];
 #pragma unroll
         for (int j = 0; j < 3; ++j) g[j] += Jp[0][j] * r0 + Jp[1][j] * r1;
-        T* W = wsc + (int64_t)(o - ob) * 6 * B;
+        T* W = wsc + (int64_t)(o - ob) * SLOT;
 #pragma unroll
-        for (int i = 0; i < B; ++i) {
+        for (int i = 0; i < B; ++i)
 #pragma unroll
           for (int j = 0; j < 3; ++j) W[i * 3 + j] = Jc[0][i] * Jp[0][j] + Jc[1][i] * Jp[1][j];
+        // U = Jc^T Jc and Jc^T r
+        if (one_group) {
+#pragma unroll
+          for (int e = 0; e < KK + K; ++e) W[6 * B + e] = T(0);
+        }
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
           const int ci = col[i];
           if (ci < 0) continue;
-          atomicAdd(&sh.rhs[ci], (SS)(Jc[0][i] * r0 + Jc[1][i] * r1));
+          const T ri = Jc[0][i] * r0 + Jc[1][i] * r1;
+          if (one_group && i >= 6) W[6 * B + KK + (i - 6)] = ri;
+          else Radd(ci, (SS)ri);
 #pragma unroll
-          for (int j = 0; j < B; ++j) {
+          for (int j = 0; j <= i; ++j) {
             const int cj = col[j];
-            if (cj < 0 || cj > ci) continue;
-            atomicAdd(&sh.S[tri(ci, cj)], (SS)(Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j]));
+            const T u = Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j];
+            if (one_group && j >= 6) {
+              W[6 * B + (i - 6) * (i - 5) / 2 + (j - 6)] = u;  // held columns are skipped at the reduction
+              continue;
+            }
+            if (cj < 0) continue;
+            if (one_group || cj <= ci) {
+              Sadd(tri(ci, cj), (SS)u);
+            } else {
+              Sadd(tri(cj, ci), (SS)u);
+            }
           }
         }
       }
@@ -375,7 +473,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       }
       const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
-        T* W = wsc + (int64_t)(o - ob) * 6 * B;
+        T* W = wsc + (int64_t)(o - ob) * SLOT;
         const uint32_t c = a.cam[o], gi = a.icam[o];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -385,72 +483,147 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
 #pragma unroll
           for (int j = 0; j < 3; ++j) W[3 * B + i * 3 + j] = y[j];
           const int ci = i < 6 ? a.ext_col[6 * (int64_t)c + i] : a.intr_col[K * (int64_t)gi + (i - 6)];
-          if (ci >= 0) atomicAdd(&sh.rhs[ci], (SS)(-(y[0] * g[0] + y[1] * g[1] + y[2] * g[2])));
+          const T q = -(y[0] * g[0] + y[1] * g[1] + y[2] * g[2]);
+          if (ci < 0) continue;
+          if (one_group && i >= 6) W[6 * B + KK + (i - 6)] += q;
+          else Radd(ci, (SS)q);
         }
       }
       __syncwarp();
-      for (uint32_t x = 0; x < m; ++x) {
-        const uint32_t oa = ob + x;
-        const uint32_t ca = a.cam[oa], ga = a.icam[oa];
-        const T* Wha = wsc + (int64_t)x * 6 * B + 3 * B;
+      if (one_group) {
+        // per-point sums over the observations, Wh_K = sum W_k V^-1 and
+        // W_K = sum W_k (K x 3 each), kept in the warp's extra scratch slot
+        T* sums = wsc + (int64_t)a.max_views * SLOT;
+        for (int e = lane; e < 3 * K; e += 32) {
+          T hs = T(0), ws = T(0);
+          for (uint32_t x = 0; x < m; ++x) {
+            const T* Wx = wsc + (int64_t)x * SLOT;
+            hs += Wx[3 * B + 18 + e];
+            ws += Wx[18 + e];
+          }
+          sums[e] = hs;
+          sums[3 * K + e] = ws;
+        }
+        // the point's U_kk and intrinsic rhs: sums over its observations' slots
+        for (int e = lane; e < KK + K; e += 32) {
+          T acc = T(0);
+          for (uint32_t x = 0; x < m; ++x) acc += wsc[(int64_t)x * SLOT + 6 * B + e];
+          if (e < KK) {
+            int i = 0;
+            while ((i + 1) * (i + 2) / 2 <= e) ++i;
+            const int j = e - i * (i + 1) / 2;
+            if (kcol[i] >= 0 && kcol[j] >= 0) Sadd(tri(kcol[i], kcol[j]), (SS)acc);
+          } else if (kcol[e - KK] >= 0) {
+            Radd(kcol[e - KK], (SS)acc);
+          }
+        }
+        __syncwarp();
+        // S_kk -= Wh_K W_K^T (lower triangle of the K x K block)
+        for (int e = lane; e < KK; e += 32) {
+          int i = 0;
+          while ((i + 1) * (i + 2) / 2 <= e) ++i;
+          const int j = e - i * (i + 1) / 2;
+          const int ci = kcol[i], cj = kcol[j];
+          if (ci < 0 || cj < 0) continue;
+          const T sacc = sums[3 * i] * sums[3 * K + 3 * j] + sums[3 * i + 1] * sums[3 * K + 3 * j + 1] +
+                         sums[3 * i + 2] * sums[3 * K + 3 * j + 2];
+          Sadd(tri(ci, cj), (SS)(-sacc));
+        }
+        // S_k,c(y) -= Wh_K W_ey^T for every observation y
         for (uint32_t y = 0; y < m; ++y) {
-          const uint32_t obb = ob + y;
-          const uint32_t cb = a.cam[obb], gb = a.icam[obb];
-          const T* Wb = wsc + (int64_t)y * 6 * B;
-          for (int e = lane; e < B * B; e += 32) {
-            const int i = e / B, j = e % B;
-            const int ci = i < 6 ? a.ext_col[6 * (int64_t)ca + i] : a.intr_col[K * (int64_t)ga + (i - 6)];
-            const int cj = j < 6 ? a.ext_col[6 * (int64_t)cb + j] : a.intr_col[K * (int64_t)gb + (j - 6)];
-            if (ci < 0 || cj < 0 || cj > ci) continue;
-            atomicAdd(&sh.S[tri(ci, cj)],
-                      (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
+          const uint32_t cb = a.cam[ob + y];
+          const T* Wy = wsc + (int64_t)y * SLOT;
+          for (int e = lane; e < 6 * K; e += 32) {
+            const int i = e / 6, j = e % 6;
+            const int ci = kcol[i], cj = a.ext_col[6 * (int64_t)cb + j];
+            if (ci < 0 || cj < 0) continue;
+            const T sacc = sums[3 * i] * Wy[3 * j] + sums[3 * i + 1] * Wy[3 * j + 1] + sums[3 * i + 2] * Wy[3 * j + 2];
+            Sadd(tri(ci, cj), (SS)(-sacc));
+          }
+        }
+        // extrinsic blocks: pairs with camera a > b, and each observation's own block
+        for (uint32_t x = 0; x < m; ++x) {
+          const uint32_t ca = a.cam[ob + x];
+          const T* Wha = wsc + (int64_t)x * SLOT + 3 * B;
+          for (uint32_t y = 0; y < m; ++y) {
+            const uint32_t cb = a.cam[ob + y];
+            if (cb > ca) continue;
+            const T* Wb = wsc + (int64_t)y * SLOT;
+            for (int e = lane; e < 36; e += 32) {
+              const int i = e / 6, j = e % 6;
+              const int ci = a.ext_col[6 * (int64_t)ca + i], cj = a.ext_col[6 * (int64_t)cb + j];
+              if (ci < 0 || cj < 0 || cj > ci) continue;
+              Sadd(tri(ci, cj),
+                   (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
+            }
+          }
+        }
+      } else {
+        for (uint32_t x = 0; x < m; ++x) {
+          const uint32_t oa = ob + x;
+          const uint32_t ca = a.cam[oa], ga = a.icam[oa];
+          const T* Wha = wsc + (int64_t)x * SLOT + 3 * B;
+          for (uint32_t y = 0; y < m; ++y) {
+            const uint32_t obb = ob + y;
+            const uint32_t cb = a.cam[obb], gb = a.icam[obb];
+            const T* Wb = wsc + (int64_t)y * SLOT;
+            for (int e = lane; e < B * B; e += 32) {
+              const int i = e / B, j = e % B;
+              const int ci = i < 6 ? a.ext_col[6 * (int64_t)ca + i] : a.intr_col[K * (int64_t)ga + (i - 6)];
+              const int cj = j < 6 ? a.ext_col[6 * (int64_t)cb + j] : a.intr_col[K * (int64_t)gb + (j - 6)];
+              if (ci < 0 || cj < 0 || cj > ci) continue;
+              Sadd(tri(ci, cj),
+                   (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
+            }
           }
         }
       }
       __syncwarp();
     }
     __syncthreads();
+    if constexpr (kGS) {
+      for (int i = tid; i < n; i += kThreads) sh.rhs[i] = (SS)__ldcg(g_rhs + i);
+      __syncthreads();
+    }
     // ---- Cholesky of S (outer-product elimination, one barrier per column)
     for (int j = 0; j < n; ++j) {
-      SS d = sh.S[tri(j, j)];
+      SS d = Sld(tri(j, j));
       if (!(d > SS(0)) || !isfinite((double)d)) {
         d = SS(1);
         if (tid == 0) {
           sh.flag = 1;
-          sh.S[tri(j, j)] = d;
+          Sst(tri(j, j), d);
         }
       }
       const SS invd = SS(1) / d;
-      const int mm = n - 1 - j;
-      for (int idx = tid; idx < mm * mm; idx += kThreads) {
-        const int i = j + 1 + idx / mm, l = j + 1 + idx % mm;
-        if (l <= i) sh.S[tri(i, l)] -= sh.S[tri(i, j)] * sh.S[tri(l, j)] * invd;
+      // trailing update of the lower triangle: rows by warp, columns by lane
+      for (int i = j + 1 + warp; i < n; i += kWarps) {
+        const SS sij = Sld(tri(i, j)) * invd;
+        const int ri = tri(i, 0);
+        for (int l = j + 1 + lane; l <= i; l += 32) Sst(ri + l, Sld(ri + l) - sij * Sld(tri(l, j)));
       }
       __syncthreads();
     }
-    for (int j = tid; j < n; j += kThreads) sh.z[j] = sqrt(sh.S[tri(j, j)]);
+    for (int j = tid; j < n; j += kThreads) sh.z[j] = sqrt(Sld(tri(j, j)));
     __syncthreads();
-    for (int idx = tid; idx < n * (n + 1) / 2; idx += kThreads) {
-      int i = (int)((sqrt(8.0 * idx + 1.0) - 1.0) * 0.5);
-      while (tri(i + 1, 0) <= idx) ++i;
-      while (tri(i, 0) > idx) --i;
-      const int j = idx - tri(i, 0);
-      if (j < i) sh.S[idx] /= sh.z[j];
+    for (int i = warp; i < n; i += kWarps) {
+      const int ri = tri(i, 0);
+      for (int j = lane; j < i; j += 32) Sst(ri + j, Sld(ri + j) / sh.z[j]);
     }
     __syncthreads();
-    for (int j = tid; j < n; j += kThreads) sh.S[tri(j, j)] = sh.z[j];
+    for (int j = tid; j < n; j += kThreads) Sst(tri(j, j), sh.z[j]);
     __syncthreads();
     // forward L y = rhs (column oriented), then backward L^T z = y; z holds the solution
     for (int j = 0; j < n; ++j) {
-      const SS yj = sh.rhs[j] / sh.S[tri(j, j)];
-      for (int i = j + 1 + tid; i < n; i += kThreads) sh.rhs[i] -= sh.S[tri(i, j)] * yj;
+      const SS yj = sh.rhs[j] / Sld(tri(j, j));
+      for (int i = j + 1 + tid; i < n; i += kThreads) sh.rhs[i] -= Sld(tri(i, j)) * yj;
       __syncthreads();
       if (tid == 0) sh.rhs[j] = yj;
       __syncthreads();
     }
     for (int j = n - 1; j >= 0; --j) {
-      const SS xj = sh.rhs[j] / sh.S[tri(j, j)];
-      for (int i = tid; i < j; i += kThreads) sh.rhs[i] -= sh.S[tri(j, i)] * xj;
+      const SS xj = sh.rhs[j] / Sld(tri(j, j));
+      for (int i = tid; i < j; i += kThreads) sh.rhs[i] -= Sld(tri(j, i)) * xj;
       __syncthreads();
       if (tid == 0) sh.z[j] = xj;
       __syncthreads();
@@ -464,7 +637,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
         T fz0 = T(0), fz1 = T(0);
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -490,7 +663,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
         double m0 = 0.0, m1 = 0.0;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -532,6 +705,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     mcc = block_sum(mcc, sh.red, &sh.bcast[3]);
     stp = block_sum(stp, sh.red, &sh.bcast[4]);
     __threadfence_block();
+    make_poses(a.ext2, 1);
     bool cfinite = true;
     const double new_cost_raw = cost_at(a.ext2, a.intr2, a.pts2, &cfinite);
     ++iter;
@@ -569,6 +743,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads) a.pts[3 * (int64_t)P.x0 + i] = a.pts2[3 * (int64_t)P.x0 + i];
       for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) a.ext[6 * (int64_t)P.c0 + i] = a.ext2[6 * (int64_t)P.c0 + i];
       for (uint32_t i = tid; i < K * P.ni; i += kThreads) a.intr[K * (int64_t)P.g0 + i] = a.intr2[K * (int64_t)P.g0 + i];
+      if (use_pose)
+        for (uint32_t i = tid; i < 12 * P.nc; i += kThreads) sh.pose[0][i] = sh.pose[1][i];
       __syncthreads();
       linearize(false, &gmax, &xnorm);
       if (gmax <= a.gtol) term = GBBA_CONVERGENCE;
@@ -598,7 +774,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   const int mem = probs[0].memory;
   const int k = model == kPinholeF ? 1 : model == kRadialK3 ? 6 : 8;
   const bool fp64 = o->precision == GBBA_PRECISION_FP64;
-  const int nmax = fp64 ? NMax<double>::v : NMax<float>::v;
+  const int nmax = kNMax;
   cudaStream_t st = h->active;
   // sizes, offsets and problem-local reduced column maps (host)
   std::vector<BProb> bp(np_);
@@ -682,6 +858,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
       BProb* probs;
       BOut* out;
       void *Vinv, *gp, *wsc;
+      double* gscr;
     } q;
     q.ext = A.template take<double>(6 * tc); q.intr = A.template take<double>(k * tg); q.pts = A.template take<double>(3 * tx);
     q.ext2 = A.template take<double>(6 * tc); q.intr2 = A.template take<double>(k * tg); q.pts2 = A.template take<double>(3 * tx);
@@ -695,7 +872,8 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     q.ecol = A.template take<int32_t>(6 * tc); q.icol = A.template take<int32_t>(k * tg); q.ivar = A.template take<uint8_t>(tg);
     q.probs = A.template take<BProb>(np_); q.out = A.template take<BOut>(2 * np_);
     q.Vinv = A.template take<char>(6 * tx * tsize); q.gp = A.template take<char>(3 * tx * tsize);
-    q.wsc = A.template take<char>((size_t)np_ * kWarps * max_views * 6 * B * tsize);
+    q.wsc = A.template take<char>((size_t)np_ * kWarps * (max_views + 1) * (6 * B + k * (k + 1) / 2 + k) * tsize);
+    q.gscr = A.template take<double>((size_t)np_ * kGlobalSlice);
     return q;
   };
   plan(pl);
@@ -783,7 +961,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   a.ext = q.ext; a.intr = q.intr; a.pts = q.pts; a.ext2 = q.ext2; a.intr2 = q.intr2; a.pts2 = q.pts2;
   a.obs = q.obs; a.cam = q.cam_s; a.icam = q.icam_s; a.pt_off = q.off;
   a.ext_col = q.ecol; a.intr_col = q.icol; a.intr_var = q.ivar;
-  a.scale_p = q.scale_p; a.diag_p = q.diag_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc;
+  a.scale_p = q.scale_p; a.diag_p = q.diag_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc; a.gscr = q.gscr;
   a.max_views = max_views; a.out = q.out;
   a.max_iterations = o->max_num_iterations; a.max_invalid = o->max_num_consecutive_invalid_steps;
   a.jacobi = o->jacobi_scaling; a.loss_type = o->loss_type; a.loss_a = o->loss_scale;
@@ -794,50 +972,29 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   GBBA_CUDA(cudaEventCreate(&e0));
   GBBA_CUDA(cudaEventCreate(&e1));
   GBBA_CUDA(cudaEventRecord(e0, st));
-  // Problems whose reduced system fits shared memory in FP64 keep S, its
-  // factor and the step in FP64 (the mixed path then only has FP32 Jacobians);
-  // larger windows of the mixed path keep S in FP32.  The order list holds the
-  // FP64-S problems first, each group largest first.
-  int n64 = 0;
-  {
-    std::vector<uint32_t> o64, o32;
-    for (uint32_t i : order) (bp[i].n <= (uint32_t)NMax<double>::v ? o64 : o32).push_back(i);
-    n64 = (int)o64.size();
-    o64.insert(o64.end(), o32.begin(), o32.end());
-    GBBA_CUDA(cudaMemcpyAsync(q.order, o64.data(), 4 * np_, cudaMemcpyHostToDevice, st));
-    GBBA_CUDA(cudaStreamSynchronize(st));
-  }
   BArgs* base = &a;
-  auto launch = [&](auto kern, size_t smem, int count, int first) {
-    if (count <= 0) return;
+  auto launch = [&](auto kern, size_t smem) {
+    if (np_ <= 0) return;
     GBBA_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    BArgs b = *base;
-    b.order = q.order + first;
-    b.wscratch = (char*)q.wsc + (size_t)first * kWarps * max_views * 6 * B * tsize;
-    kern<<<count, kThreads, smem, st>>>(b);
+    kern<<<np_, kThreads, smem, st>>>(*base);
     check_launch(h);
   };
-  const size_t sm64 = sizeof(Shared<double, NMax<double>::v>), sm32 = sizeof(Shared<float, NMax<float>::v>);
+  // FP64: S in the global slice (small shared footprint); mixed: FP32 S in
+  // shared memory
+  const size_t sm64 = sizeof(SharedOf<double>::type), sm32 = sizeof(SharedOf<float>::type);
   if (fp64) {
-    if (model == kPinholeF) launch(k_lm_batched<kPinholeF, double, double>, sm64, n64, 0);
-    else if (model == kRadialK3) launch(k_lm_batched<kRadialK3, double, double>, sm64, n64, 0);
-    else launch(k_lm_batched<kBrownT2, double, double>, sm64, n64, 0);
+    if (model == kPinholeF) launch(k_lm_batched<kPinholeF, double, double>, sm64);
+    else if (model == kRadialK3) launch(k_lm_batched<kRadialK3, double, double>, sm64);
+    else launch(k_lm_batched<kBrownT2, double, double>, sm64);
   } else {
-    if (model == kPinholeF) {
-      launch(k_lm_batched<kPinholeF, float, double>, sm64, n64, 0);
-      launch(k_lm_batched<kPinholeF, float, float>, sm32, np_ - n64, n64);
-    } else if (model == kRadialK3) {
-      launch(k_lm_batched<kRadialK3, float, double>, sm64, n64, 0);
-      launch(k_lm_batched<kRadialK3, float, float>, sm32, np_ - n64, n64);
-    } else {
-      launch(k_lm_batched<kBrownT2, float, double>, sm64, n64, 0);
-      launch(k_lm_batched<kBrownT2, float, float>, sm32, np_ - n64, n64);
-    }
+    if (model == kPinholeF) launch(k_lm_batched<kPinholeF, float, float>, sm32);
+    else if (model == kRadialK3) launch(k_lm_batched<kRadialK3, float, float>, sm32);
+    else launch(k_lm_batched<kBrownT2, float, float>, sm32);
   }
   // Mixed path: the FP64 kernel continues from the mixed solution (its own
-  // LM restart, at most 10 iterations, tolerances 1000x tighter) on the
-  // problems that fit it, so that the final iterates carry FP64 Jacobians and
-  // steps and end at the minimum rather than anywhere inside the stopping band
+  // LM restart, at most fp64_polish_iterations iterations, tolerances 1000x
+  // tighter), so that the final iterates carry FP64 Jacobians and steps and
+  // end at the minimum rather than anywhere inside the stopping band
   // |dcost| <= 1e-6 cost.
   const bool polish = !fp64 && o->fp64_polish_iterations > 0;
   BArgs pol = a;
@@ -847,18 +1004,9 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     pol.ftol = a.ftol * 1e-3;  // converge past ceres's 1e-6 stopping band
     pol.ptol = a.ptol * 1e-3;
     base = &pol;
-    // windows whose S does not fit shared memory in FP64 polish with FP64
-    // Jacobians and an FP32 S
-    if (model == kPinholeF) {
-      launch(k_lm_batched<kPinholeF, double, double>, sm64, n64, 0);
-      launch(k_lm_batched<kPinholeF, double, float>, sm32, np_ - n64, n64);
-    } else if (model == kRadialK3) {
-      launch(k_lm_batched<kRadialK3, double, double>, sm64, n64, 0);
-      launch(k_lm_batched<kRadialK3, double, float>, sm32, np_ - n64, n64);
-    } else {
-      launch(k_lm_batched<kBrownT2, double, double>, sm64, n64, 0);
-      launch(k_lm_batched<kBrownT2, double, float>, sm32, np_ - n64, n64);
-    }
+    if (model == kPinholeF) launch(k_lm_batched<kPinholeF, double, double>, sm64);
+    else if (model == kRadialK3) launch(k_lm_batched<kRadialK3, double, double>, sm64);
+    else launch(k_lm_batched<kBrownT2, double, double>, sm64);
   }
   GBBA_CUDA(cudaEventRecord(e1, st));
   std::vector<BOut> out(2 * np_);
