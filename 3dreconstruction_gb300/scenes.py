@@ -275,6 +275,21 @@ def local_batch(num_problems=4096, seed=4, cams=(5, 40), points=(200, 5000), mod
     return out
 
 
+def local_window(seed, index, cams=(5, 40), points=(200, 5000), model=abi.BROWN_T2, hold_second=True):
+    """Window `index` of the batched local-BA workload, from its own seeded
+    generator (so that windows can be generated in parallel): cameras uniform
+    in `cams`, points uniform in `points`, one Brown-T2 intrinsic group.  With
+    hold_second, camera 1 is held besides the gauge camera 0, which fixes the
+    scale so that each window's minimum is isolated."""
+    rng = np.random.default_rng([seed, index])
+    c = int(rng.integers(cams[0], cams[1] + 1))
+    p = int(rng.integers(points[0], points[1] + 1))
+    prob = local_problem(rng, c, p, model=model)
+    if hold_second:
+        prob["camera_constant"][1] = 1
+    return prob
+
+
 def track_scene(num_cameras=200, num_tracks=1_000_000, seed=2, radius=15.0, extent=3.0, sigma=1.0,
                 min_len=2, max_len=30, f_range=(800.0, 1200.0)):
     """Batched-triangulation workload: tracks as CSR over a camera table."""

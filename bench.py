@@ -206,6 +206,51 @@ def measure_triangulation(h, torch, steps, warmup):
             "algorithmic_bytes": tri_algorithmic_bytes(no, nt), "tracks_ok_frac": ok}
 
 
+def _local_window(args):
+    seed, index = args
+    return importlib.import_module("3dreconstruction_gb300.scenes").local_window(seed, index)
+
+
+def measure_batched(h, abi, windows, seed=4):
+    """Batched local BA (gbba_solve_batched): `windows` independent windows of
+    the 4,096-window workload's distributions (5-40 cameras, 200-5,000 points,
+    Brown-T2, one intrinsic group, cameras 0 and 1 held).  The plain FP64
+    batched solve gives each window's C*; the mixed solve, without and with its
+    FP64 polish, is timed and checked window by window against
+    (1 + 1e-6) C*.  Times are whole C-ABI calls from host buffers."""
+    import multiprocessing as mp
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
+        probs = pool.map(_local_window, [(seed, i) for i in range(windows)], chunksize=4)
+    gen_s = time.perf_counter() - t0
+    nobs = np.array([len(p["observations"]) for p in probs], dtype=np.float64)
+
+    def run(prec, polish):
+        hps = [abi.HostProblem(p) for p in probs]
+        structs = (abi.GbbaProblem * len(hps))(*[hp.struct() for hp in hps])
+        sums = (abi.GbbaSummary * len(hps))()
+        o = abi.default_options(precision=prec)
+        o.max_num_iterations = 100
+        o.fp64_polish_iterations = polish
+        t = time.perf_counter()
+        h.check(h.lib.gbba_solve_batched(h.h, structs, len(hps), ctypes.byref(o), sums), "gbba_solve_batched")
+        dt = time.perf_counter() - t
+        costs = np.array([s.final_cost for s in sums])
+        its = np.array([s.num_iterations for s in sums], dtype=np.float64)
+        return {"seconds": dt, "iterations": int(its.sum()), "obs_iter_per_s": float((nobs * its).sum() / dt)}, costs
+
+    fp64, cstar = run(abi.PRECISION_FP64, 0)
+    out = {"workload": f"local{windows}: {windows} windows, cameras U{{5..40}}, points U{{200..5000}}, Brown-T2, "
+                       "one intrinsic group, cameras 0 and 1 held",
+           "observations": int(nobs.sum()), "generation_s": gen_s, "fp64": fp64}
+    for name, polish in (("mixed", 0), ("mixed_fp64_polish", 10)):
+        r, costs = run(abi.PRECISION_MIXED, polish)
+        r["reaches_cstar_frac"] = float(np.mean(costs <= cstar * (1 + 1e-6)))
+        r["speedup_vs_fp64"] = fp64["seconds"] / r["seconds"]
+        out[name] = r
+    return out
+
+
 def make_scene(workload):
     scenes = importlib.import_module("3dreconstruction_gb300.scenes")
     if workload == "medium":
@@ -419,6 +464,8 @@ def run_ours(args):
         line["time_to_cost"] = ttc
     if rank == 0 and args.triangulation:
         line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup)
+    if rank == 0 and args.batched_windows > 0:
+        line["batched"] = measure_batched(h, abi, args.batched_windows)
     if rank == 0 and args.cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(scene, opts, os.cpu_count() or 1).items()
                                 if k != "seconds"}
@@ -441,6 +488,8 @@ def main():
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")
+    ap.add_argument("--batched-windows", type=int, default=512,
+                    help="windows of the batched local-BA measurement (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
