@@ -75,10 +75,10 @@ def factor_flops(n_red):
     return n_red ** 3 / 3.0 + 2.0 * n_red ** 2
 
 
-# DRAM bytes (read + write) of one Schur phase on the medium workload, from
-# ncu's dram__bytes_read.sum + dram__bytes_write.sum summed over the phase's
-# kernels (profiles/schur_phase_medium.md); None until captured.
-SCHUR_TRAFFIC_PER_PHASE = None
+# DRAM bytes (read + write) of one Schur phase on the medium workload: ncu's
+# dram__bytes_read.sum + dram__bytes_write.sum summed over the phase's four
+# kernels (profiles/schur_phase_medium.md).
+SCHUR_TRAFFIC_PER_PHASE = 4.65e9
 
 # FP32 SIMT peak of a GB300: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
