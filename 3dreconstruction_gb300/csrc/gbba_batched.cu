@@ -72,6 +72,10 @@ struct BArgs {
   double *scale_p, *diag_p;
   void *Vinv, *gp, *wscratch;  // compute type
   double* gscr;                // kGlobalSlice doubles per CTA
+  // FP32 path: per observation, the corrected FP64 residual and sqrt(rho')
+  // at the current parameters and at the candidate ([2][3 * total_obs])
+  double* rcache;
+  int64_t total_obs;
   int max_views;
   BOut* out;
   // options
@@ -135,11 +139,15 @@ __device__ __forceinline__ double block_max(double v, double* red, double* out) 
 // With pose (FP64 pose_matrix of the problem's cameras, indexed from the
 // problem's first camera c0), the FP32 path takes its FP64 residual from it
 // instead of the Rodrigues sine / cosine per observation.
+//
+// With rc (FP32 path), the corrected residual and sqrt(rho') are taken from
+// the residual cache written by the cost evaluation at the same parameters,
+// and only the FP32 Jacobian is evaluated.
 template <int M, typename T>
 __device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, const double* intr, const double* pts,
                                            int64_t o, uint32_t p, double r[2], T Jc[2][6 + Model<M>::K], T Jp[2][3],
                                            int col[6 + Model<M>::K], const double* pose = nullptr,
-                                           uint32_t c0 = 0) {
+                                           uint32_t c0 = 0, const double* rc = nullptr) {
   constexpr int K = Model<M>::K;
   const uint32_t c = a.cam[o], g = a.icam[o];
   const double2 ob = a.obs[o];
@@ -154,6 +162,33 @@ __device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, co
   if constexpr (sizeof(T) == 8) {
     residual<M, double, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (double*)nullptr);
   } else {
+    if (rc) {
+      T Ef[6], Kf[K], Xf[3], rf[2];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
+#pragma unroll
+      for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
+      residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
+      r[0] = rc[0];
+      r[1] = rc[1];
+#pragma unroll
+      for (int j = 0; j < 6; ++j) col[j] = a.ext_col[6 * (int64_t)c + j];
+#pragma unroll
+      for (int j = 0; j < K; ++j) col[6 + j] = a.intr_col[K * (int64_t)g + j];
+      const T s = (T)rc[2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) Jc[i][j] = Je[i][j] * s;
+#pragma unroll
+        for (int j = 0; j < K; ++j) Jc[i][6 + j] = Jk[i][j] * s;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) Jp[i][j] = Jx[i][j] * s;
+      }
+      return 0.0;
+    }
     if (pose) {
       residual_pose<M, double>(Kd, pose + 12 * (c - c0), Xd, ob.x, ob.y, r);
     } else {
@@ -237,6 +272,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   };
 
   const bool use_pose = P.nc <= (uint32_t)kPoseCams;
+  // residual cache (FP32 path): slot `cur` holds the current parameters'
+  constexpr bool kCache = sizeof(T) == 4;
+  int cur = 0;
+  auto rc_at = [&](int64_t o) -> const double* {
+    return kCache ? a.rcache + (int64_t)cur * 3 * a.total_obs + 3 * o : nullptr;
+  };
   // poses of ext (slot 0) or ext2 (slot 1); the barrier makes them visible
   auto make_poses = [&](const double* ext, int slot) {
     if (use_pose) {
@@ -252,6 +293,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   const double* pose_x = use_pose ? sh.pose[0] : nullptr;
   auto cost_at = [&](const double* ext, const double* intr, const double* pts, bool* finite) -> double {
     const double* pz = !use_pose ? nullptr : ext == a.ext ? sh.pose[0] : sh.pose[1];
+    double* wc = kCache ? a.rcache + (int64_t)(ext == a.ext ? cur : cur ^ 1) * 3 * a.total_obs : nullptr;
     double acc = 0.0;
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       // obs of point p are [pt_off[p], pt_off[p+1])
@@ -266,6 +308,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         else residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
         double sr1;
         acc += robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+        if (wc) {
+          wc[3 * (int64_t)o] = r[0] * sr1;
+          wc[3 * (int64_t)o + 1] = r[1] * sr1;
+          wc[3 * (int64_t)o + 2] = sr1;
+        }
       }
     }
     const double c = block_sum(acc, sh.red, &sh.bcast[0]);
@@ -287,7 +334,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
@@ -393,7 +440,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           const T s = col[j] >= 0 ? (T)sh.scale_c[col[j]] : T(0);
@@ -637,7 +684,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
         T fz0 = T(0), fz1 = T(0);
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -663,7 +710,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0);
+        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
         double m0 = 0.0, m1 = 0.0;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
@@ -745,6 +792,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       for (uint32_t i = tid; i < K * P.ni; i += kThreads) a.intr[K * (int64_t)P.g0 + i] = a.intr2[K * (int64_t)P.g0 + i];
       if (use_pose)
         for (uint32_t i = tid; i < 12 * P.nc; i += kThreads) sh.pose[0][i] = sh.pose[1][i];
+      cur ^= 1;  // the candidate's residual cache becomes the current one
       __syncthreads();
       linearize(false, &gmax, &xnorm);
       if (gmax <= a.gtol) term = GBBA_CONVERGENCE;
@@ -859,6 +907,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
       BOut* out;
       void *Vinv, *gp, *wsc;
       double* gscr;
+      double* rcache;
     } q;
     q.ext = A.template take<double>(6 * tc); q.intr = A.template take<double>(k * tg); q.pts = A.template take<double>(3 * tx);
     q.ext2 = A.template take<double>(6 * tc); q.intr2 = A.template take<double>(k * tg); q.pts2 = A.template take<double>(3 * tx);
@@ -874,6 +923,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     q.Vinv = A.template take<char>(6 * tx * tsize); q.gp = A.template take<char>(3 * tx * tsize);
     q.wsc = A.template take<char>((size_t)np_ * kWarps * (max_views + 1) * (6 * B + k * (k + 1) / 2 + k) * tsize);
     q.gscr = A.template take<double>((size_t)np_ * kGlobalSlice);
+    q.rcache = A.template take<double>((size_t)6 * std::max<int64_t>(to, 1));
     return q;
   };
   plan(pl);
@@ -962,6 +1012,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   a.obs = q.obs; a.cam = q.cam_s; a.icam = q.icam_s; a.pt_off = q.off;
   a.ext_col = q.ecol; a.intr_col = q.icol; a.intr_var = q.ivar;
   a.scale_p = q.scale_p; a.diag_p = q.diag_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc; a.gscr = q.gscr;
+  a.rcache = q.rcache; a.total_obs = to;
   a.max_views = max_views; a.out = q.out;
   a.max_iterations = o->max_num_iterations; a.max_invalid = o->max_num_consecutive_invalid_steps;
   a.jacobi = o->jacobi_scaling; a.loss_type = o->loss_type; a.loss_a = o->loss_scale;
