@@ -576,33 +576,49 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
                          sums[3 * i + 2] * sums[3 * K + 3 * j + 2];
           Sadd(tri(ci, cj), (SS)(-sacc));
         }
-        // S_k,c(y) -= Wh_K W_ey^T for every observation y
-        for (uint32_t y = 0; y < m; ++y) {
+        // S_k,c(y) -= Wh_K W_ey^T for every observation y: work items (y, i, j)
+        for (uint32_t t = lane; t < m * 6 * K; t += 32) {
+          const uint32_t y = t / (6 * K), e = t % (6 * K);
+          const int i = e / 6, j = e % 6;
           const uint32_t cb = a.cam[ob + y];
+          const int ci = kcol[i], cj = a.ext_col[6 * (int64_t)cb + j];
+          if (ci < 0 || cj < 0) continue;
           const T* Wy = wsc + (int64_t)y * SLOT;
-          for (int e = lane; e < 6 * K; e += 32) {
-            const int i = e / 6, j = e % 6;
-            const int ci = kcol[i], cj = a.ext_col[6 * (int64_t)cb + j];
-            if (ci < 0 || cj < 0) continue;
-            const T sacc = sums[3 * i] * Wy[3 * j] + sums[3 * i + 1] * Wy[3 * j + 1] + sums[3 * i + 2] * Wy[3 * j + 2];
-            Sadd(tri(ci, cj), (SS)(-sacc));
-          }
+          const T sacc = sums[3 * i] * Wy[3 * j] + sums[3 * i + 1] * Wy[3 * j + 1] + sums[3 * i + 2] * Wy[3 * j + 2];
+          Sadd(tri(ci, cj), (SS)(-sacc));
         }
-        // extrinsic blocks: pairs with camera a > b, and each observation's own block
-        for (uint32_t x = 0; x < m; ++x) {
-          const uint32_t ca = a.cam[ob + x];
-          const T* Wha = wsc + (int64_t)x * SLOT + 3 * B;
-          for (uint32_t y = 0; y < m; ++y) {
-            const uint32_t cb = a.cam[ob + y];
-            if (cb > ca) continue;
-            const T* Wb = wsc + (int64_t)y * SLOT;
-            for (int e = lane; e < 36; e += 32) {
-              const int i = e / 6, j = e % 6;
-              const int ci = a.ext_col[6 * (int64_t)ca + i], cj = a.ext_col[6 * (int64_t)cb + j];
-              if (ci < 0 || cj < 0 || cj > ci) continue;
-              Sadd(tri(ci, cj),
-                   (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
+        // extrinsic blocks: work items (unordered observation pair x >= y, i, j).
+        // The pair's block is taken with the higher camera's observation first
+        // (its entries are all in the lower triangle); an observation's own
+        // block and a camera that sees the point twice keep the lower part of
+        // both orders.
+        const uint32_t nq = m * (m + 1) / 2;
+        for (uint32_t t = lane; t < nq * 36; t += 32) {
+          const uint32_t q = t / 36, e = t % 36;
+          uint32_t x = (uint32_t)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
+          while ((x + 1) * (x + 2) / 2 <= q) ++x;
+          while (x * (x + 1) / 2 > q) --x;
+          const uint32_t y = q - x * (x + 1) / 2;
+          const uint32_t cx = a.cam[ob + x], cy = a.cam[ob + y];
+          const int i = e / 6, j = e % 6;
+          for (int side = 0; side < 2; ++side) {
+            uint32_t u = x, w = y;
+            if (side == 0) {
+              if (cx < cy) {
+                u = y;
+                w = x;
+              }
+            } else {
+              if (!(cx == cy && x != y)) break;
+              u = y;
+              w = x;
             }
+            const uint32_t cu = side == 0 && cx < cy ? cy : cx, cw = side == 0 && cx < cy ? cx : cy;
+            const int ci = a.ext_col[6 * (int64_t)cu + i], cj = a.ext_col[6 * (int64_t)cw + j];
+            if (ci < 0 || cj < 0 || cj > ci) continue;
+            const T* Whu = wsc + (int64_t)u * SLOT + 3 * B;
+            const T* Ww = wsc + (int64_t)w * SLOT;
+            Sadd(tri(ci, cj), (SS)(-(Whu[3 * i] * Ww[3 * j] + Whu[3 * i + 1] * Ww[3 * j + 1] + Whu[3 * i + 2] * Ww[3 * j + 2])));
           }
         }
       } else {
