@@ -239,7 +239,7 @@ gbba_status gbba_create(int device, gbba_handle** out) {
     GBBA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, least));
     GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_main, cudaEventDisableTiming));
     GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_side, cudaEventDisableTiming));
-    GBBA_CUDA(cudaHostAlloc((void**)&h->pinned, 64 * sizeof(double), cudaHostAllocDefault));
+    GBBA_CUDA(cudaHostAlloc((void**)&h->pinned, 256 * sizeof(double), cudaHostAllocDefault));
     GBBA_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
   } catch (const Error& e) {
     delete h;

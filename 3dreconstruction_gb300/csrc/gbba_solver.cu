@@ -283,11 +283,14 @@ __global__ void k_scale_diag(int64_t n, const double* cn, const double* g, doubl
 }
 
 // S <- diag(D_c^2) (identity on the padding), rhs <- 0.
+// With fused, the camera diagonal D_c^2 / radius is added later in the same
+// iteration (k_rhs_camera forms it from the current Jacobian).
 template <typename T>
-__global__ void k_schur_init(T* S, T* rhs, int64_t n, int64_t n_pad, const double* diag_c, const double* radius) {
+__global__ void k_schur_init(T* S, T* rhs, int64_t n, int64_t n_pad, const double* diag_c, const double* radius,
+                             int fused) {
   const double rad = *radius;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad; i += (int64_t)gridDim.x * blockDim.x) {
-    S[i * n_pad + i] = i < n ? (T)(diag_c[i] / rad) : T(1);
+    S[i * n_pad + i] = i < n ? (fused ? T(0) : (T)(diag_c[i] / rad)) : T(1);
     rhs[i] = T(0);
   }
 }
@@ -489,11 +492,25 @@ __global__ void k_pt_groups(const uint32_t* __restrict__ pt_off, int64_t np, con
 }
 
 // Stage 1, one warp per point group: V, V^-1, g_p and the observation records.
+// The LM diagonal of a point's columns is formed here from the current
+// Jacobian (D_p^2 = clamp(diag(Jp'Jp))), stored in diag_p; the point's
+// gradient max norm (unscaled) goes into one of kGmaxShards slots.
+constexpr int kGmaxShards = 64;
+__device__ __forceinline__ void gmax_update(unsigned long long* shards, double m) {
+  if (!shards) return;  // no gradient tolerance: the norm is not needed
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0)
+    atomicMax(shards + (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) & (kGmaxShards - 1)),
+              (unsigned long long)__double_as_longlong(m));
+}
+
 template <int M, typename T>
 __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                          const double* __restrict__ scale_c,
                                                          const double* __restrict__ scale_p,
-                                                         const double* __restrict__ diag_p,
+                                                         double* __restrict__ diag_p, double dmin, double dmax,
+                                                         unsigned long long* __restrict__ gmax_shards,
                                                          const double* __restrict__ radius, T* __restrict__ Vinv,
                                                          T* __restrict__ gp, T* __restrict__ rec,
                                                          int* __restrict__ flag) {
@@ -540,15 +557,26 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     for (int i = 0; i < 6; ++i) v[i] = __shfl_sync(0xffffffffu, v[i], tail);
 #pragma unroll
     for (int i = 0; i < 3; ++i) g[i] = __shfl_sync(0xffffffffu, g[i], tail);
+    double gm = 0.0;
+    if (gmax_shards && valid && lane == head) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) gm = fmax(gm, fabs((double)g[j] / scale_p[3 * (int64_t)p + j]));
+    }
+    gmax_update(gmax_shards, gm);
     if (!valid) return;
+    const double dp[3] = {fmin(fmax((double)v[0], dmin), dmax), fmin(fmax((double)v[3], dmin), dmax),
+                          fmin(fmax((double)v[5], dmin), dmax)};
     T vi[6];
-    const bool ok = point_vinv<T>(v, diag_p + 3 * (int64_t)p, rad, vi);
+    const bool ok = point_vinv<T>(v, dp, rad, vi);
     if (lane == head) {
       if (!ok) atomicExch(flag, 2);
 #pragma unroll
       for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
 #pragma unroll
-      for (int i = 0; i < 3; ++i) gp[3 * (int64_t)p + i] = g[i];
+      for (int i = 0; i < 3; ++i) {
+        gp[3 * (int64_t)p + i] = g[i];
+        diag_p[3 * (int64_t)p + i] = dp[i];
+      }
     }
     const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
     const T r0 = (T)J.r[0], r1 = (T)J.r[1];
@@ -648,14 +676,25 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
   for (int i = 0; i < 6; ++i) v[i] = warp_sum(v[i]);
 #pragma unroll
   for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
+  double gm = 0.0;
+  if (gmax_shards && lane == 0) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) gm = fmax(gm, fabs((double)g[j] / scale_p[3 * (int64_t)p + j]));
+  }
+  gmax_update(gmax_shards, gm);
+  const double dp[3] = {fmin(fmax((double)v[0], dmin), dmax), fmin(fmax((double)v[3], dmin), dmax),
+                        fmin(fmax((double)v[5], dmin), dmax)};
   T vi[6];
-  const bool ok = point_vinv<T>(v, diag_p + 3 * (int64_t)p, rad, vi);
+  const bool ok = point_vinv<T>(v, dp, rad, vi);
   if (lane == 0) {
     if (!ok) atomicExch(flag, 2);
 #pragma unroll
     for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) gp[3 * (int64_t)p + i] = g[i];
+    for (int i = 0; i < 3; ++i) {
+      gp[3 * (int64_t)p + i] = g[i];
+      diag_p[3 * (int64_t)p + i] = dp[i];
+    }
   }
   const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
   for (uint32_t o = o0 + lane; o < o1; o += 32) {
@@ -938,10 +977,15 @@ __global__ void __launch_bounds__(128) k_pair_merge(const PairMerge* __restrict_
   write_block<B, T>((uint32_t)(m.key / nc), (uint32_t)(m.key % nc), acc, lane, ext_col, intr_col, cam_group, K, S, ld);
 }
 
-// Stage 3, one block of 256 threads per camera: rhs of the camera's columns =
-// sum of q over the camera's observations.  Thread t sums observations
-// t, t+256, ... of the camera CSR; the per-thread sums are reduced by a warp
-// butterfly and then over the eight warps in order (a fixed order).
+// Stage 3, one block of 256 threads per camera, from the observation records
+// of the camera (camera CSR):
+//   rhs of the camera's columns = sum of q,
+//   column norms of the scaled, corrected Jacobian -> LM diagonal
+//   D_c^2 = clamp(sum Jc^2), stored in diag_c and (dense) added to S's
+//   diagonal as D_c^2 / radius, and the camera gradient's max norm
+//   (unscaled, sum Jc r / scale) into the gradient shards.
+// Thread t sums observations t, t+256, ...; the per-thread sums are reduced
+// by a warp butterfly and then over the eight warps in order (a fixed order).
 constexpr int kRhsThreads = 256;
 template <int B, typename T>
 __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __restrict__ cam_off,
@@ -950,32 +994,63 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
                                                             const int32_t* __restrict__ ext_col,
                                                             const int32_t* __restrict__ intr_col,
                                                             const int32_t* __restrict__ cam_group, int K, int64_t nc,
-                                                            T* __restrict__ rhs) {
+                                                            T* __restrict__ rhs, const double* __restrict__ scale_c,
+                                                            double* __restrict__ diag_c, double dmin, double dmax,
+                                                            const double* __restrict__ radius, T* __restrict__ S,
+                                                            int64_t ld, unsigned long long* __restrict__ gmax_shards) {
   using R = Rec<B>;
-  __shared__ T part[kRhsThreads / 32][B];
+  __shared__ T part[3][kRhsThreads / 32][B];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c = blockIdx.x;
-  T acc[B];
+  T acc[B], nrm[B], grd[B];
 #pragma unroll
-  for (int i = 0; i < B; ++i) acc[i] = T(0);
+  for (int i = 0; i < B; ++i) acc[i] = nrm[i] = grd[i] = T(0);
   for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
-    const T* r = rec + (int64_t)cam_obs[q] * R::kSize + R::kQ;
+    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+    const T r0 = r[R::kR], r1 = r[R::kR + 1];
 #pragma unroll
-    for (int i = 0; i < B; ++i) acc[i] += r[i];
+    for (int i = 0; i < B; ++i) {
+      const T j0 = r[R::kJc + i], j1 = r[R::kJc + B + i];
+      acc[i] += r[R::kQ + i];
+      nrm[i] += j0 * j0 + j1 * j1;
+      grd[i] += j0 * r0 + j1 * r1;
+    }
   }
 #pragma unroll
-  for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
+  for (int i = 0; i < B; ++i) {
+    acc[i] = warp_sum(acc[i]);
+    nrm[i] = warp_sum(nrm[i]);
+    grd[i] = warp_sum(grd[i]);
+  }
   if (lane == 0) {
 #pragma unroll
-    for (int i = 0; i < B; ++i) part[warp][i] = acc[i];
+    for (int i = 0; i < B; ++i) {
+      part[0][warp][i] = acc[i];
+      part[1][warp][i] = nrm[i];
+      part[2][warp][i] = grd[i];
+    }
   }
   __syncthreads();
   if (threadIdx.x < B) {
+    const int i = threadIdx.x;
     T v = T(0);
+    double cn = 0.0, g = 0.0;
 #pragma unroll
-    for (int w = 0; w < kRhsThreads / 32; ++w) v += part[w][threadIdx.x];
-    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, threadIdx.x);
-    if (ci >= 0) rhs[ci] = v;
+    for (int w = 0; w < kRhsThreads / 32; ++w) {
+      v += part[0][w][i];
+      cn += (double)part[1][w][i];
+      g += (double)part[2][w][i];
+    }
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, i);
+    if (ci >= 0) {
+      rhs[ci] = v;
+      const double d = fmin(fmax(cn, dmin), dmax);
+      diag_c[ci] = d;
+      if (S) S[(int64_t)ci * ld + ci] += (T)(d / *radius);
+      if (gmax_shards)
+        atomicMax(gmax_shards + (c & (kGmaxShards - 1)),
+                  (unsigned long long)__double_as_longlong(fabs(g / scale_c[ci])));
+    }
   }
 }
 
@@ -1685,6 +1760,7 @@ struct Solve {
   double *cn_c, *cn_p, *g_c, *g_p, *scale_c, *scale_p, *diag_c, *diag_p;
   double* radius;
   unsigned long long* gmax_bits;
+  unsigned long long* gmax_shards;  // gradient max norm of the fused linearisation (kGmaxShards slots)
   int *flag, *nonfinite;
   void *S, *rhs, *zsol, *Linv, *Vinv, *gpv, *Wbuf, *What;
   double *part_mcc, *part_step_p, *part_step_c, *part_cost, *part_x, *scalars;
@@ -1768,6 +1844,7 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.diag_p = a.template take<double>(3 * s.np);
   s.radius = a.template take<double>(1);
   s.gmax_bits = a.template take<unsigned long long>(1);
+  s.gmax_shards = a.template take<unsigned long long>(kGmaxShards);
   s.flag = a.template take<int>(1);
   s.nonfinite = a.template take<int>(1);
   const int64_t n_s = s.dense ? s.n_pad : 0;
@@ -2341,6 +2418,36 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     *gmax = __builtin_bit_cast(double, (long long)bits);
     *xnorm = std::sqrt(pin[1]);
   };
+  // Fused linearisation (pair path): after an accepted step only the poses,
+  // the FP32 copies and the x norm are refreshed here; the LM diagonal and
+  // the gradient at the new point come out of the next Schur phase
+  // (k_schur_point_rec, k_rhs_camera), so no separate Jacobian pass runs.
+  const bool fused = s.pair_path;
+  auto refresh = [&]() {
+    if (kPose && s.nc > 0) {
+      k_cam_pose<<<nb_cam_pose, 128, 0, st>>>(s.ext, s.nc, s.pose);
+      check_launch(h);
+    }
+    if (kPose) {
+      to_float(s.ext, s.ext_f, 6 * s.nc);
+      to_float(s.intr, s.intr_f, (int64_t)s.k * s.ni);
+      to_float(s.pts, s.pts_f, 3 * s.np);
+    }
+    k_xnorm<<<gx, 256, 0, st>>>(s.ext, s.ext_col, n_e, s.intr, s.intr_var, s.k, n_i, s.pts, 3 * s.np, s.part_x);
+    check_launch(h);
+    k_reduce3<<<1, 256, 0, st>>>(s.part_x, gx, s.part_x, 0, s.part_x, 0, s.part_x, 0, s.scalars + 4);
+    check_launch(h);
+  };
+  // gradient max norm of the last Schur phase (reads its shards; synchronises)
+  auto read_gmax = [&]() -> double {
+    unsigned long long* hb = reinterpret_cast<unsigned long long*>(pin + 64);
+    GBBA_CUDA(cudaMemcpyAsync(hb, s.gmax_shards, sizeof(unsigned long long) * kGmaxShards, cudaMemcpyDeviceToHost,
+                              st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    double m = 0.0;
+    for (int i = 0; i < kGmaxShards; ++i) m = std::max(m, __builtin_bit_cast(double, (long long)hb[i]));
+    return m;
+  };
 
   // initial cost
   GBBA_CUDA(cudaMemsetAsync(s.nonfinite, 0, sizeof(int), st));
@@ -2378,6 +2485,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   // graphs that every iteration replays.
   Prob P = make_prob(s, s.ext, s.intr, s.pts, o);
   if (kPose && s.nc > 0) P.pose = s.pose;  // refreshed by linearize() after every accepted step
+  // gradient norm of the fused linearisation: only with a gradient tolerance
+  unsigned long long* const gshards = o->gradient_tolerance > 0.0 ? s.gmax_shards : nullptr;
   if (kPose) {
     P.ext_f = s.ext_f;
     P.intr_f = s.intr_f;
@@ -2389,10 +2498,11 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   auto record_phase = [&](int ph) {
     switch (ph) {
       case 0:
+        if (s.pair_path) GBBA_CUDA(cudaMemsetAsync(s.gmax_shards, 0, sizeof(unsigned long long) * kGmaxShards, st));
         if (s.dense) {
           GBBA_CUDA(cudaMemsetAsync(S, 0, sizeof(T) * s.n_pad * s.n_pad, st));
           k_schur_init<T><<<(unsigned)std::min<int64_t>(ceil_div(s.n_pad, 256), 1024), 256, 0, st>>>(
-              S, rhs, s.n_red, s.n_pad, s.diag_c, s.radius);
+              S, rhs, s.n_red, s.n_pad, s.diag_c, s.radius, s.pair_path ? 1 : 0);
           check_launch(h);
         } else {
           GBBA_CUDA(cudaMemsetAsync(rhs, 0, sizeof(T) * s.n_pad, st));
@@ -2402,8 +2512,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
           k_schur_point_rec<M, T><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
-              P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, s.radius, (T*)s.Vinv,
-                                                            (T*)s.gpv, (T*)s.rec, s.flag);
+              P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
+              gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
           check_launch(h);
           if (s.dense && s.n_blocks > 0) {
             k_schur_pairs<B, T><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
@@ -2419,7 +2529,9 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
           }
           if (s.nc > 0) {
             k_rhs_camera<B, T><<<(unsigned)s.nc, kRhsThreads, 0, st>>>(
-                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs);
+                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs,
+                s.scale_c, s.diag_c, o->min_lm_diagonal, o->max_lm_diagonal, s.radius, s.dense ? S : nullptr,
+                s.n_pad, gshards);
             check_launch(h);
           }
           if (!s.dense) {
@@ -2498,9 +2610,23 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       phase_launches[ph] = h->launches - l0;
     }
   };
+  // On the fused path the gradient at an accepted point is checked after the
+  // next Schur phase (before that phase's step is used), and, when the
+  // iteration limit ends the solve right after an accepted step, by one
+  // more Schur phase: the same terminations as ceres's check right after
+  // the step is accepted.
+  bool need_grad = false;
+  const bool check_grad = o->gradient_tolerance > 0.0;
   while (term < 0) {
     if (iteration >= o->max_num_iterations) {
       term = GBBA_NO_CONVERGENCE;
+      if (fused && need_grad && check_grad) {
+        pin[2] = radius;
+        GBBA_CUDA(cudaMemcpyAsync(s.radius, pin + 2, sizeof(double), cudaMemcpyHostToDevice, st));
+        run_phase(0);
+        run_phase(1);
+        if (read_gmax() <= o->gradient_tolerance) term = GBBA_CONVERGENCE;
+      }
       break;
     }
     pin[2] = radius;
@@ -2512,6 +2638,14 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     GBBA_CUDA(cudaEventRecord(ev[4], st));
     run_phase(1);
     GBBA_CUDA(cudaEventRecord(ev[1], st));
+    if (fused && need_grad && check_grad) {
+      need_grad = false;
+      if (read_gmax() <= o->gradient_tolerance) {
+        term = GBBA_CONVERGENCE;
+        break;
+      }
+    }
+    need_grad = false;
     run_phase(2);
     GBBA_CUDA(cudaEventRecord(ev[5], st));
     run_phase(3);
@@ -2524,7 +2658,9 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     GBBA_CUDA(cudaMemcpyAsync(hs, s.scalars, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaMemcpyAsync(&hs->flag, s.flag, sizeof(int), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaMemcpyAsync(&hs->nonfinite, s.nonfinite, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (fused) GBBA_CUDA(cudaMemcpyAsync(pin + 20, s.scalars + 4, sizeof(double), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaStreamSynchronize(st));
+    if (fused) x_norm = std::sqrt(pin[20]);
     float ms_a = 0, ms_b = 0, ms_c = 0, ms_k = 0, ms_f = 0;
     cudaEventElapsedTime(&ms_a, ev[0], ev[1]);
     cudaEventElapsedTime(&ms_b, ev[1], ev[2]);
@@ -2574,10 +2710,15 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       GBBA_CUDA(cudaMemcpyAsync(s.ext, s.ext2, sizeof(double) * n_e, cudaMemcpyDeviceToDevice, st));
       GBBA_CUDA(cudaMemcpyAsync(s.intr, s.intr2, sizeof(double) * n_i, cudaMemcpyDeviceToDevice, st));
       GBBA_CUDA(cudaMemcpyAsync(s.pts, s.pts2, sizeof(double) * 3 * s.np, cudaMemcpyDeviceToDevice, st));
-      const double tj = now_s();
-      linearize(false, &gmax, &x_norm);
-      sum->jacobian_time_s += now_s() - tj;
-      if (gmax <= o->gradient_tolerance) term = GBBA_CONVERGENCE;
+      if (fused) {
+        refresh();
+        need_grad = true;
+      } else {
+        const double tj = now_s();
+        linearize(false, &gmax, &x_norm);
+        sum->jacobian_time_s += now_s() - tj;
+        if (gmax <= o->gradient_tolerance) term = GBBA_CONVERGENCE;
+      }
     } else {
       ++sum->num_unsuccessful_steps;
       radius = radius / decrease_factor;  // StepRejected and StepIsInvalid
