@@ -263,6 +263,21 @@ def test_batched_fp64_matches_individual_solves(handle, abi, scenes):
         np.testing.assert_allclose(prm["points"], pi["points"], atol=1e-4)
 
 
+def test_batched_fp64_large_windows_match_individual_solves(handle, abi, scenes):
+    """FP64 windows of 31-40 cameras (reduced systems of 182-236 unknowns,
+    above what an FP64 S in shared memory could hold) keep S in global memory
+    and reach the same final cost as gbba_solve."""
+    probs = local_problems(scenes, 6, seed=114, cams=(31, 40), points=(400, 900))
+    opts = abi.default_options(max_num_iterations=50)
+    st, bs, _ = batched_solve(handle, abi, probs, opts)
+    assert st == abi.SUCCESS
+    for p, s in zip(probs, bs):
+        assert s.reduced_system_size > 176
+        si, _ = solve(handle, abi, p, opts)
+        assert s.usable and si.usable
+        assert abs(s.final_cost - si.final_cost) <= 1e-6 * si.final_cost, (s.final_cost, si.final_cost)
+
+
 def test_batched_mixed_reaches_fp64_cost(handle, abi, scenes):
     """Mixed-precision windows reach the FP64 minimum within 1e-6.  Some local
     windows have flat valleys in which ceres's default stopping rule
