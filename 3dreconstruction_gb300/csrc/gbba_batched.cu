@@ -69,7 +69,7 @@ struct BArgs {
   const uint32_t *cam, *icam, *pt_off;
   const int32_t *ext_col, *intr_col;  // problem-local reduced columns (-1 = held)
   const uint8_t* intr_var;
-  double *scale_p, *diag_p;
+  double* scale_p;
   void *Vinv, *gp, *wscratch;  // compute type
   double* gscr;                // kGlobalSlice doubles per CTA
   // FP32 path: per observation, the corrected FP64 residual and sqrt(rho')
@@ -83,11 +83,36 @@ struct BArgs {
   double loss_a, ftol, gtol, ptol, r0, rmax, rmin, min_rel, dmin, dmax;
 };
 
+// One observation's scratch slot (compute type values): W = Jc^T Jp and
+// W V^-1 (B x 3 each, row i = camera parameter i), the scaled camera Jacobian
+// Jc (2 x B) and, in a window with one intrinsic group, the observation's
+// U_kk lower triangle and intrinsic rhs correction.  Parts start on 4-value
+// (16-byte) boundaries.  The back substitution reuses the slot for Jc z and
+// the residual (4 doubles) and Jp (6 values).
+__host__ __device__ constexpr int rnd4(int v) { return (v + 3) & ~3; }
+template <int K>
+struct Slot {
+  static constexpr int B = 6 + K, KK = K * (K + 1) / 2;
+  static constexpr int kW = 0, kWh = rnd4(3 * B), kJ = kWh + rnd4(3 * B), kU = kJ + rnd4(2 * B), kQ = kU + KK;
+  static constexpr int kSize = rnd4(kQ + K);
+  static_assert(kSize >= 8 + 6, "back substitution entries fit the slot");
+};
+
+template <typename T>
+__device__ __forceinline__ void ld18(const T* p, T v[18]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) ld4<T>(p + 4 * q, v + 4 * q);
+  v[16] = p[16];
+  v[17] = p[17];
+}
+
 // NS: values of S held in shared memory (1 when S lives in global memory).
-constexpr int kPoseCams = 64;  // windows with more cameras evaluate residuals by Rodrigues
+constexpr int kPoseCams = 64;  // larger windows evaluate residuals by Rodrigues and read columns from global memory
 template <typename T, int NS, int N>
 struct Shared {
   double pose[2][kPoseCams * 12];  // FP64 poses of ext (0) and of the candidate ext2 (1)
+  int32_t ecol[kPoseCams * 6];     // the window's extrinsic columns (-1 = held)
+  int32_t kcol[8];                 // one intrinsic group: its columns
   T S[NS];
   T rhs[N];
   T z[N];
@@ -239,13 +264,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   const int n = (int)P.n;
   T* Vinv = (T*)a.Vinv;
   T* gpv = (T*)a.gp;
-  // per-warp scratch, one slot per observation of the warp's current point:
-  // W and W V^-1 (6B values), then (one intrinsic group) the observation's
-  // U_kk lower triangle and intrinsic rhs (KK + K values); one more slot
-  // holds per-point sums
-  constexpr int KK = K * (K + 1) / 2;
-  constexpr int SLOT = 6 * B + KK + K;
-  T* wsc = (T*)a.wscratch + ((int64_t)blockIdx.x * kWarps + warp) * (int64_t)(a.max_views + 1) * SLOT;
+  // per-warp scratch, one slot per observation of the warp's current point;
+  // one more slot holds per-point sums
+  using SL = Slot<K>;
+  constexpr int KK = SL::KK;
+  T* wsc = (T*)a.wscratch + ((int64_t)blockIdx.x * kWarps + warp) * (int64_t)(a.max_views + 1) * SL::kSize;
   // global slice: column norms [kNMax], gradient [kNMax], rhs [kNMax], S (FP64)
   double* gsl = a.gscr + (int64_t)blockIdx.x * kGlobalSlice;
   double* g_acc = gsl;
@@ -272,6 +295,49 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   };
 
   const bool use_pose = P.nc <= (uint32_t)kPoseCams;
+  // reduced column of camera c's extrinsic parameter j (-1 = held)
+  auto ecol = [&](uint32_t c, int j) -> int {
+    return use_pose ? sh.ecol[6 * (c - P.c0) + j] : a.ext_col[6 * (int64_t)c + j];
+  };
+  // The 6x6 extrinsic block of S for observations u (camera cu) and w (camera
+  // cw <= cu) of one point: -(W V^-1)_u W_w^T, plus U_ee = Jc_e^T Jc_e when u
+  // is the observation's own pair; a diagonal block keeps its lower triangle.
+  auto ext_block = [&](const T* base, uint32_t u, uint32_t w, uint32_t cu, uint32_t cw, bool own) {
+    const T* Su = base + (int64_t)u * SL::kSize;
+    const T* Sw = base + (int64_t)w * SL::kSize;
+    int ci[6], cj[6];
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      ci[j] = ecol(cu, j);
+      cj[j] = ecol(cw, j);
+    }
+    // W_w (and for an observation's own pair its Jc_e) in registers; the
+    // rows of (W V^-1)_u are read as they are used (FP64: register budget)
+    T ww[18], j0[6], j1[6];
+    ld18<T>(Sw + SL::kW, ww);
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      j0[j] = own ? Sw[SL::kJ + j] : T(0);
+      j1[j] = own ? Sw[SL::kJ + B + j] : T(0);
+    }
+    T hu[18];
+    if constexpr (sizeof(T) == 4) ld18<T>(Su + SL::kWh, hu);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      if (ci[i] < 0) continue;
+      if constexpr (sizeof(T) != 4) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) hu[3 * i + k] = Su[SL::kWh + 3 * i + k];
+      }
+#pragma unroll
+      for (int j = 0; j < 6; ++j) {
+        if (cj[j] < 0 || cj[j] > ci[i]) continue;
+        const T s = j0[i] * j0[j] + j1[i] * j1[j] -
+                    (hu[3 * i] * ww[3 * j] + hu[3 * i + 1] * ww[3 * j + 1] + hu[3 * i + 2] * ww[3 * j + 2]);
+        Sadd(tri(ci[i], cj[j]), (SS)s);
+      }
+    }
+  };
   // residual cache (FP32 path): slot `cur` holds the current parameters'
   constexpr bool kCache = sizeof(T) == 4;
   int cur = 0;
@@ -320,8 +386,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     return c;
   };
 
-  // gradient max norm, x norm; scale (first) and LM diagonal
-  auto linearize = [&](bool first, double* gmax, double* xnorm) {
+  // norm of the variable parameters (parameter tolerance)
+  auto param_norm = [&]() -> double {
+    double xs = 0.0;
+    for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) {
+      const int64_t j = 6 * (int64_t)P.c0 + i;
+      if (a.ext_col[j] >= 0) xs += a.ext[j] * a.ext[j];
+    }
+    for (uint32_t i = tid; i < K * P.ni; i += kThreads) {
+      const int64_t j = K * (int64_t)P.g0 + i;
+      if (a.intr_var[j / K]) xs += a.intr[j] * a.intr[j];
+    }
+    for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads) {
+      const double v = a.pts[3 * (int64_t)P.x0 + i];
+      xs += v * v;
+    }
+    return sqrt(block_sum(xs, sh.red, &sh.bcast[2]));
+  };
+  // Jacobi scale (first) and gradient max norm at the current parameters.
+  // After the first linearisation the Schur build forms the LM diagonal and
+  // the gradient from its own Jacobian; this pass only runs again to check
+  // the gradient of an accepted last step at the iteration limit.
+  auto linearize = [&](bool first) -> double {
     for (int i = tid; i < n; i += kThreads) {
       __stcg(g_acc + i, 0.0);
       __stcg(g_grad + i, 0.0);
@@ -355,38 +441,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         gp3[j] = warp_sum(gp3[j]);
       }
       if (lane < 3) {
-        const double c = cp[lane];
+        const double c = lane == 0 ? cp[0] : lane == 1 ? cp[1] : cp[2];
         if (first) a.scale_p[3 * (int64_t)p + lane] = a.jacobi ? 1.0 / (1.0 + sqrt(c)) : 1.0;
-        const double sc = a.scale_p[3 * (int64_t)p + lane];
-        a.diag_p[3 * (int64_t)p + lane] = fmin(fmax(c * sc * sc, a.dmin), a.dmax);
-        gm = fmax(gm, fabs(gp3[lane]));
+        gm = fmax(gm, fabs(lane == 0 ? gp3[0] : lane == 1 ? gp3[1] : gp3[2]));
       }
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
-      const double acc = __ldcg(g_acc + i);
-      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(acc)) : 1.0;
-      const double sc = sh.scale_c[i];
-      sh.diag_c[i] = fmin(fmax(acc * sc * sc, a.dmin), a.dmax);
+      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(__ldcg(g_acc + i))) : 1.0;
       gm = fmax(gm, fabs(__ldcg(g_grad + i)));
     }
-    *gmax = block_max(gm, sh.red, &sh.bcast[1]);
-    double xs = 0.0;
-    for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) {
-      const int64_t j = 6 * (int64_t)P.c0 + i;
-      if (a.ext_col[j] >= 0) xs += a.ext[j] * a.ext[j];
-    }
-    for (uint32_t i = tid; i < K * P.ni; i += kThreads) {
-      const int64_t j = K * (int64_t)P.g0 + i;
-      if (a.intr_var[j / K]) xs += a.intr[j] * a.intr[j];
-    }
-    for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads) {
-      const double v = a.pts[3 * (int64_t)P.x0 + i];
-      xs += v * v;
-    }
-    *xnorm = sqrt(block_sum(xs, sh.red, &sh.bcast[2]));
+    return block_max(gm, sh.red, &sh.bcast[1]);
   };
 
+  // the window's column maps, fixed for the whole solve (made visible by make_poses' barrier)
+  if (use_pose)
+    for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) sh.ecol[i] = a.ext_col[6 * (int64_t)P.c0 + i];
+  if (tid < 8) sh.kcol[tid] = P.ni == 1 && tid < K ? a.intr_col[K * (int64_t)P.g0 + tid] : -1;
   bool finite = true;
   make_poses(a.ext, 0);
   double cost = cost_at(a.ext, a.intr, a.pts, &finite);
@@ -404,37 +475,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     return;
   }
-  double gmax, xnorm;
-  linearize(true, &gmax, &xnorm);
+  double gmax = linearize(true), xnorm = param_norm();
+  bool check_grad = false;  // an accepted step's gradient is checked by the next Schur build
   int term = gmax <= a.gtol ? GBBA_CONVERGENCE : -1;
   double radius = a.r0, decrease = 2.0;
   int invalid = 0, iter = 0;
   while (term < 0) {
     if (iter >= a.max_iterations) {
       term = GBBA_NO_CONVERGENCE;
+      if (check_grad && linearize(false) <= a.gtol) term = GBBA_CONVERGENCE;
       break;
     }
-    // ---- S = diag(D_c^2) + sum F'F - sum (F'E) V^-1 (E'F), rhs
+    // ---- S = sum F'F - sum (F'E) V^-1 (E'F) + diag(D_c^2), rhs, and from
+    // the same Jacobian the column norms (LM diagonal) and the gradient
     for (int i = tid; i < n * (n + 1) / 2; i += kThreads) Sst(i, SS(0));
     for (int i = tid; i < n; i += kThreads) {
       if constexpr (kGS) __stcg(g_rhs + i, 0.0);
       else sh.rhs[i] = SS(0);
+      __stcg(g_acc + i, 0.0);
+      __stcg(g_grad + i, 0.0);
     }
     if (tid == 0) sh.flag = 0;
     __syncthreads();
-    for (int i = tid; i < n; i += kThreads) Sst(tri(i, i), (SS)(sh.diag_c[i] / radius));
-    __syncthreads();
     // One intrinsic group per window (the local-BA case): the intrinsic
     // columns are common to every observation, so their terms factor through
-    // per-point sums (no observation pairs) and per-lane accumulators:
-    //   S_kk -= (sum_x W_kx V^-1)(sum_y W_ky)^T,  S_k,c(y) -= (sum_x W_kx V^-1) W_ey^T,
-    //   U_kk += sum_o J_ko^T J_ko (per lane, flushed once), rhs_k likewise;
-    // only the 6x6 extrinsic blocks need the observation pairs (camera a > b,
-    // or the diagonal block of a single observation).
+    // per-point sums (no observation pairs):
+    //   S_kk += sum_o U_kk - (sum_x W_kx V^-1)(sum_y W_ky)^T,
+    //   S_k,c(y) += U_ke(y) - (sum_x W_kx V^-1) W_ey^T  (one lane per observation y),
+    // and only the 6x6 extrinsic blocks need the observation pairs (one lane
+    // per pair; an observation's own pair carries its U_ee).
     const bool one_group = P.ni == 1;
-    const int32_t* kcol = a.intr_col + K * (int64_t)P.g0;  // the group's columns (-1 = held)
+    double gm = 0.0;  // gradient max norm (unscaled) over this thread's points and columns
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1], m = oe - ob;
+      const double* spp = a.scale_p + 3 * (int64_t)p;
       T v[6] = {}, g[3] = {};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
         double r[2];
@@ -449,7 +523,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const T s = (T)a.scale_p[3 * (int64_t)p + j];
+          const T s = (T)spp[j];
           Jp[0][j] *= s;
           Jp[1][j] *= s;
         }
@@ -462,36 +536,42 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         v[5] += Jp[0][2] * Jp[0][2] + Jp[1][2] * Jp[1][2];
 #pragma unroll
         for (int j = 0; j < 3; ++j) g[j] += Jp[0][j] * r0 + Jp[1][j] * r1;
-        T* W = wsc + (int64_t)(o - ob) * SLOT;
+        T* W = wsc + (int64_t)(o - ob) * SL::kSize;
 #pragma unroll
         for (int i = 0; i < B; ++i)
 #pragma unroll
-          for (int j = 0; j < 3; ++j) W[i * 3 + j] = Jc[0][i] * Jp[0][j] + Jc[1][i] * Jp[1][j];
-        // U = Jc^T Jc and Jc^T r
-        if (one_group) {
-#pragma unroll
-          for (int e = 0; e < KK + K; ++e) W[6 * B + e] = T(0);
-        }
+          for (int j = 0; j < 3; ++j) W[SL::kW + i * 3 + j] = Jc[0][i] * Jp[0][j] + Jc[1][i] * Jp[1][j];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
-          const int ci = col[i];
-          if (ci < 0) continue;
-          const T ri = Jc[0][i] * r0 + Jc[1][i] * r1;
-          if (one_group && i >= 6) W[6 * B + KK + (i - 6)] = ri;
-          else Radd(ci, (SS)ri);
+          W[SL::kJ + i] = Jc[0][i];
+          W[SL::kJ + B + i] = Jc[1][i];
+        }
+        // column norms and gradient of the scaled Jacobian, FP64 sums
 #pragma unroll
-          for (int j = 0; j <= i; ++j) {
-            const int cj = col[j];
-            const T u = Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j];
-            if (one_group && j >= 6) {
-              W[6 * B + (i - 6) * (i - 5) / 2 + (j - 6)] = u;  // held columns are skipped at the reduction
-              continue;
-            }
-            if (cj < 0) continue;
-            if (one_group || cj <= ci) {
-              Sadd(tri(ci, cj), (SS)u);
-            } else {
-              Sadd(tri(cj, ci), (SS)u);
+        for (int j = 0; j < B; ++j) {
+          if (col[j] < 0) continue;
+          const double x0 = Jc[0][j], x1 = Jc[1][j];
+          atomicAdd(g_acc + col[j], x0 * x0 + x1 * x1);
+          atomicAdd(g_grad + col[j], x0 * r[0] + x1 * r[1]);
+        }
+        if (one_group) {
+          // the observation's U_kk lower triangle (held columns are skipped at the reduction)
+#pragma unroll
+          for (int i = 0; i < K; ++i)
+#pragma unroll
+            for (int j = 0; j <= i; ++j)
+              W[SL::kU + i * (i + 1) / 2 + j] = Jc[0][6 + i] * Jc[0][6 + j] + Jc[1][6 + i] * Jc[1][6 + j];
+        } else {
+#pragma unroll
+          for (int i = 0; i < B; ++i) {
+            const int ci = col[i];
+            if (ci < 0) continue;
+#pragma unroll
+            for (int j = 0; j <= i; ++j) {
+              const int cj = col[j];
+              if (cj < 0) continue;
+              const T u = Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j];
+              Sadd(cj <= ci ? tri(ci, cj) : tri(cj, ci), (SS)u);
             }
           }
         }
@@ -500,8 +580,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       for (int i = 0; i < 6; ++i) v[i] = warp_sum(v[i]);
 #pragma unroll
       for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
-      const T a00 = v[0] + (T)(a.diag_p[3 * (int64_t)p] / radius), a11 = v[3] + (T)(a.diag_p[3 * (int64_t)p + 1] / radius),
-              a22 = v[5] + (T)(a.diag_p[3 * (int64_t)p + 2] / radius);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) gm = fmax(gm, fabs((double)g[j] / spp[j]));
+      // point block damped by its own LM diagonal clamp(diag V) / radius
+      const T a00 = v[0] + (T)(fmin(fmax((double)v[0], a.dmin), a.dmax) / radius),
+              a11 = v[3] + (T)(fmin(fmax((double)v[3], a.dmin), a.dmax) / radius),
+              a22 = v[5] + (T)(fmin(fmax((double)v[5], a.dmin), a.dmax) / radius);
       const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
       const T d1 = a11 - l10 * l10;
       const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
@@ -520,48 +604,51 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       }
       const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
-        T* W = wsc + (int64_t)(o - ob) * SLOT;
+        T* W = wsc + (int64_t)(o - ob) * SL::kSize;
         const uint32_t c = a.cam[o], gi = a.icam[o];
 #pragma unroll
         for (int i = 0; i < B; ++i) {
           T y[3];
 #pragma unroll
-          for (int j = 0; j < 3; ++j) y[j] = W[i * 3] * Vf[0][j] + W[i * 3 + 1] * Vf[1][j] + W[i * 3 + 2] * Vf[2][j];
+          for (int j = 0; j < 3; ++j)
+            y[j] = W[SL::kW + i * 3] * Vf[0][j] + W[SL::kW + i * 3 + 1] * Vf[1][j] + W[SL::kW + i * 3 + 2] * Vf[2][j];
 #pragma unroll
-          for (int j = 0; j < 3; ++j) W[3 * B + i * 3 + j] = y[j];
-          const int ci = i < 6 ? a.ext_col[6 * (int64_t)c + i] : a.intr_col[K * (int64_t)gi + (i - 6)];
+          for (int j = 0; j < 3; ++j) W[SL::kWh + i * 3 + j] = y[j];
           const T q = -(y[0] * g[0] + y[1] * g[1] + y[2] * g[2]);
-          if (ci < 0) continue;
-          if (one_group && i >= 6) W[6 * B + KK + (i - 6)] += q;
-          else Radd(ci, (SS)q);
+          if (one_group && i >= 6) {
+            W[SL::kQ + (i - 6)] = q;
+            continue;
+          }
+          const int ci = i < 6 ? ecol(c, i) : a.intr_col[K * (int64_t)gi + (i - 6)];
+          if (ci >= 0) Radd(ci, (SS)q);
         }
       }
       __syncwarp();
       if (one_group) {
         // per-point sums over the observations, Wh_K = sum W_k V^-1 and
         // W_K = sum W_k (K x 3 each), kept in the warp's extra scratch slot
-        T* sums = wsc + (int64_t)a.max_views * SLOT;
+        T* sums = wsc + (int64_t)a.max_views * SL::kSize;
         for (int e = lane; e < 3 * K; e += 32) {
           T hs = T(0), ws = T(0);
           for (uint32_t x = 0; x < m; ++x) {
-            const T* Wx = wsc + (int64_t)x * SLOT;
-            hs += Wx[3 * B + 18 + e];
-            ws += Wx[18 + e];
+            const T* Wx = wsc + (int64_t)x * SL::kSize;
+            hs += Wx[SL::kWh + 18 + e];
+            ws += Wx[SL::kW + 18 + e];
           }
           sums[e] = hs;
           sums[3 * K + e] = ws;
         }
-        // the point's U_kk and intrinsic rhs: sums over its observations' slots
+        // the point's U_kk and intrinsic rhs correction: sums over its observations' slots
         for (int e = lane; e < KK + K; e += 32) {
           T acc = T(0);
-          for (uint32_t x = 0; x < m; ++x) acc += wsc[(int64_t)x * SLOT + 6 * B + e];
+          for (uint32_t x = 0; x < m; ++x) acc += wsc[(int64_t)x * SL::kSize + SL::kU + e];
           if (e < KK) {
             int i = 0;
             while ((i + 1) * (i + 2) / 2 <= e) ++i;
             const int j = e - i * (i + 1) / 2;
-            if (kcol[i] >= 0 && kcol[j] >= 0) Sadd(tri(kcol[i], kcol[j]), (SS)acc);
-          } else if (kcol[e - KK] >= 0) {
-            Radd(kcol[e - KK], (SS)acc);
+            if (sh.kcol[i] >= 0 && sh.kcol[j] >= 0) Sadd(tri(sh.kcol[i], sh.kcol[j]), (SS)acc);
+          } else if (sh.kcol[e - KK] >= 0) {
+            Radd(sh.kcol[e - KK], (SS)acc);
           }
         }
         __syncwarp();
@@ -570,70 +657,67 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
           int i = 0;
           while ((i + 1) * (i + 2) / 2 <= e) ++i;
           const int j = e - i * (i + 1) / 2;
-          const int ci = kcol[i], cj = kcol[j];
+          const int ci = sh.kcol[i], cj = sh.kcol[j];
           if (ci < 0 || cj < 0) continue;
           const T sacc = sums[3 * i] * sums[3 * K + 3 * j] + sums[3 * i + 1] * sums[3 * K + 3 * j + 1] +
                          sums[3 * i + 2] * sums[3 * K + 3 * j + 2];
           Sadd(tri(ci, cj), (SS)(-sacc));
         }
-        // S_k,c(y) -= Wh_K W_ey^T for every observation y: work items (y, i, j)
-        for (uint32_t t = lane; t < m * 6 * K; t += 32) {
-          const uint32_t y = t / (6 * K), e = t % (6 * K);
-          const int i = e / 6, j = e % 6;
-          const uint32_t cb = a.cam[ob + y];
-          const int ci = kcol[i], cj = a.ext_col[6 * (int64_t)cb + j];
-          if (ci < 0 || cj < 0) continue;
-          const T* Wy = wsc + (int64_t)y * SLOT;
-          const T sacc = sums[3 * i] * Wy[3 * j] + sums[3 * i + 1] * Wy[3 * j + 1] + sums[3 * i + 2] * Wy[3 * j + 2];
-          Sadd(tri(ci, cj), (SS)(-sacc));
+        // S_k,c(y) += U_ke(y) - Wh_K W_ey^T: one lane per observation y
+        // (intrinsic columns follow every extrinsic column: lower triangle)
+        for (uint32_t y = lane; y < m; y += 32) {
+          const T* Wy = wsc + (int64_t)y * SL::kSize;
+          const uint32_t cy = a.cam[ob + y];
+          int cj[6];
+#pragma unroll
+          for (int j = 0; j < 6; ++j) cj[j] = ecol(cy, j);
+          if (cj[0] < 0 && cj[1] < 0 && cj[2] < 0 && cj[3] < 0 && cj[4] < 0 && cj[5] < 0) continue;
+          T wy[18], j0[6], j1[6];
+          ld18<T>(Wy + SL::kW, wy);
+#pragma unroll
+          for (int j = 0; j < 6; ++j) {
+            j0[j] = Wy[SL::kJ + j];
+            j1[j] = Wy[SL::kJ + B + j];
+          }
+#pragma unroll
+          for (int i = 0; i < K; ++i) {
+            const int ci = sh.kcol[i];
+            if (ci < 0) continue;
+            const T s0 = sums[3 * i], s1 = sums[3 * i + 1], s2 = sums[3 * i + 2];
+            const T k0 = Wy[SL::kJ + 6 + i], k1 = Wy[SL::kJ + B + 6 + i];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) {
+              if (cj[j] < 0) continue;
+              const T val = k0 * j0[j] + k1 * j1[j] - (s0 * wy[3 * j] + s1 * wy[3 * j + 1] + s2 * wy[3 * j + 2]);
+              Sadd(tri(ci, cj[j]), (SS)val);
+            }
+          }
         }
-        // extrinsic blocks: work items (unordered observation pair x >= y, i, j).
-        // The pair's block is taken with the higher camera's observation first
-        // (its entries are all in the lower triangle); an observation's own
-        // block and a camera that sees the point twice keep the lower part of
-        // both orders.
+        // extrinsic blocks: one lane per unordered observation pair x >= y
         const uint32_t nq = m * (m + 1) / 2;
-        for (uint32_t t = lane; t < nq * 36; t += 32) {
-          const uint32_t q = t / 36, e = t % 36;
+        for (uint32_t q = lane; q < nq; q += 32) {
           uint32_t x = (uint32_t)((sqrtf(8.0f * (float)q + 1.0f) - 1.0f) * 0.5f);
           while ((x + 1) * (x + 2) / 2 <= q) ++x;
           while (x * (x + 1) / 2 > q) --x;
           const uint32_t y = q - x * (x + 1) / 2;
           const uint32_t cx = a.cam[ob + x], cy = a.cam[ob + y];
-          const int i = e / 6, j = e % 6;
-          for (int side = 0; side < 2; ++side) {
-            uint32_t u = x, w = y;
-            if (side == 0) {
-              if (cx < cy) {
-                u = y;
-                w = x;
-              }
-            } else {
-              if (!(cx == cy && x != y)) break;
-              u = y;
-              w = x;
-            }
-            const uint32_t cu = side == 0 && cx < cy ? cy : cx, cw = side == 0 && cx < cy ? cx : cy;
-            const int ci = a.ext_col[6 * (int64_t)cu + i], cj = a.ext_col[6 * (int64_t)cw + j];
-            if (ci < 0 || cj < 0 || cj > ci) continue;
-            const T* Whu = wsc + (int64_t)u * SLOT + 3 * B;
-            const T* Ww = wsc + (int64_t)w * SLOT;
-            Sadd(tri(ci, cj), (SS)(-(Whu[3 * i] * Ww[3 * j] + Whu[3 * i + 1] * Ww[3 * j + 1] + Whu[3 * i + 2] * Ww[3 * j + 2])));
-          }
+          if (cx >= cy) ext_block(wsc, x, y, cx, cy, x == y);
+          else ext_block(wsc, y, x, cy, cx, false);
+          if (cx == cy && x != y) ext_block(wsc, y, x, cy, cx, false);  // a camera that sees the point twice
         }
       } else {
         for (uint32_t x = 0; x < m; ++x) {
           const uint32_t oa = ob + x;
           const uint32_t ca = a.cam[oa], ga = a.icam[oa];
-          const T* Wha = wsc + (int64_t)x * SLOT + 3 * B;
+          const T* Wha = wsc + (int64_t)x * SL::kSize + SL::kWh;
           for (uint32_t y = 0; y < m; ++y) {
             const uint32_t obb = ob + y;
             const uint32_t cb = a.cam[obb], gb = a.icam[obb];
-            const T* Wb = wsc + (int64_t)y * SLOT;
+            const T* Wb = wsc + (int64_t)y * SL::kSize + SL::kW;
             for (int e = lane; e < B * B; e += 32) {
               const int i = e / B, j = e % B;
-              const int ci = i < 6 ? a.ext_col[6 * (int64_t)ca + i] : a.intr_col[K * (int64_t)ga + (i - 6)];
-              const int cj = j < 6 ? a.ext_col[6 * (int64_t)cb + j] : a.intr_col[K * (int64_t)gb + (j - 6)];
+              const int ci = i < 6 ? ecol(ca, i) : a.intr_col[K * (int64_t)ga + (i - 6)];
+              const int cj = j < 6 ? ecol(cb, j) : a.intr_col[K * (int64_t)gb + (j - 6)];
               if (ci < 0 || cj < 0 || cj > ci) continue;
               Sadd(tri(ci, cj),
                    (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
@@ -644,9 +728,25 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       __syncwarp();
     }
     __syncthreads();
-    if constexpr (kGS) {
-      for (int i = tid; i < n; i += kThreads) sh.rhs[i] = (SS)__ldcg(g_rhs + i);
-      __syncthreads();
+    // LM diagonal D_c^2 = clamp(column norms), rhs = gradient + Schur
+    // correction, gradient max norm of this linearisation
+    for (int i = tid; i < n; i += kThreads) {
+      const double d = fmin(fmax(__ldcg(g_acc + i), a.dmin), a.dmax);
+      sh.diag_c[i] = d;
+      Sst(tri(i, i), Sld(tri(i, i)) + (SS)(d / radius));
+      const double gi = __ldcg(g_grad + i);
+      if constexpr (kGS) sh.rhs[i] = (SS)(gi + __ldcg(g_rhs + i));
+      else sh.rhs[i] = (SS)(gi + (double)sh.rhs[i]);
+      gm = fmax(gm, fabs(gi / sh.scale_c[i]));
+    }
+    gmax = block_max(gm, sh.red, &sh.bcast[1]);
+    // ceres checks the gradient right after an accepted step
+    if (check_grad) {
+      check_grad = false;
+      if (gmax <= a.gtol) {
+        term = GBBA_CONVERGENCE;
+        break;
+      }
     }
     // ---- Cholesky of S (outer-product elimination, one barrier per column)
     for (int j = 0; j < n; ++j) {
@@ -691,28 +791,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       if (tid == 0) sh.z[j] = xj;
       __syncthreads();
     }
-    // ---- back substitution, model cost change, candidate points
+    // ---- back substitution, model cost change, candidate points.  The
+    // first pass over a point's observations keeps each one's Jc z (FP64),
+    // residual and Jp in its scratch slot for the second pass.
     double mcc = 0.0, stp = 0.0;
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1];
+      const double* spp = a.scale_p + 3 * (int64_t)p;
       T t[3] = {};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
         double r[2];
         T Jc[2][B], Jp[2][3];
         int col[B];
         obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
-        T fz0 = T(0), fz1 = T(0);
+        double f0 = 0.0, f1 = 0.0;
 #pragma unroll
         for (int i = 0; i < B; ++i) {
           if (col[i] < 0) continue;
-          const T zi = (T)(sh.z[col[i]] * sh.scale_c[col[i]]);
-          fz0 += Jc[0][i] * zi;
-          fz1 += Jc[1][i] * zi;
+          const double zi = (double)sh.z[col[i]] * sh.scale_c[col[i]];
+          f0 += (double)Jc[0][i] * zi;
+          f1 += (double)Jc[1][i] * zi;
         }
+        const T fz0 = (T)f0, fz1 = (T)f1;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] += (Jp[0][j] * fz0 + Jp[1][j] * fz1) * (T)spp[j];
+        double* d = reinterpret_cast<double*>(wsc + (int64_t)(o - ob) * SL::kSize);
+        d[0] = f0;
+        d[1] = f1;
+        d[2] = r[0];
+        d[3] = r[1];
+        T* jp = reinterpret_cast<T*>(d + 4);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const T s = (T)a.scale_p[3 * (int64_t)p + j];
-          t[j] += (Jp[0][j] * fz0 + Jp[1][j] * fz1) * s;
+          jp[j] = Jp[0][j];
+          jp[3 + j] = Jp[1][j];
         }
       }
 #pragma unroll
@@ -722,34 +834,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       const T y[3] = {vi[0] * q0 + vi[1] * q1 + vi[2] * q2, vi[1] * q0 + vi[3] * q1 + vi[4] * q2,
                       vi[2] * q0 + vi[4] * q1 + vi[5] * q2};
       if (!isfinite((double)y[0]) || !isfinite((double)y[1]) || !isfinite((double)y[2])) sh.flag = 3;
-      for (uint32_t o = ob + lane; o < oe; o += 32) {
-        double r[2];
-        T Jc[2][B], Jp[2][3];
-        int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
-        double m0 = 0.0, m1 = 0.0;
+      double ys[3];
 #pragma unroll
-        for (int i = 0; i < B; ++i) {
-          if (col[i] < 0) continue;
-          const double zi = (double)sh.z[col[i]] * sh.scale_c[col[i]];
-          m0 += (double)Jc[0][i] * zi;
-          m1 += (double)Jc[1][i] * zi;
-        }
+      for (int j = 0; j < 3; ++j) ys[j] = (double)y[j] * spp[j];
+      for (uint32_t o = ob + lane; o < oe; o += 32) {
+        const double* d = reinterpret_cast<const double*>(wsc + (int64_t)(o - ob) * SL::kSize);
+        const T* jp = reinterpret_cast<const T*>(d + 4);
+        double m0 = d[0], m1 = d[1];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const double yj = (double)y[j] * a.scale_p[3 * (int64_t)p + j];
-          m0 += (double)Jp[0][j] * yj;
-          m1 += (double)Jp[1][j] * yj;
+          m0 += (double)jp[j] * ys[j];
+          m1 += (double)jp[3 + j] * ys[j];
         }
         m0 = -m0;
         m1 = -m1;
-        mcc += -(m0 * (r[0] + m0 / 2.0) + m1 * (r[1] + m1 / 2.0));
+        mcc += -(m0 * (d[2] + m0 / 2.0) + m1 * (d[3] + m1 / 2.0));
       }
       if (lane < 3) {
-        const double d = -(double)y[lane] * a.scale_p[3 * (int64_t)p + lane];
-        a.pts2[3 * (int64_t)p + lane] = a.pts[3 * (int64_t)p + lane] + d;
-        stp += d * d;
+        const double dx = -(lane == 0 ? ys[0] : lane == 1 ? ys[1] : ys[2]);
+        a.pts2[3 * (int64_t)p + lane] = a.pts[3 * (int64_t)p + lane] + dx;
+        stp += dx * dx;
       }
+      __syncwarp();
     }
     for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) {
       const int64_t j = 6 * (int64_t)P.c0 + i;
@@ -810,8 +916,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         for (uint32_t i = tid; i < 12 * P.nc; i += kThreads) sh.pose[0][i] = sh.pose[1][i];
       cur ^= 1;  // the candidate's residual cache becomes the current one
       __syncthreads();
-      linearize(false, &gmax, &xnorm);
-      if (gmax <= a.gtol) term = GBBA_CONVERGENCE;
+      xnorm = param_norm();
+      check_grad = true;
     } else {
       ++res.unsuccessful;
       radius /= decrease;
@@ -909,12 +1015,12 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   for (int i = 0; i < np_; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](uint32_t x, uint32_t y) { return (bp[x].o1 - bp[x].o0) > (bp[y].o1 - bp[y].o0); });
-  const int B = 6 + k;
+  const int slot_values = k == 1 ? Slot<1>::kSize : k == 6 ? Slot<6>::kSize : Slot<8>::kSize;
   const size_t tsize = 8;  // FP64-sized: the mixed path ends with an FP64 polish
   Planner pl;
   auto plan = [&](auto& A) {
     struct Ptrs {
-      double *ext, *intr, *pts, *ext2, *intr2, *pts2, *obs_in, *scale_p, *diag_p;
+      double *ext, *intr, *pts, *ext2, *intr2, *pts2, *obs_in, *scale_p;
       double2* obs;
       uint32_t *cam, *icam, *pt, *cam_s, *icam_s, *counts, *off, *fill, *chunks, *perm, *order;
       int32_t *ecol, *icol;
@@ -928,7 +1034,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     q.ext = A.template take<double>(6 * tc); q.intr = A.template take<double>(k * tg); q.pts = A.template take<double>(3 * tx);
     q.ext2 = A.template take<double>(6 * tc); q.intr2 = A.template take<double>(k * tg); q.pts2 = A.template take<double>(3 * tx);
     q.obs_in = A.template take<double>(2 * to); q.obs = A.template take<double2>(to);
-    q.scale_p = A.template take<double>(3 * tx); q.diag_p = A.template take<double>(3 * tx);
+    q.scale_p = A.template take<double>(3 * tx);
     q.cam = A.template take<uint32_t>(to); q.icam = A.template take<uint32_t>(to); q.pt = A.template take<uint32_t>(to);
     q.cam_s = A.template take<uint32_t>(to); q.icam_s = A.template take<uint32_t>(to);
     q.counts = A.template take<uint32_t>(tx + 1); q.off = A.template take<uint32_t>(tx + 1);
@@ -937,7 +1043,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     q.ecol = A.template take<int32_t>(6 * tc); q.icol = A.template take<int32_t>(k * tg); q.ivar = A.template take<uint8_t>(tg);
     q.probs = A.template take<BProb>(np_); q.out = A.template take<BOut>(2 * np_);
     q.Vinv = A.template take<char>(6 * tx * tsize); q.gp = A.template take<char>(3 * tx * tsize);
-    q.wsc = A.template take<char>((size_t)np_ * kWarps * (max_views + 1) * (6 * B + k * (k + 1) / 2 + k) * tsize);
+    q.wsc = A.template take<char>((size_t)np_ * kWarps * (max_views + 1) * slot_values * tsize);
     q.gscr = A.template take<double>((size_t)np_ * kGlobalSlice);
     q.rcache = A.template take<double>((size_t)6 * std::max<int64_t>(to, 1));
     return q;
@@ -1027,7 +1133,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   a.ext = q.ext; a.intr = q.intr; a.pts = q.pts; a.ext2 = q.ext2; a.intr2 = q.intr2; a.pts2 = q.pts2;
   a.obs = q.obs; a.cam = q.cam_s; a.icam = q.icam_s; a.pt_off = q.off;
   a.ext_col = q.ecol; a.intr_col = q.icol; a.intr_var = q.ivar;
-  a.scale_p = q.scale_p; a.diag_p = q.diag_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc; a.gscr = q.gscr;
+  a.scale_p = q.scale_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc; a.gscr = q.gscr;
   a.rcache = q.rcache; a.total_obs = to;
   a.max_views = max_views; a.out = q.out;
   a.max_iterations = o->max_num_iterations; a.max_invalid = o->max_num_consecutive_invalid_steps;
