@@ -66,15 +66,18 @@ struct BArgs {
   const uint32_t* order;
   double *ext, *intr, *pts, *ext2, *intr2, *pts2;
   const double2* obs;
-  const uint32_t *cam, *icam, *pt_off;
+  const uint32_t *cam, *icam, *pt_off, *pt_s;  // pt_s: point of each (sorted) observation
   const int32_t *ext_col, *intr_col;  // problem-local reduced columns (-1 = held)
   const uint8_t* intr_var;
   double* scale_p;
   void *Vinv, *gp, *wscratch;  // compute type
   double* gscr;                // kGlobalSlice doubles per CTA
-  // FP32 path: per observation, the corrected FP64 residual and sqrt(rho')
-  // at the current parameters and at the candidate ([2][3 * total_obs])
-  double* rcache;
+  // FP32 path: FP32 copies of the current parameters and of the point
+  // scales, and per observation the corrected residual and sqrt(rho') of the
+  // FP64 cost evaluation at the current parameters and at the candidate
+  // ([2][total_obs])
+  float *ext_f, *intr_f, *pts_f, *scale_pf;
+  float4* rcache;
   int64_t total_obs;
   int max_views;
   BOut* out;
@@ -86,15 +89,17 @@ struct BArgs {
 // One observation's scratch slot (compute type values): W = Jc^T Jp and
 // W V^-1 (B x 3 each, row i = camera parameter i), the scaled camera Jacobian
 // Jc (2 x B) and, in a window with one intrinsic group, the observation's
-// U_kk lower triangle and intrinsic rhs correction.  Parts start on 4-value
+// U_kk lower triangle, intrinsic rhs correction and intrinsic gradient
+// Jc_k^T r.  Parts start on 4-value
 // (16-byte) boundaries.  The back substitution reuses the slot for Jc z and
 // the residual (4 doubles) and Jp (6 values).
 __host__ __device__ constexpr int rnd4(int v) { return (v + 3) & ~3; }
 template <int K>
 struct Slot {
   static constexpr int B = 6 + K, KK = K * (K + 1) / 2;
-  static constexpr int kW = 0, kWh = rnd4(3 * B), kJ = kWh + rnd4(3 * B), kU = kJ + rnd4(2 * B), kQ = kU + KK;
-  static constexpr int kSize = rnd4(kQ + K);
+  static constexpr int kW = 0, kWh = rnd4(3 * B), kJ = kWh + rnd4(3 * B), kU = kJ + rnd4(2 * B), kQ = kU + KK,
+                       kG = kQ + K;
+  static constexpr int kSize = rnd4(kG + K);
   static_assert(kSize >= 8 + 6, "back substitution entries fit the slot");
 };
 
@@ -116,8 +121,11 @@ struct Shared {
   T S[NS];
   T rhs[N];
   T z[N];
+  T zs[N];  // the camera step in the original parameterisation, z * scale_c
   double scale_c[N];
   double diag_c[N];
+  float scale_cf[N];      // FP32 path: scale_c, and the column norms and
+  float colsq[N], grad[N];  // gradient of the Schur build's Jacobian
   double red[kWarps];
   double bcast[8];
   int flag;
@@ -160,84 +168,54 @@ __device__ __forceinline__ double block_max(double v, double* red, double* out) 
   return *out;
 }
 
-// Residual (FP64), corrected Jacobian blocks (compute type) of observation o.
-// With pose (FP64 pose_matrix of the problem's cameras, indexed from the
-// problem's first camera c0), the FP32 path takes its FP64 residual from it
-// instead of the Rodrigues sine / cosine per observation.
-//
-// With rc (FP32 path), the corrected residual and sqrt(rho') are taken from
-// the residual cache written by the cost evaluation at the same parameters,
-// and only the FP32 Jacobian is evaluated.
+// Linearisation of observation o (point p) at the current parameters: the
+// corrected residual rr and Jacobian blocks (compute type) and the reduced
+// columns of its camera-side parameters.
+//   FP64: residual, robust correction and Jacobian evaluated here from the
+//   FP64 parameters.
+//   FP32: the corrected residual and sqrt(rho') come from the cost
+//   evaluation's cache at the same parameters (rc), the Jacobian from the
+//   FP32 parameter copies (it does not depend on the observed point), so
+//   that no FP64 arithmetic is left.
 template <int M, typename T>
-__device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, const double* intr, const double* pts,
-                                           int64_t o, uint32_t p, double r[2], T Jc[2][6 + Model<M>::K], T Jp[2][3],
-                                           int col[6 + Model<M>::K], const double* pose = nullptr,
-                                           uint32_t c0 = 0, const double* rc = nullptr) {
+__device__ __forceinline__ void obs_lin(const BArgs& a, int64_t o, uint32_t p, const float4* rc, T rr[2],
+                                        T Jc[2][6 + Model<M>::K], T Jp[2][3], int col[6 + Model<M>::K]) {
   constexpr int K = Model<M>::K;
   const uint32_t c = a.cam[o], g = a.icam[o];
-  const double2 ob = a.obs[o];
-  double Ed[6], Kd[K], Xd[3];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) Ed[i] = ext[6 * (int64_t)c + i];
-#pragma unroll
-  for (int i = 0; i < K; ++i) Kd[i] = intr[K * (int64_t)g + i];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) Xd[i] = pts[3 * (int64_t)p + i];
-  T Je[2][6], Jk[2][K], Jx[2][3];
+  T Je[2][6], Jk[2][K], Jx[2][3], s;
   if constexpr (sizeof(T) == 8) {
+    double Ed[6], Kd[K], Xd[3], r[2];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) Ed[i] = a.ext[6 * (int64_t)c + i];
+#pragma unroll
+    for (int i = 0; i < K; ++i) Kd[i] = a.intr[K * (int64_t)g + i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) Xd[i] = a.pts[3 * (int64_t)p + i];
+    const double2 ob = a.obs[o];
     residual<M, double, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (double*)nullptr);
+    double sr1;
+    robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+    rr[0] = r[0] * sr1;
+    rr[1] = r[1] * sr1;
+    s = sr1;
   } else {
-    if (rc) {
-      T Ef[6], Kf[K], Xf[3], rf[2];
-#pragma unroll
-      for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
-#pragma unroll
-      for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
-#pragma unroll
-      for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
-      residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
-      r[0] = rc[0];
-      r[1] = rc[1];
-#pragma unroll
-      for (int j = 0; j < 6; ++j) col[j] = a.ext_col[6 * (int64_t)c + j];
-#pragma unroll
-      for (int j = 0; j < K; ++j) col[6 + j] = a.intr_col[K * (int64_t)g + j];
-      const T s = (T)rc[2];
-#pragma unroll
-      for (int i = 0; i < 2; ++i) {
-#pragma unroll
-        for (int j = 0; j < 6; ++j) Jc[i][j] = Je[i][j] * s;
-#pragma unroll
-        for (int j = 0; j < K; ++j) Jc[i][6 + j] = Jk[i][j] * s;
-#pragma unroll
-        for (int j = 0; j < 3; ++j) Jp[i][j] = Jx[i][j] * s;
-      }
-      return 0.0;
-    }
-    if (pose) {
-      residual_pose<M, double>(Kd, pose + 12 * (c - c0), Xd, ob.x, ob.y, r);
-    } else {
-      double dJe[2][6], dJk[2][K], dJx[2][3];
-      residual<M, double, false>(Kd, Ed, Xd, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
-    }
     T Ef[6], Kf[K], Xf[3], rf[2];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) Ef[i] = (T)Ed[i];
+    for (int i = 0; i < 6; ++i) Ef[i] = a.ext_f[6 * (int64_t)c + i];
 #pragma unroll
-    for (int i = 0; i < K; ++i) Kf[i] = (T)Kd[i];
+    for (int i = 0; i < K; ++i) Kf[i] = a.intr_f[K * (int64_t)g + i];
 #pragma unroll
-    for (int i = 0; i < 3; ++i) Xf[i] = (T)Xd[i];
-    residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
+    for (int i = 0; i < 3; ++i) Xf[i] = a.pts_f[3 * (int64_t)p + i];
+    residual<M, T, true>(Kf, Ef, Xf, T(0), T(0), rf, Je, Jk, Jx, (T*)nullptr);
+    const float4 q = rc[o];
+    rr[0] = q.x;
+    rr[1] = q.y;
+    s = q.z;
   }
-  double sr1;
-  const double cost = robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
-  r[0] *= sr1;
-  r[1] *= sr1;
 #pragma unroll
   for (int j = 0; j < 6; ++j) col[j] = a.ext_col[6 * (int64_t)c + j];
 #pragma unroll
   for (int j = 0; j < K; ++j) col[6 + j] = a.intr_col[K * (int64_t)g + j];
-  const T s = (T)sr1;
 #pragma unroll
   for (int i = 0; i < 2; ++i) {
 #pragma unroll
@@ -247,7 +225,6 @@ __device__ __forceinline__ double obs_eval(const BArgs& a, const double* ext, co
 #pragma unroll
     for (int j = 0; j < 3; ++j) Jp[i][j] = Jx[i][j] * s;
   }
-  return cost;
 }
 
 // T: Jacobians and point blocks; SS: the shared-memory S, its factor and the step.
@@ -292,6 +269,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   auto Radd = [&](int i, SS v) {
     if constexpr (kGS) atomicAdd(g_rhs + i, (double)v);
     else atomicAdd(&sh.rhs[i], v);
+  };
+  // the Schur build's column norms (Nadd) and gradient (Gadd) of the scaled
+  // Jacobian: FP64 in the global slice, FP32 in shared memory
+  auto Nadd = [&](int i, T v) {
+    if constexpr (kGS) atomicAdd(g_acc + i, (double)v);
+    else atomicAdd(&sh.colsq[i], (float)v);
+  };
+  auto Gadd = [&](int i, T v) {
+    if constexpr (kGS) atomicAdd(g_grad + i, (double)v);
+    else atomicAdd(&sh.grad[i], (float)v);
   };
 
   const bool use_pose = P.nc <= (uint32_t)kPoseCams;
@@ -341,8 +328,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   // residual cache (FP32 path): slot `cur` holds the current parameters'
   constexpr bool kCache = sizeof(T) == 4;
   int cur = 0;
-  auto rc_at = [&](int64_t o) -> const double* {
-    return kCache ? a.rcache + (int64_t)cur * 3 * a.total_obs + 3 * o : nullptr;
+  auto rc_cur = [&]() -> const float4* { return kCache ? a.rcache + (int64_t)cur * a.total_obs : nullptr; };
+  // FP32 path: FP32 copies of the window's parameters (ext, intr, pts)
+  auto make_f32 = [&](const double* ext, const double* intr, const double* pts) {
+    if constexpr (kCache) {
+      for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) a.ext_f[6 * (int64_t)P.c0 + i] = (float)ext[6 * (int64_t)P.c0 + i];
+      for (uint32_t i = tid; i < K * P.ni; i += kThreads) a.intr_f[K * (int64_t)P.g0 + i] = (float)intr[K * (int64_t)P.g0 + i];
+      for (uint32_t i = tid; i < 3 * (P.x1 - P.x0); i += kThreads)
+        a.pts_f[3 * (int64_t)P.x0 + i] = (float)pts[3 * (int64_t)P.x0 + i];
+    }
+  };
+  // scales in the compute type
+  auto csc = [&](int i) -> T {
+    if constexpr (kCache) return sh.scale_cf[i];
+    else return sh.scale_c[i];
+  };
+  auto psc = [&](uint32_t p, int j) -> T {
+    if constexpr (kCache) return a.scale_pf[3 * (int64_t)p + j];
+    else return a.scale_p[3 * (int64_t)p + j];
   };
   // poses of ext (slot 0) or ext2 (slot 1); the barrier makes them visible
   auto make_poses = [&](const double* ext, int slot) {
@@ -356,30 +359,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     __syncthreads();
   };
-  const double* pose_x = use_pose ? sh.pose[0] : nullptr;
   auto cost_at = [&](const double* ext, const double* intr, const double* pts, bool* finite) -> double {
     const double* pz = !use_pose ? nullptr : ext == a.ext ? sh.pose[0] : sh.pose[1];
-    double* wc = kCache ? a.rcache + (int64_t)(ext == a.ext ? cur : cur ^ 1) * 3 * a.total_obs : nullptr;
+    float4* wc = kCache ? a.rcache + (int64_t)(ext == a.ext ? cur : cur ^ 1) * a.total_obs : nullptr;
     double acc = 0.0;
-    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
-      // obs of point p are [pt_off[p], pt_off[p+1])
-      for (uint32_t o = a.pt_off[p] + lane; o < a.pt_off[p + 1]; o += 32) {
-        const uint32_t c = a.cam[o], g = a.icam[o];
-        double E[6], Kp[K], X[3], r[2], dJe[2][6], dJk[2][K], dJx[2][3];
-        for (int i = 0; i < 6; ++i) E[i] = ext[6 * (int64_t)c + i];
-        for (int i = 0; i < K; ++i) Kp[i] = intr[K * (int64_t)g + i];
-        for (int i = 0; i < 3; ++i) X[i] = pts[3 * (int64_t)p + i];
-        const double2 ob = a.obs[o];
-        if (pz) residual_pose<M, double>(Kp, pz + 12 * (c - P.c0), X, ob.x, ob.y, r);
-        else residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
-        double sr1;
-        acc += robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
-        if (wc) {
-          wc[3 * (int64_t)o] = r[0] * sr1;
-          wc[3 * (int64_t)o + 1] = r[1] * sr1;
-          wc[3 * (int64_t)o + 2] = sr1;
-        }
-      }
+    // one thread per observation: the cost needs no per-point sums
+    const uint32_t oz = a.pt_off[P.x1];
+    for (uint32_t o = a.pt_off[P.x0] + tid; o < oz; o += kThreads) {
+      const uint32_t p = a.pt_s[o], c = a.cam[o], g = a.icam[o];
+      double E[6], Kp[K], X[3], r[2], dJe[2][6], dJk[2][K], dJx[2][3];
+      for (int i = 0; i < 6; ++i) E[i] = ext[6 * (int64_t)c + i];
+      for (int i = 0; i < K; ++i) Kp[i] = intr[K * (int64_t)g + i];
+      for (int i = 0; i < 3; ++i) X[i] = pts[3 * (int64_t)p + i];
+      const double2 ob = a.obs[o];
+      if (pz) residual_pose<M, double>(Kp, pz + 12 * (c - P.c0), X, ob.x, ob.y, r);
+      else residual<M, double, false>(Kp, E, X, ob.x, ob.y, r, dJe, dJk, dJx, (double*)nullptr);
+      double sr1;
+      acc += robust<double>(a.loss_type, a.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+      if (wc) wc[o] = make_float4((float)(r[0] * sr1), (float)(r[1] * sr1), (float)sr1, 0.f);
     }
     const double c = block_sum(acc, sh.red, &sh.bcast[0]);
     *finite = isfinite(c);
@@ -417,10 +414,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       double cp[3] = {0, 0, 0}, gp3[3] = {0, 0, 0};
       for (uint32_t o = a.pt_off[p] + lane; o < a.pt_off[p + 1]; o += 32) {
-        double r[2];
-        T Jc[2][B], Jp[2][3];
+        T rr[2], Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
+        obs_lin<M, T>(a, o, p, rc_cur(), rr, Jc, Jp, col);
+        const double r[2] = {(double)rr[0], (double)rr[1]};
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
@@ -442,13 +439,20 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       }
       if (lane < 3) {
         const double c = lane == 0 ? cp[0] : lane == 1 ? cp[1] : cp[2];
-        if (first) a.scale_p[3 * (int64_t)p + lane] = a.jacobi ? 1.0 / (1.0 + sqrt(c)) : 1.0;
+        if (first) {
+          const double sc = a.jacobi ? 1.0 / (1.0 + sqrt(c)) : 1.0;
+          a.scale_p[3 * (int64_t)p + lane] = sc;
+          if constexpr (kCache) a.scale_pf[3 * (int64_t)p + lane] = (float)sc;
+        }
         gm = fmax(gm, fabs(lane == 0 ? gp3[0] : lane == 1 ? gp3[1] : gp3[2]));
       }
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
-      if (first) sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(__ldcg(g_acc + i))) : 1.0;
+      if (first) {
+        sh.scale_c[i] = a.jacobi ? 1.0 / (1.0 + sqrt(__ldcg(g_acc + i))) : 1.0;
+        sh.scale_cf[i] = (float)sh.scale_c[i];
+      }
       gm = fmax(gm, fabs(__ldcg(g_grad + i)));
     }
     return block_max(gm, sh.red, &sh.bcast[1]);
@@ -458,6 +462,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   if (use_pose)
     for (uint32_t i = tid; i < 6 * P.nc; i += kThreads) sh.ecol[i] = a.ext_col[6 * (int64_t)P.c0 + i];
   if (tid < 8) sh.kcol[tid] = P.ni == 1 && tid < K ? a.intr_col[K * (int64_t)P.g0 + tid] : -1;
+  make_f32(a.ext, a.intr, a.pts);
   bool finite = true;
   make_poses(a.ext, 0);
   double cost = cost_at(a.ext, a.intr, a.pts, &finite);
@@ -490,10 +495,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     // the same Jacobian the column norms (LM diagonal) and the gradient
     for (int i = tid; i < n * (n + 1) / 2; i += kThreads) Sst(i, SS(0));
     for (int i = tid; i < n; i += kThreads) {
-      if constexpr (kGS) __stcg(g_rhs + i, 0.0);
-      else sh.rhs[i] = SS(0);
-      __stcg(g_acc + i, 0.0);
-      __stcg(g_grad + i, 0.0);
+      if constexpr (kGS) {
+        __stcg(g_rhs + i, 0.0);
+        __stcg(g_acc + i, 0.0);
+        __stcg(g_grad + i, 0.0);
+      } else {
+        sh.rhs[i] = SS(0);
+        sh.colsq[i] = 0.f;
+        sh.grad[i] = 0.f;
+      }
     }
     if (tid == 0) sh.flag = 0;
     __syncthreads();
@@ -505,29 +515,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     // and only the 6x6 extrinsic blocks need the observation pairs (one lane
     // per pair; an observation's own pair carries its U_ee).
     const bool one_group = P.ni == 1;
-    double gm = 0.0;  // gradient max norm (unscaled) over this thread's points and columns
+    const T irad = T(1.0 / radius), dmin = (T)a.dmin, dmax = (T)a.dmax;
+    T gmt = T(0);  // gradient max norm (unscaled) over this thread's points
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1], m = oe - ob;
-      const double* spp = a.scale_p + 3 * (int64_t)p;
+      const T sp[3] = {psc(p, 0), psc(p, 1), psc(p, 2)};
       T v[6] = {}, g[3] = {};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
-        double r[2];
-        T Jc[2][B], Jp[2][3];
+        T rr[2], Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
+        obs_lin<M, T>(a, o, p, rc_cur(), rr, Jc, Jp, col);
 #pragma unroll
         for (int j = 0; j < B; ++j) {
-          const T s = col[j] >= 0 ? (T)sh.scale_c[col[j]] : T(0);
+          const T s = col[j] >= 0 ? csc(col[j]) : T(0);
           Jc[0][j] *= s;
           Jc[1][j] *= s;
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          const T s = (T)spp[j];
-          Jp[0][j] *= s;
-          Jp[1][j] *= s;
+          Jp[0][j] *= sp[j];
+          Jp[1][j] *= sp[j];
         }
-        const T r0 = (T)r[0], r1 = (T)r[1];
+        const T r0 = rr[0], r1 = rr[1];
         v[0] += Jp[0][0] * Jp[0][0] + Jp[1][0] * Jp[1][0];
         v[1] += Jp[0][0] * Jp[0][1] + Jp[1][0] * Jp[1][1];
         v[2] += Jp[0][0] * Jp[0][2] + Jp[1][0] * Jp[1][2];
@@ -546,13 +555,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
           W[SL::kJ + i] = Jc[0][i];
           W[SL::kJ + B + i] = Jc[1][i];
         }
-        // column norms and gradient of the scaled Jacobian, FP64 sums
+        // column norms and gradient of the scaled Jacobian (the intrinsic
+        // columns of a one-group window through the per-point sums: every
+        // observation shares them)
 #pragma unroll
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
-          const double x0 = Jc[0][j], x1 = Jc[1][j];
-          atomicAdd(g_acc + col[j], x0 * x0 + x1 * x1);
-          atomicAdd(g_grad + col[j], x0 * r[0] + x1 * r[1]);
+          const T x0 = Jc[0][j], x1 = Jc[1][j];
+          if (one_group && j >= 6) {
+            W[SL::kG + (j - 6)] = x0 * r0 + x1 * r1;
+            continue;
+          }
+          Nadd(col[j], x0 * x0 + x1 * x1);
+          Gadd(col[j], x0 * r0 + x1 * r1);
         }
         if (one_group) {
           // the observation's U_kk lower triangle (held columns are skipped at the reduction)
@@ -581,11 +596,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
 #pragma unroll
       for (int i = 0; i < 3; ++i) g[i] = warp_sum(g[i]);
 #pragma unroll
-      for (int j = 0; j < 3; ++j) gm = fmax(gm, fabs((double)g[j] / spp[j]));
+      for (int j = 0; j < 3; ++j) gmt = fmax(gmt, fabs(g[j] / sp[j]));
       // point block damped by its own LM diagonal clamp(diag V) / radius
-      const T a00 = v[0] + (T)(fmin(fmax((double)v[0], a.dmin), a.dmax) / radius),
-              a11 = v[3] + (T)(fmin(fmax((double)v[3], a.dmin), a.dmax) / radius),
-              a22 = v[5] + (T)(fmin(fmax((double)v[5], a.dmin), a.dmax) / radius);
+      const T a00 = v[0] + fmin(fmax(v[0], dmin), dmax) * irad, a11 = v[3] + fmin(fmax(v[3], dmin), dmax) * irad,
+              a22 = v[5] + fmin(fmax(v[5], dmin), dmax) * irad;
       const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
       const T d1 = a11 - l10 * l10;
       const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
@@ -638,17 +652,23 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
           sums[e] = hs;
           sums[3 * K + e] = ws;
         }
-        // the point's U_kk and intrinsic rhs correction: sums over its observations' slots
-        for (int e = lane; e < KK + K; e += 32) {
+        // the point's U_kk (its diagonal: the column norms), intrinsic rhs
+        // correction and intrinsic gradient: sums over its observations' slots
+        for (int e = lane; e < KK + 2 * K; e += 32) {
           T acc = T(0);
           for (uint32_t x = 0; x < m; ++x) acc += wsc[(int64_t)x * SL::kSize + SL::kU + e];
           if (e < KK) {
             int i = 0;
             while ((i + 1) * (i + 2) / 2 <= e) ++i;
             const int j = e - i * (i + 1) / 2;
-            if (sh.kcol[i] >= 0 && sh.kcol[j] >= 0) Sadd(tri(sh.kcol[i], sh.kcol[j]), (SS)acc);
-          } else if (sh.kcol[e - KK] >= 0) {
-            Radd(sh.kcol[e - KK], (SS)acc);
+            if (sh.kcol[i] >= 0 && sh.kcol[j] >= 0) {
+              Sadd(tri(sh.kcol[i], sh.kcol[j]), (SS)acc);
+              if (i == j) Nadd(sh.kcol[i], acc);
+            }
+          } else if (e < KK + K) {
+            if (sh.kcol[e - KK] >= 0) Radd(sh.kcol[e - KK], (SS)acc);
+          } else if (sh.kcol[e - KK - K] >= 0) {
+            Gadd(sh.kcol[e - KK - K], acc);
           }
         }
         __syncwarp();
@@ -730,13 +750,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     __syncthreads();
     // LM diagonal D_c^2 = clamp(column norms), rhs = gradient + Schur
     // correction, gradient max norm of this linearisation
+    double gm = (double)gmt;
     for (int i = tid; i < n; i += kThreads) {
-      const double d = fmin(fmax(__ldcg(g_acc + i), a.dmin), a.dmax);
+      const double acc = kGS ? __ldcg(g_acc + i) : (double)sh.colsq[i];
+      const double gi = kGS ? __ldcg(g_grad + i) : (double)sh.grad[i];
+      const double d = fmin(fmax(acc, a.dmin), a.dmax);
       sh.diag_c[i] = d;
       Sst(tri(i, i), Sld(tri(i, i)) + (SS)(d / radius));
-      const double gi = __ldcg(g_grad + i);
-      if constexpr (kGS) sh.rhs[i] = (SS)(gi + __ldcg(g_rhs + i));
-      else sh.rhs[i] = (SS)(gi + (double)sh.rhs[i]);
+      sh.rhs[i] = (SS)(gi + (kGS ? __ldcg(g_rhs + i) : (double)sh.rhs[i]));
       gm = fmax(gm, fabs(gi / sh.scale_c[i]));
     }
     gmax = block_max(gm, sh.red, &sh.bcast[1]);
@@ -791,40 +812,40 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       if (tid == 0) sh.z[j] = xj;
       __syncthreads();
     }
+    // camera step in the original parameterisation
+    for (int j = tid; j < n; j += kThreads) sh.zs[j] = (SS)((double)sh.z[j] * sh.scale_c[j]);
+    __syncthreads();
     // ---- back substitution, model cost change, candidate points.  The
-    // first pass over a point's observations keeps each one's Jc z (FP64),
-    // residual and Jp in its scratch slot for the second pass.
+    // first pass over a point's observations keeps each one's Jc z, residual
+    // and Jp in its scratch slot for the second pass.
     double mcc = 0.0, stp = 0.0;
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1];
-      const double* spp = a.scale_p + 3 * (int64_t)p;
+      const T sp[3] = {psc(p, 0), psc(p, 1), psc(p, 2)};
       T t[3] = {};
       for (uint32_t o = ob + lane; o < oe; o += 32) {
-        double r[2];
-        T Jc[2][B], Jp[2][3];
+        T rr[2], Jc[2][B], Jp[2][3];
         int col[B];
-        obs_eval<M, T>(a, a.ext, a.intr, a.pts, o, p, r, Jc, Jp, col, pose_x, P.c0, rc_at(o));
-        double f0 = 0.0, f1 = 0.0;
+        obs_lin<M, T>(a, o, p, rc_cur(), rr, Jc, Jp, col);
+        T f0 = T(0), f1 = T(0);
 #pragma unroll
         for (int i = 0; i < B; ++i) {
           if (col[i] < 0) continue;
-          const double zi = (double)sh.z[col[i]] * sh.scale_c[col[i]];
-          f0 += (double)Jc[0][i] * zi;
-          f1 += (double)Jc[1][i] * zi;
+          const T zi = sh.zs[col[i]];
+          f0 += Jc[0][i] * zi;
+          f1 += Jc[1][i] * zi;
         }
-        const T fz0 = (T)f0, fz1 = (T)f1;
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] += (Jp[0][j] * fz0 + Jp[1][j] * fz1) * (T)spp[j];
-        double* d = reinterpret_cast<double*>(wsc + (int64_t)(o - ob) * SL::kSize);
+        for (int j = 0; j < 3; ++j) t[j] += (Jp[0][j] * f0 + Jp[1][j] * f1) * sp[j];
+        T* d = wsc + (int64_t)(o - ob) * SL::kSize;
         d[0] = f0;
         d[1] = f1;
-        d[2] = r[0];
-        d[3] = r[1];
-        T* jp = reinterpret_cast<T*>(d + 4);
+        d[2] = rr[0];
+        d[3] = rr[1];
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
-          jp[j] = Jp[0][j];
-          jp[3 + j] = Jp[1][j];
+          d[4 + j] = Jp[0][j];
+          d[7 + j] = Jp[1][j];
         }
       }
 #pragma unroll
@@ -834,24 +855,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       const T y[3] = {vi[0] * q0 + vi[1] * q1 + vi[2] * q2, vi[1] * q0 + vi[3] * q1 + vi[4] * q2,
                       vi[2] * q0 + vi[4] * q1 + vi[5] * q2};
       if (!isfinite((double)y[0]) || !isfinite((double)y[1]) || !isfinite((double)y[2])) sh.flag = 3;
-      double ys[3];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) ys[j] = (double)y[j] * spp[j];
+      const T ys[3] = {y[0] * sp[0], y[1] * sp[1], y[2] * sp[2]};
+      // model cost change: each term in the compute type, the sum in FP64
       for (uint32_t o = ob + lane; o < oe; o += 32) {
-        const double* d = reinterpret_cast<const double*>(wsc + (int64_t)(o - ob) * SL::kSize);
-        const T* jp = reinterpret_cast<const T*>(d + 4);
-        double m0 = d[0], m1 = d[1];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-          m0 += (double)jp[j] * ys[j];
-          m1 += (double)jp[3 + j] * ys[j];
-        }
-        m0 = -m0;
-        m1 = -m1;
-        mcc += -(m0 * (d[2] + m0 / 2.0) + m1 * (d[3] + m1 / 2.0));
+        const T* d = wsc + (int64_t)(o - ob) * SL::kSize;
+        const T m0 = -(d[0] + d[4] * ys[0] + d[5] * ys[1] + d[6] * ys[2]);
+        const T m1 = -(d[1] + d[7] * ys[0] + d[8] * ys[1] + d[9] * ys[2]);
+        mcc += (double)(-(m0 * (d[2] + m0 / T(2)) + m1 * (d[3] + m1 / T(2))));
       }
       if (lane < 3) {
-        const double dx = -(lane == 0 ? ys[0] : lane == 1 ? ys[1] : ys[2]);
+        const double dx = -(double)(lane == 0 ? y[0] : lane == 1 ? y[1] : y[2]) * a.scale_p[3 * (int64_t)p + lane];
         a.pts2[3 * (int64_t)p + lane] = a.pts[3 * (int64_t)p + lane] + dx;
         stp += dx * dx;
       }
@@ -914,6 +927,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       for (uint32_t i = tid; i < K * P.ni; i += kThreads) a.intr[K * (int64_t)P.g0 + i] = a.intr2[K * (int64_t)P.g0 + i];
       if (use_pose)
         for (uint32_t i = tid; i < 12 * P.nc; i += kThreads) sh.pose[0][i] = sh.pose[1][i];
+      make_f32(a.ext2, a.intr2, a.pts2);
       cur ^= 1;  // the candidate's residual cache becomes the current one
       __syncthreads();
       xnorm = param_norm();
@@ -1029,7 +1043,9 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
       BOut* out;
       void *Vinv, *gp, *wsc;
       double* gscr;
-      double* rcache;
+      float4* rcache;
+      float *ext_f, *intr_f, *pts_f, *scale_pf;
+      uint32_t* pt_s;
     } q;
     q.ext = A.template take<double>(6 * tc); q.intr = A.template take<double>(k * tg); q.pts = A.template take<double>(3 * tx);
     q.ext2 = A.template take<double>(6 * tc); q.intr2 = A.template take<double>(k * tg); q.pts2 = A.template take<double>(3 * tx);
@@ -1045,7 +1061,10 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     q.Vinv = A.template take<char>(6 * tx * tsize); q.gp = A.template take<char>(3 * tx * tsize);
     q.wsc = A.template take<char>((size_t)np_ * kWarps * (max_views + 1) * slot_values * tsize);
     q.gscr = A.template take<double>((size_t)np_ * kGlobalSlice);
-    q.rcache = A.template take<double>((size_t)6 * std::max<int64_t>(to, 1));
+    q.rcache = A.template take<float4>((size_t)2 * std::max<int64_t>(to, 1));
+    q.ext_f = A.template take<float>(6 * tc); q.intr_f = A.template take<float>(k * tg);
+    q.pts_f = A.template take<float>(3 * tx); q.scale_pf = A.template take<float>(3 * tx);
+    q.pt_s = A.template take<uint32_t>(to);
     return q;
   };
   plan(pl);
@@ -1103,13 +1122,15 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
     std::vector<uint32_t> hperm(to);
     GBBA_CUDA(cudaMemcpyAsync(hperm.data(), q.perm, 4 * to, cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaStreamSynchronize(st));
-    std::vector<uint32_t> c2(to), g2(to);
+    std::vector<uint32_t> c2(to), g2(to), p2(to);
     for (int64_t i = 0; i < to; ++i) {
       c2[i] = cam[hperm[i]];
       g2[i] = icam[hperm[i]];
+      p2[i] = pt[hperm[i]];
     }
     GBBA_CUDA(cudaMemcpyAsync(q.cam_s, c2.data(), 4 * to, cudaMemcpyHostToDevice, st));
     GBBA_CUDA(cudaMemcpyAsync(q.icam_s, g2.data(), 4 * to, cudaMemcpyHostToDevice, st));
+    GBBA_CUDA(cudaMemcpyAsync(q.pt_s, p2.data(), 4 * to, cudaMemcpyHostToDevice, st));
     std::vector<double> ob(2 * to);
     if (mem == GBBA_MEMORY_HOST) {
       for (int64_t i = 0; i < to; ++i) {
@@ -1135,6 +1156,7 @@ gbba_status solve_batched_impl(gbba_handle* h, const gbba_problem* probs, int32_
   a.ext_col = q.ecol; a.intr_col = q.icol; a.intr_var = q.ivar;
   a.scale_p = q.scale_p; a.Vinv = q.Vinv; a.gp = q.gp; a.wscratch = q.wsc; a.gscr = q.gscr;
   a.rcache = q.rcache; a.total_obs = to;
+  a.ext_f = q.ext_f; a.intr_f = q.intr_f; a.pts_f = q.pts_f; a.scale_pf = q.scale_pf; a.pt_s = q.pt_s;
   a.max_views = max_views; a.out = q.out;
   a.max_iterations = o->max_num_iterations; a.max_invalid = o->max_num_consecutive_invalid_steps;
   a.jacobi = o->jacobi_scaling; a.loss_type = o->loss_type; a.loss_a = o->loss_scale;
