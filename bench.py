@@ -78,7 +78,7 @@ def factor_flops(n_red):
 # DRAM bytes (read + write) of one Schur phase on the medium workload: ncu's
 # dram__bytes_read.sum + dram__bytes_write.sum summed over the phase's four
 # kernels (profiles/schur_phase_medium.md).
-SCHUR_TRAFFIC_PER_PHASE = 4.65e9
+SCHUR_TRAFFIC_PER_PHASE = 4.96e9
 
 # FP32 SIMT peak of a GB300: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
