@@ -21,9 +21,12 @@ Metric: observations x LM iterations per second (higher is better).
   factor_roofline  the dense FP32 Cholesky of S (a latency-bound chain of
              64-wide panels): n^3/3 flops / its event-timed duration against
              the FP32 SIMT peak.
-  time_to_cost  plain FP64 GPU path run to convergence gives C*; the mixed
-             path (FP32 LM, then its FP64 polish of at most 10 iterations)
-             is timed to its final cost and checked against (1+1e-6) C*.
+  time_to_cost  plain FP64 GPU path run to convergence (ceres's stopping
+             rule) gives C*; the mixed path with the same options and no
+             FP64 polish is timed to its final cost and checked against
+             (1+1e-6) C*.  The mixed run finished by its FP64 polish (at most
+             10 iterations, each a plain-FP64 iteration) is reported beside
+             it.
   cpu_baseline  the CPU oracle (restatement of ceres LM + dense Schur,
              OpenMP over the host cores) on a bounded sample: 1 LM iteration.
 
@@ -454,10 +457,12 @@ def run_ours(args):
     # ---- time to cost: plain FP64 GPU to convergence (C*), mixed to (1+1e-6) C*
     if args.time_to_cost and rank == 0:
         ttc = {}
-        for name, prec in (("fp64", abi.PRECISION_FP64), ("mixed", abi.PRECISION_MIXED)):
+        for name, prec, polish in (("fp64", abi.PRECISION_FP64, 0), ("mixed", abi.PRECISION_MIXED, 0),
+                                   ("mixed_fp64_polish", abi.PRECISION_MIXED, 10)):
             for f, v in pristine.items():
                 getattr(dp, f).copy_(v)
             o = solve_options(scene, args.ttc_iters, prec, stream=sptr, tol=True)
+            o.fp64_polish_iterations = polish
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             h.check(h.lib.gbba_solve(h.h, ctypes.byref(st), ctypes.byref(o), ctypes.byref(summ)), "ttc")
@@ -465,8 +470,11 @@ def run_ours(args):
             ttc[name] = {"seconds": time.perf_counter() - t0, "final_cost": summ.final_cost,
                          "iterations": summ.num_iterations, "termination": summ.termination_type}
         cstar = ttc["fp64"]["final_cost"]
-        ttc["mixed_reaches_cstar"] = bool(ttc["mixed"]["final_cost"] <= cstar * (1 + 1e-6))
-        ttc["speedup"] = ttc["fp64"]["seconds"] / ttc["mixed"]["seconds"]
+        for name in ("mixed", "mixed_fp64_polish"):
+            ttc[name]["reaches_cstar"] = bool(ttc[name]["final_cost"] <= cstar * (1 + 1e-6))
+            ttc[name]["speedup"] = ttc["fp64"]["seconds"] / ttc[name]["seconds"]
+        ttc["mixed_reaches_cstar"] = ttc["mixed"]["reaches_cstar"]
+        ttc["speedup"] = ttc["mixed"]["speedup"]
         line["time_to_cost"] = ttc
     if rank == 0 and args.triangulation:
         line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup)
