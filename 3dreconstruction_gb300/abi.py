@@ -130,6 +130,18 @@ class GbbaSummary(C.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+TUNE_MAX_CANDIDATES = 4
+
+
+class GbbaTuning(C.Structure):
+    _fields_ = [
+        ("pair_chunk", C.c_int32),
+        ("num_candidates", C.c_int32),
+        ("candidates", C.c_int32 * TUNE_MAX_CANDIDATES),
+        ("schur_time_s", C.c_double * TUNE_MAX_CANDIDATES),
+    ]
+
+
 def default_options(**kw):
     """ceres::Solver::Options defaults (include/ceres/solver.h:81-129)."""
     o = GbbaOptions()
@@ -279,6 +291,8 @@ def declare_gbba(lib):
     lib.gbba_solve.restype = C.c_int
     lib.gbba_solve_batched.argtypes = [vp, P(GbbaProblem), C.c_int32, P(GbbaOptions), P(GbbaSummary)]
     lib.gbba_solve_batched.restype = C.c_int
+    lib.gbba_autotune.argtypes = [vp, P(GbbaProblem), P(GbbaOptions), C.c_int32, P(GbbaTuning)]
+    lib.gbba_autotune.restype = C.c_int
     lib.gbba_project_forward.argtypes = [vp, P(GbbaProblem), C.c_int32, C.c_double, vp, vp]
     lib.gbba_project_forward.restype = C.c_int
     lib.gbba_project_backward.argtypes = [vp, P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp, vp]
@@ -299,7 +313,7 @@ def declare_gbba(lib):
 # Every symbol the C-ABI headers declare (checked by the CPU tests).
 EXPORTED_SYMBOLS = (
     "gbba_create", "gbba_destroy", "gbba_default_options", "gbba_status_string",
-    "gbba_abi_version", "gbba_launch_count", "gbba_solve", "gbba_solve_batched",
+    "gbba_abi_version", "gbba_launch_count", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
     "gbba_project_forward", "gbba_project_backward", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
 )

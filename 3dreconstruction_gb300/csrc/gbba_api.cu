@@ -286,6 +286,77 @@ gbba_status gbba_solve_batched(gbba_handle* h, const gbba_problem* problems, int
   return guarded(h, o->stream, [&]() { return solve_batched_impl(h, problems, num_problems, o, summaries); });
 }
 
+gbba_status gbba_autotune(gbba_handle* h, const gbba_problem* P, const gbba_options* o, int32_t iterations,
+                          gbba_tuning* out) {
+  if (!o || !out || iterations < 1) return GBBA_ERROR_INVALID_ARGUMENT;
+  const gbba_status pc = check_problem(P);
+  if (pc != GBBA_SUCCESS) return pc;
+  std::memset(out, 0, sizeof(*out));
+  return guarded(h, o->stream, [&]() -> gbba_status {
+    const int k = P->camera_model == kPinholeF ? 1 : P->camera_model == kRadialK3 ? 6 : 8;
+    const size_t ne = 6 * (size_t)P->num_cameras, ni = k * (size_t)P->num_intrinsics, np = 3 * (size_t)P->num_points;
+    const bool dev = P->memory == GBBA_MEMORY_DEVICE;
+    cudaStream_t st = h->active;
+    // the parameters, restored after every trial
+    std::vector<double> keep(ne + ni + np);
+    auto move = [&](bool save) {
+      double* arr[3] = {P->extrinsics, P->intrinsics, P->points};
+      const size_t cnt[3] = {ne, ni, np};
+      size_t off = 0;
+      for (int a = 0; a < 3; ++a) {
+        if (cnt[a]) {
+          double* host = keep.data() + off;
+          if (!dev) std::memcpy(save ? host : arr[a], save ? arr[a] : host, 8 * cnt[a]);
+          else
+            GBBA_CUDA(cudaMemcpyAsync(save ? (void*)host : (void*)arr[a], save ? (const void*)arr[a] : (const void*)host,
+                                      8 * cnt[a], save ? cudaMemcpyDeviceToHost : cudaMemcpyHostToDevice, st));
+        }
+        off += cnt[a];
+      }
+      if (dev) GBBA_CUDA(cudaStreamSynchronize(st));
+    };
+    move(true);
+    // fixed work per trial: exactly `iterations` LM iterations
+    gbba_options t = *o;
+    t.max_num_iterations = iterations;
+    t.function_tolerance = 0.0;
+    t.gradient_tolerance = 0.0;
+    t.parameter_tolerance = 0.0;
+    t.fp64_polish_iterations = 0;
+    const int32_t cand[3] = {32, 64, 128};
+    const int keep_chunk = h->pair_chunk;
+    out->num_candidates = 3;
+    int best = -1;
+    for (int c = 0; c < 3; ++c) {
+      h->pair_chunk = cand[c];
+      double per_iter = 0.0;
+      for (int rep = 0; rep < 2; ++rep) {  // the first run warms the workspace
+        gbba_summary sum;
+        std::memset(&sum, 0, sizeof(sum));
+        gbba_status s = GBBA_SUCCESS;
+        try {
+          s = solve_impl(h, P, &t, &sum);
+        } catch (...) {
+          h->pair_chunk = keep_chunk;
+          throw;
+        }
+        move(false);
+        if (s != GBBA_SUCCESS) {
+          h->pair_chunk = keep_chunk;
+          return s;
+        }
+        per_iter = sum.num_iterations > 0 ? sum.schur_kernel_time_s / sum.num_iterations : sum.schur_kernel_time_s;
+      }
+      out->candidates[c] = cand[c];
+      out->schur_time_s[c] = per_iter;
+      if (best < 0 || per_iter < out->schur_time_s[best]) best = c;
+    }
+    h->pair_chunk = cand[best];
+    out->pair_chunk = cand[best];
+    return GBBA_SUCCESS;
+  });
+}
+
 gbba_status gbba_project_forward(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,
                                  double* residuals, double* cost) {
   const gbba_status pc = check_problem(P);

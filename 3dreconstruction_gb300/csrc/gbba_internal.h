@@ -98,6 +98,8 @@ struct gbba_handle {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_main = nullptr, ev_side = nullptr;
   int prio_hi = 0;
+  // observation pairs per work item of the camera-pair products (gbba_autotune)
+  int pair_chunk = 128;
 };
 
 namespace gbba {

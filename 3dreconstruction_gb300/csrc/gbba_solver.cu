@@ -2189,7 +2189,8 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
                                                 key_bits(nk), st));
       count_launch(h, 4);
     }
-    // work items: chunks of at most kPairChunk pairs per camera-pair block
+    // work items: chunks of at most `chunk` (<= kPairChunk) pairs per camera-pair block
+    const uint32_t chunk = (uint32_t)std::min(std::max(h->pair_chunk, 1), kPairChunk);
     std::vector<uint32_t> hoff(nk + 1);
     GBBA_CUDA(cudaMemcpyAsync(hoff.data(), s.blk_off, sizeof(uint32_t) * (nk + 1), cudaMemcpyDeviceToHost, st));
     GBBA_CUDA(cudaStreamSynchronize(st));
@@ -2199,14 +2200,14 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     for (int64_t key = 0; key < nk; ++key) {
       const uint32_t b = hoff[key], e = hoff[key + 1];
       if (e == b) continue;
-      const uint32_t nch = (e - b + kPairChunk - 1) / kPairChunk;
+      const uint32_t nch = (e - b + chunk - 1) / chunk;
       if (nch == 1) {
         items.push_back(PairItem{(uint32_t)key, b, e, -1});
         continue;
       }
       merges.push_back(PairMerge{(uint32_t)key, (uint32_t)slots, nch});
       for (uint32_t c = 0; c < nch; ++c)
-        items.push_back(PairItem{(uint32_t)key, b + c * kPairChunk, std::min(e, b + (c + 1) * kPairChunk), slots++});
+        items.push_back(PairItem{(uint32_t)key, b + c * chunk, std::min(e, b + (c + 1) * chunk), slots++});
     }
     Arena& I = h->item_arena;
     I.reset();

@@ -193,6 +193,24 @@ gbba_status gbba_solve_batched(gbba_handle* handle, const gbba_problem* problems
                                int32_t num_problems, const gbba_options* options,
                                gbba_summary* summaries);
 
+/* Autotuner of the atomic-free Schur build.  Its camera-pair products run one
+ * warp per work item of at most `pair_chunk` observation pairs of one
+ * camera-pair block; smaller items spread the long diagonal blocks over more
+ * warps, larger ones read fewer partial sums.  gbba_autotune runs
+ * `iterations` LM iterations of `problem` with `options` for each candidate
+ * item size, times the Schur phase on the device, and keeps the fastest in
+ * the handle for its later solves.  The problem's parameters are restored
+ * after each trial, so the call leaves them unchanged. */
+#define GBBA_TUNE_MAX_CANDIDATES 4
+typedef struct gbba_tuning {
+  int32_t pair_chunk;                                    /* chosen work-item size (pairs) */
+  int32_t num_candidates;
+  int32_t candidates[GBBA_TUNE_MAX_CANDIDATES];          /* 32, 64, 128 */
+  double schur_time_s[GBBA_TUNE_MAX_CANDIDATES];         /* Schur-phase device time per LM iteration */
+} gbba_tuning;
+gbba_status gbba_autotune(gbba_handle* handle, const gbba_problem* problem, const gbba_options* options,
+                          int32_t iterations, gbba_tuning* tuning);
+
 /* Differentiation contract, forward half: residuals r = pred - obs (not
  * robustified, [num_observations][2], may be NULL) and the robustified cost
  * 1/2 sum rho(|r|^2) (may be NULL).  Replaces ceres::Problem::Evaluate's

@@ -42,7 +42,8 @@ def test_no_device_is_reported_not_faked(gb, abi):
 
 
 def test_struct_layout_matches_c(abi):
-    fields = {"gbba_problem": abi.GbbaProblem, "gbba_options": abi.GbbaOptions, "gbba_summary": abi.GbbaSummary}
+    fields = {"gbba_problem": abi.GbbaProblem, "gbba_options": abi.GbbaOptions, "gbba_summary": abi.GbbaSummary,
+              "gbba_tuning": abi.GbbaTuning}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbba.h"', "int main(void){"]
     for cname, cls in fields.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')

@@ -201,6 +201,35 @@ def test_atomic_free_schur_matches_atomic_path(handle, abi, scenes, monkeypatch)
     np.testing.assert_allclose(p_pair["points"], p_atom["points"], atol=1e-8)
 
 
+def test_autotune_keeps_the_fastest_work_item_size(gb, abi, scenes):
+    """gbba_autotune times the Schur phase for each pair work-item size, keeps
+    the fastest in the handle and leaves the problem's parameters unchanged;
+    a solve with the tuned size reaches the default size's final cost."""
+    sc = scenes.medium_scene(num_cameras=40, num_points=3000, seed=131)
+    sc["camera_constant"][1] = 1
+    opts = scenes.ba_options_for(sc, max_num_iterations=15)
+    h = gb.Handle(0)  # its own handle: the tuned size stays with it
+    try:
+        s_ref, _ = solve(h, abi, sc, opts)
+        hp = abi.HostProblem(sc)
+        before = {k: v.copy() for k, v in hp.params().items()}
+        tun = abi.GbbaTuning()
+        p = hp.struct()
+        st = h.lib.gbba_autotune(h.h, C.byref(p), C.byref(opts), 2, C.byref(tun))
+        assert st == abi.SUCCESS
+        assert tun.num_candidates == 3 and list(tun.candidates[:3]) == [32, 64, 128]
+        times = list(tun.schur_time_s[:3])
+        assert all(t > 0 for t in times)
+        assert tun.pair_chunk == tun.candidates[times.index(min(times))]
+        for k, v in hp.params().items():
+            np.testing.assert_array_equal(v, before[k])
+        s_tuned = h.solve(hp, opts)
+        assert s_tuned.usable
+        assert abs(s_tuned.final_cost - s_ref.final_cost) <= 1e-9 * s_ref.final_cost
+    finally:
+        h.close()
+
+
 @pytest.mark.parametrize("precision", [0, 1])
 def test_cuda_graph_replay_matches_eager_launches(precision, handle, abi, scenes):
     sc = scenes.medium_scene(num_cameras=20, num_points=1000, seed=102)
