@@ -14,11 +14,15 @@
 //     in a per-CTA slice of global memory (L2-resident), accumulated with
 //     native global FP64 reductions: shared memory has no FP64 add, and an
 //     FP64 S of n = 256 would not fit it;
-//   - the camera column norms and gradient are accumulated in the same
-//     global slice (FP64 reductions);
-//   - points are processed one warp per point (V, V^-1, g_p, W, W V^-1);
-//   - the Cholesky factorisation and both triangular solves run in shared
-//     memory; the accept / reject decision is taken by thread 0.
+//   - the cost pass runs one thread per observation (FP64 residuals from the
+//     window's FP64 poses in shared memory);
+//   - the Schur build runs one warp per point (V, V^-1, g_p, W, W V^-1) and
+//     also forms the column norms and the gradient of its Jacobian (the LM
+//     diagonal and ceres's gradient check): FP64 sums in the global slice,
+//     FP32 sums in shared memory;
+//   - the Cholesky factorisation and both triangular solves run where S
+//     lives; every thread evaluates the step and takes the same accept /
+//     reject decision.
 // CTAs never wait on each other, so the launch cannot deadlock; the hardware
 // schedules the next problem onto an SM as soon as one finishes (problems are
 // ordered largest first to shorten the tail).
