@@ -91,6 +91,19 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def replicas_throughput(ms, units_per_rank, world, device="cpu"):
+    """Whole-job throughput of `world` independent replicas: every rank's
+    units over the slowest rank's time (the max over ranks, one all-reduce on
+    the process group: NCCL on the GPU machine, gloo in the CPU tests).  Returns
+    (value, max_ms)."""
+    if world > 1:
+        import torch
+        t = torch.tensor([float(ms)], device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * units_per_rank / (ms / 1e3), ms
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled during the timed region."""
 
@@ -370,12 +383,7 @@ def run_ours(args):
     barrier()
     clk = clocks.stop()
     launches = h.launches() - launches0
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * no * iters / (ms / 1e3)
+    value, ms = replicas_throughput(e0.elapsed_time(e1), no * iters, world, device=f"cuda:{local}")
     n_red = int(summ.reduced_system_size)
 
     # ---- end to end through the C ABI with pinned host buffers (e2e)
