@@ -131,8 +131,18 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.f.close()
+        with open(self.path) as f:
+            out = self.summarize(f)
+        os.unlink(self.path)
+        return out
+
+    @staticmethod
+    def summarize(lines):
+        """Median SM clock, maximum SM clock and the throttle reasons seen
+        Active in nvidia-smi rows of the query above (csv, noheader, nounits);
+        lines that do not parse are skipped.  None without a sample."""
         rows = []
-        for line in open(self.path):
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -140,7 +150,6 @@ class ClockSampler:
                 rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
             except ValueError:
                 pass
-        os.unlink(self.path)
         if not rows:
             return None
         sm = sorted(r[0] for r in rows)
