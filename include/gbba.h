@@ -193,7 +193,8 @@ gbba_status gbba_solve_batched(gbba_handle* handle, const gbba_problem* problems
                                int32_t num_problems, const gbba_options* options,
                                gbba_summary* summaries);
 
-/* Autotuner of the atomic-free Schur build.  Its camera-pair products run one
+/* Autotuner of the atomic-free Schur build (no counterpart in the reference,
+ * whose ceres solve has no tunable kernels).  Its camera-pair products run one
  * warp per work item of at most `pair_chunk` observation pairs of one
  * camera-pair block; smaller items spread the long diagonal blocks over more
  * warps, larger ones read fewer partial sums.  gbba_autotune runs
