@@ -31,6 +31,8 @@ LOSS_HUBER = 1
 SOLVER_AUTO = 0
 SOLVER_DENSE_SCHUR = 1
 SOLVER_ITERATIVE_SCHUR = 2
+SCHUR_BUILD_AUTO = 0
+SCHUR_BUILD_POINT_ATOMIC = 1
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
@@ -101,7 +103,7 @@ class GbbaOptions(C.Structure):
         ("use_cuda_graphs", C.c_int32),
         ("stream", C.c_void_p),
         ("fp64_polish_iterations", C.c_int32),
-        ("reserved", C.c_int32),
+        ("schur_build", C.c_int32),
     ]
 
 
@@ -168,7 +170,7 @@ def default_options(**kw):
     o.use_cuda_graphs = 1
     o.stream = None
     o.fp64_polish_iterations = 10
-    o.reserved = 0
+    o.schur_build = 0
     for k, v in kw.items():
         if not hasattr(o, k):
             raise AttributeError(k)

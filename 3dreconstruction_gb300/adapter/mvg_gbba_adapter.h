@@ -16,6 +16,7 @@
 #define MVG_GBBA_ADAPTER_H_
 
 #include <cstdint>
+#include <cstdio>
 #include <vector>
 
 #include "../../include/gbba.h"
@@ -30,6 +31,13 @@ inline gbba_handle* ThreadHandle() {
   return h;
 }
 inline std::vector<uint32_t> Narrow(const std::vector<size_t>& v) { return std::vector<uint32_t>(v.begin(), v.end()); }
+// The reference's triangulation functions return nothing; when the GPU call
+// fails the adapter leaves the caller's output untouched and says why here.
+inline bool Report(gbba_status st, const char* what) {
+  if (st == GBBA_SUCCESS) return true;
+  std::fprintf(stderr, "mvg gpu %s: %s (output left unchanged)\n", what, gbba_status_string(st));
+  return false;
+}
 }  // namespace gbba_detail
 
 namespace sfm {
@@ -149,7 +157,9 @@ void TriangulateDLT(const Mat34& P1, const Vec2& x1, const Mat34& P2, const Vec2
       a[4 * r + c] = P1(r, c);
       b[4 * r + c] = P2(r, c);
     }
-  gbtri_dlt2_batched(mvg::gbba_detail::ThreadHandle(), 1, a, b, 12, u, v, X, nullptr, GBBA_MEMORY_HOST);
+  gbba_handle* h = mvg::gbba_detail::ThreadHandle();
+  const gbba_status st = h ? gbtri_dlt2_batched(h, 1, a, b, 12, u, v, X, nullptr, GBBA_MEMORY_HOST) : GBBA_ERROR_NO_DEVICE;
+  if (!mvg::gbba_detail::Report(st, "TriangulateDLT")) return;
   for (int i = 0; i < 4; ++i) (*X_homogeneous)(i) = X[i];
 }
 
@@ -168,8 +178,11 @@ void TriangulateNView(const Mat2X& x, const std::vector<Mat34>& Ps, Vec4* X) {
   }
   const int64_t off[2] = {0, n};
   double out[4];
-  gbtri_nview_batched(mvg::gbba_detail::ThreadHandle(), GBTRI_NVIEW, P.data(), n, off, cam.data(), xy.data(), 1, out,
-                      nullptr, GBBA_MEMORY_HOST);
+  gbba_handle* h = mvg::gbba_detail::ThreadHandle();
+  const gbba_status st = h ? gbtri_nview_batched(h, GBTRI_NVIEW, P.data(), n, off, cam.data(), xy.data(), 1, out,
+                                                 nullptr, GBBA_MEMORY_HOST)
+                           : GBBA_ERROR_NO_DEVICE;
+  if (!mvg::gbba_detail::Report(st, "TriangulateNView")) return;
   for (int i = 0; i < 4; ++i) (*X)(i) = out[i];
 }
 

@@ -217,7 +217,7 @@ void gbba_default_options(gbba_options* o) {
   o->use_cuda_graphs = 1;
   o->stream = nullptr;
   o->fp64_polish_iterations = 10;
-  o->reserved = 0;
+  o->schur_build = GBBA_SCHUR_BUILD_AUTO;
 }
 
 gbba_status gbba_create(int device, gbba_handle** out) {

@@ -589,20 +589,20 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64
   if (tid < NB) b[(int64_t)jb * NB + tid] -= part[tid] + part[NB + tid] + part[2 * NB + tid] + part[3 * NB + tid];
 }
 
-// Opt the kernels into their dynamic shared memory (once per process and
-// type; called before any stream capture).
+// Opt the kernels into their dynamic shared memory (once per device and type;
+// called before any stream capture).
 template <typename T>
 void dense_cholesky_prepare() {
-  static bool configured = false;
-  if (configured) return;
-  const int sm = (int)dense_smem_bytes<T>();
-  GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)potrf_smem_bytes<T>()));
-  GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-  GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-  GBBA_CUDA(cudaFuncSetAttribute(k_syrk_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)wide_smem_bytes<T>()));
-  configured = true;
+  static PerDeviceOnce once;
+  once.run([] {
+    const int sm = (int)dense_smem_bytes<T>();
+    GBBA_CUDA(cudaFuncSetAttribute(k_potrf_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)potrf_smem_bytes<T>()));
+    GBBA_CUDA(cudaFuncSetAttribute(k_trsm_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    GBBA_CUDA(cudaFuncSetAttribute(k_syrk_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)wide_smem_bytes<T>()));
+  });
 }
 
 // Launch on the panel chain at the device's greatest stream priority (the

@@ -6,6 +6,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -35,6 +36,24 @@ struct Error {
   do {                                                 \
     if (!(cond)) throw ::gbba::Error{(st), (msg)};     \
   } while (0)
+
+// Per-process set-up that belongs to a device (kernel attributes such as the
+// opt-in to more than 48 KB of dynamic shared memory): `configure` runs with
+// the current device, under a lock, at most once per device, and only a
+// success is remembered, so a failed set-up is tried again by the next call.
+struct PerDeviceOnce {
+  std::mutex lock;
+  uint64_t done = 0;  // bit d: device d is configured
+  template <typename F>
+  void run(F&& configure) {
+    int dev = 0;
+    GBBA_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> guard(lock);
+    if (dev < 64 && ((done >> dev) & 1u)) return;
+    configure();  // throws gbba::Error on failure
+    if (dev < 64) done |= uint64_t(1) << dev;
+  }
+};
 
 // A device arena: one growable allocation carved by a bump pointer.  Solves
 // reuse it across calls, so the steady state makes no cudaMalloc.

@@ -31,20 +31,30 @@ constexpr int kThreads = 256;
 static __device__ __align__(256) double g_noalloc_scratch[kBlocks + 32];
 
 struct DeviceScratch {
-  std::once_flag once;
+  std::mutex lock;
   double* addr = nullptr;
-  cudaError_t err = cudaSuccess;
 };
 constexpr int kMaxDevices = 64;
 DeviceScratch g_device_scratch[kMaxDevices];
 
-// Device address of the scratch array on the current device (set-up runs once
-// per device, with that device current).
+// Device address of the scratch array on the current device.  The lookup runs
+// with that device current and only a success is kept: after a failed lookup
+// (a context that is not ready yet, a module that failed to load) the next
+// call on that device tries again.
 cudaError_t scratch_address(int device, double** out) {
   DeviceScratch& d = g_device_scratch[device];
-  std::call_once(d.once, [&d]() { d.err = cudaGetSymbolAddress((void**)&d.addr, g_noalloc_scratch); });
+  std::lock_guard<std::mutex> guard(d.lock);
+  if (!d.addr) {
+    double* addr = nullptr;
+    const cudaError_t err = cudaGetSymbolAddress((void**)&addr, g_noalloc_scratch);
+    if (err != cudaSuccess || !addr) {
+      *out = nullptr;
+      return err != cudaSuccess ? err : cudaErrorInvalidSymbol;
+    }
+    d.addr = addr;
+  }
   *out = d.addr;
-  return d.err;
+  return cudaSuccess;
 }
 
 // Block b reduces observations [b*kObsPerBlock, (b+1)*kObsPerBlock) into
@@ -123,6 +133,10 @@ extern "C" gbba_status gbba_project_forward_noalloc(const gbba_problem* P, int32
   if (P->num_observations > 0 && (!P->observations || !P->camera_index || !P->intrinsic_index || !P->point_index ||
                                   !P->extrinsics || !P->intrinsics || !P->points))
     return GBBA_ERROR_INVALID_ARGUMENT;
+  // An error that earlier work of the caller left pending on this thread is
+  // not ours to clear or to report as this call's failure: leave it visible
+  // to the caller and do nothing.
+  if (cudaPeekAtLastError() != cudaSuccess) return GBBA_ERROR_CUDA;
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess || device < 0 || device >= kMaxDevices) {
     cudaGetLastError();

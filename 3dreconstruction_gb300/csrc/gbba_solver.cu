@@ -1777,6 +1777,7 @@ struct Solve {
   int32_t* cam_group = nullptr;
   void* rec = nullptr;
   bool dense = true;
+  int schur_build = GBBA_SCHUR_BUILD_AUTO;  // gbba_options::schur_build
   // iterative Schur (PCG) state
   double *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr, *pcg_b = nullptr;
   double *pcg_y = nullptr, *pcg_minv = nullptr, *pcg_part = nullptr;
@@ -1906,6 +1907,7 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   s.np = P->num_points;
   s.no = P->num_observations;
   s.precision = o->precision;
+  s.schur_build = o->schur_build;
   const int64_t no = s.no, np = s.np, nc = s.nc, ni = s.ni;
   cudaStream_t st = s.st;
   std::vector<uint8_t> cc(nc, 0), ic(ni, 0);
@@ -2045,7 +2047,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
   s.pair_path = false;
   const int64_t nc = s.nc, ni = s.ni, np = s.np, no = s.no;
   const bool want_pairs = s.dense;
-  if ((std::getenv("GBBA_NO_PAIR_PATH") && s.dense) || nc > 0x7fffffffLL || no > 0x7fffffffLL ||
+  if ((s.schur_build == GBBA_SCHUR_BUILD_POINT_ATOMIC && s.dense) || nc > 0x7fffffffLL || no > 0x7fffffffLL ||
       (want_pairs && (nc > 8192 || nc * nc > (int64_t)1 << 26))) {
     setup_atomic_path(h, s, tsize);
     return;

@@ -586,11 +586,8 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
           dP, doff, dcam, dxy, num_tracks, dX, derr);
     } else {
       const size_t smem = sizeof(double) * ((size_t)3 * kMaxViews * (4 + kMaxViews) + (4 + kMaxViews) * (4 + kMaxViews) + 64);
-      static bool configured = false;
-      if (!configured) {
-        GBBA_CUDA(cudaFuncSetAttribute(k_nview64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        configured = true;
-      }
+      static PerDeviceOnce once;
+      once.run([&] { GBBA_CUDA(cudaFuncSetAttribute(k_nview64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); });
       k_nview64<<<(unsigned)std::min<int64_t>(num_tracks, (int64_t)h->sm_count * 32), 32, smem, h->active>>>(
           method, dP, doff, dcam, dxy, num_tracks, dX);
     }
@@ -624,11 +621,10 @@ gbba_status gbtri_nview_batched_f32(gbba_handle* h, const float* P, int64_t num_
     float* dmd = out_view(h, min_depth, num_tracks, memory);
     check_cams(h, dcam, no, num_cameras);
     const size_t smem = tri_f32_smem(num_cameras);
-    static bool configured = false;
-    if (!configured) {
+    static PerDeviceOnce once;
+    once.run([] {
       GBBA_CUDA(cudaFuncSetAttribute(k_tri_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tri_f32_smem(kTriCams)));
-      configured = true;
-    }
+    });
     k_tri_f32<<<(unsigned)ceil_div(num_tracks, kTriThreads), kTriThreads, smem, h->active>>>(
         dP, num_cameras, doff, dcam, reinterpret_cast<const float2*>(dxy), num_tracks, gn_steps, dX, dst, dmd);
     check_launch(h);

@@ -82,6 +82,16 @@ typedef enum gbba_precision {
   GBBA_PRECISION_MIXED = 1  /* FP32 Jacobians / Schur build / factor, FP64 cost and refinement */
 } gbba_precision;
 
+/* How the dense path builds S.  AUTO takes the atomic-free camera-pair build
+ * whenever every free intrinsic block belongs to one camera (S then splits
+ * into camera-pair blocks) and the point-major build with atomic additions
+ * otherwise; POINT_ATOMIC forces the latter (both give the same S up to the
+ * order of the sums). */
+typedef enum gbba_schur_build {
+  GBBA_SCHUR_BUILD_AUTO = 0,
+  GBBA_SCHUR_BUILD_POINT_ATOMIC = 1
+} gbba_schur_build;
+
 typedef enum gbba_memory {
   GBBA_MEMORY_HOST = 0,   /* arrays are host pointers; copies are done by the call */
   GBBA_MEMORY_DEVICE = 1  /* arrays are device pointers on the handle's device */
@@ -143,7 +153,7 @@ typedef struct gbba_options {
   int32_t fp64_polish_iterations;         /* mixed path: after it stops, at most this many plain-FP64
                                              LM iterations continue from its solution with function and
                                              parameter tolerances 1000x tighter (0 = off): 10 */
-  int32_t reserved;
+  int32_t schur_build;                    /* gbba_schur_build: GBBA_SCHUR_BUILD_AUTO */
 } gbba_options;
 
 typedef struct gbba_summary {
@@ -246,10 +256,14 @@ gbba_status gbba_project_backward(gbba_handle* handle, const gbba_problem* probl
  * partial sums, ~128 KB held by every GPU that loads the library until exit):
  * problems above GBBA_NOALLOC_MAX_BLOCKS * GBBA_NOALLOC_OBS_PER_BLOCK
  * observations (33,554,432) are rejected with GBBA_ERROR_TOO_LARGE.  The first
- * call on each device looks up the scratch's device address; make that first
- * call before any stream capture.  All calls share the scratch: calls that
- * overlap on the GPU race.  An out-of-range index yields NaN residuals and a
- * NaN cost instead of a fault. */
+ * call on each device looks up the scratch's device address (a failed lookup
+ * is retried by the next call); make that first call before any stream
+ * capture.  All calls share the scratch: calls that overlap on the GPU race.
+ * An out-of-range index yields NaN residuals for its observation and a NaN
+ * cost instead of a fault; the next valid call is unaffected.  If a CUDA error
+ * from the caller's earlier work is already pending on the calling thread, the
+ * call does nothing and returns GBBA_ERROR_CUDA, leaving that error pending
+ * (cudaPeekAtLastError / cudaGetLastError still report it to the caller). */
 #define GBBA_NOALLOC_MAX_BLOCKS 16384
 #define GBBA_NOALLOC_OBS_PER_BLOCK 2048
 gbba_status gbba_project_forward_noalloc(const gbba_problem* problem, int32_t loss_type, double loss_scale,

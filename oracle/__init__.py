@@ -16,6 +16,19 @@ REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 _lib = None
 
 
+def reference_dir():
+    """Root of the reference's sources, from GBBA_REFERENCE_DIR (the same
+    variable the oracle Makefile reads), or None when they are not present."""
+    d = os.environ.get("GBBA_REFERENCE_DIR") or _default_reference_dir()
+    return d if os.path.isdir(d) else None
+
+
+def _default_reference_dir():
+    # the Makefile's default; the only place besides it that names the path
+    out = subprocess.run(["make", "-s", "-C", HERE, "print-ref"], capture_output=True, text=True)
+    return out.stdout.strip() if out.returncode == 0 else ""
+
+
 def _abi():
     return importlib.import_module("3dreconstruction_gb300.abi")
 

@@ -9,7 +9,9 @@ import pytest
 
 from conftest import ROOT
 
-REF = "/root/reference"
+import oracle
+
+REF = oracle.reference_dir() or ""
 GEN = os.path.join(ROOT, "oracle", "_ref", "gen")
 
 SRC = r'''

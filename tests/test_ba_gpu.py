@@ -187,14 +187,14 @@ def test_empty_and_all_constant_cameras(handle, abi, scenes):
     assert s.initial_cost == 0.0 and s.usable
 
 
-def test_atomic_free_schur_matches_atomic_path(handle, abi, scenes, monkeypatch):
+def test_atomic_free_schur_matches_atomic_path(handle, abi, scenes):
     """The camera-pair (segmented, atomic-free) Schur build and the point-major
     atomic build give the same solve (FP64, well-posed scene)."""
     sc = scenes.medium_scene(num_cameras=25, num_points=1500, seed=101)
     sc["camera_constant"][1] = 1
     opts = scenes.ba_options_for(sc, max_num_iterations=15)
     s_pair, p_pair = solve(handle, abi, sc, opts)
-    monkeypatch.setenv("GBBA_NO_PAIR_PATH", "1")
+    opts.schur_build = abi.SCHUR_BUILD_POINT_ATOMIC
     s_atom, p_atom = solve(handle, abi, sc, opts)
     assert s_pair.num_iterations == s_atom.num_iterations
     assert abs(s_pair.final_cost - s_atom.final_cost) <= 1e-10 * s_atom.final_cost

@@ -65,3 +65,35 @@ def test_noalloc_rejects_oversized_and_host_problems(abi):
     p.memory = abi.MEMORY_HOST
     p.num_observations = 10
     assert lib.gbba_project_forward_noalloc(C.byref(p), 0, 1.0, None, None, None) == abi.ERROR_INVALID_ARGUMENT
+
+
+def test_noalloc_out_of_range_index_gives_nan_then_recovers(handle, abi, scenes):
+    """An observation whose point index is out of range gets NaN residuals and
+    makes the cost NaN (the kernel checks every index before it reads); the
+    next valid call clears the error slot and matches gbba_project_forward."""
+    torch = pytest.importorskip("torch")
+    lib = handle.lib
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    sc = scenes.medium_scene(num_cameras=10, num_points=300, seed=93)
+    ref_res, ref_cost = allocating_forward(handle, abi, sc, abi.LOSS_HUBER, 4.0)
+    bad = dict(sc)
+    bad["point_index"] = sc["point_index"].copy()
+    bad["point_index"][7] = len(sc["points"]) + 5
+    no = len(sc["observations"])
+    for scene, expect_nan in ((bad, True), (sc, False)):
+        dp = abi.DeviceProblem(scene)
+        p = dp.struct()
+        res = torch.full((no, 2), -1.0, dtype=torch.float64, device="cuda")
+        cost = torch.full((1,), -1.0, dtype=torch.float64, device="cuda")
+        st = lib.gbba_project_forward_noalloc(C.byref(p), abi.LOSS_HUBER, 4.0, res.data_ptr(), cost.data_ptr(), stream)
+        assert st == abi.SUCCESS
+        torch.cuda.synchronize()
+        r = res.cpu().numpy()
+        if expect_nan:
+            assert np.isnan(r[7]).all() and np.isnan(cost.item())
+            ok = np.ones(no, bool)
+            ok[7] = False
+            np.testing.assert_array_equal(r[ok], ref_res[ok])
+        else:
+            np.testing.assert_array_equal(r, ref_res)
+            assert np.isfinite(cost.item()) and abs(cost.item() - ref_cost) <= 1e-12 * ref_cost
