@@ -299,13 +299,16 @@ def declare_gbba(lib):
     lib.gbba_project_forward.restype = C.c_int
     lib.gbba_project_backward.argtypes = [vp, P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp, vp]
     lib.gbba_project_backward.restype = C.c_int
+    lib.gbba_project_backward_mixed.argtypes = [vp, P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp, vp]
+    lib.gbba_project_backward_mixed.restype = C.c_int
     lib.gbba_project_forward_noalloc.argtypes = [P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp]
     lib.gbba_project_forward_noalloc.restype = C.c_int
     lib.gbtri_dlt2_batched.argtypes = [vp, C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     lib.gbtri_dlt2_batched.restype = C.c_int
     lib.gbtri_nview_batched.argtypes = [vp, C.c_int32, vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp, C.c_int32]
     lib.gbtri_nview_batched.restype = C.c_int
-    lib.gbtri_nview_batched_f32.argtypes = [vp, vp, C.c_int64, vp, vp, vp, C.c_int64, C.c_int32, vp, vp, vp, C.c_int32]
+    lib.gbtri_nview_batched_f32.argtypes = [vp, C.c_int32, vp, C.c_int64, vp, vp, vp, C.c_int64, C.c_int32, vp, vp, vp,
+                                            C.c_int32]
     lib.gbtri_nview_batched_f32.restype = C.c_int
     lib.gbtri_refine_gn.argtypes = [vp, vp, C.c_int64, vp, vp, vp, C.c_int64, C.c_int32, vp, C.c_int32]
     lib.gbtri_refine_gn.restype = C.c_int
@@ -316,6 +319,6 @@ def declare_gbba(lib):
 EXPORTED_SYMBOLS = (
     "gbba_create", "gbba_destroy", "gbba_default_options", "gbba_status_string",
     "gbba_abi_version", "gbba_launch_count", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
-    "gbba_project_forward", "gbba_project_backward", "gbba_project_forward_noalloc",
+    "gbba_project_forward", "gbba_project_backward", "gbba_project_backward_mixed", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
 )

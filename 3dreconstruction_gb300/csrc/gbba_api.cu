@@ -80,41 +80,60 @@ __global__ void __launch_bounds__(256) k_forward(const double* ext, const double
   }
 }
 
-template <int M>
+// Jacobian blocks and gradient of the robustified residual.  T = double is
+// the plain FP64 path.  T = float is the Jacobian the mixed solve uses inside
+// its Schur build (obs_jacobian<M, float, ...> in gbba_solver.cu): the FP32
+// instantiation of the same hand-written adjoint, evaluated at FP32 copies of
+// the parameters and observation, with the residual and the Corrector scale
+// sqrt(rho') taken in FP64; the blocks are written widened to FP64.
+template <int M, typename T>
 __global__ void __launch_bounds__(256) k_backward(const double* ext, const double* intr, const double* pts,
                                                   const double* obs, const uint32_t* cam, const uint32_t* icam,
                                                   const uint32_t* pt, int64_t no, int64_t nc, int64_t ni, int loss_type,
                                                   double a, double* je, double* jk, double* jx, double* grad) {
   constexpr int K = Model<M>::K;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < no; o += (int64_t)gridDim.x * blockDim.x) {
-    double E[6], Kp[K], X[3], r[2], Je[2][6], Jk[2][K], Jx[2][3];
+    double E[6], Kp[K], X[3], r[2];
+    T Je[2][6], Jk[2][K], Jx[2][3];
     const uint32_t c = cam[o], g = icam[o], p = pt[o];
     for (int i = 0; i < 6; ++i) E[i] = ext[6 * (int64_t)c + i];
     for (int i = 0; i < K; ++i) Kp[i] = intr[K * (int64_t)g + i];
     for (int i = 0; i < 3; ++i) X[i] = pts[3 * (int64_t)p + i];
-    residual<M, double, true>(Kp, E, X, obs[2 * o], obs[2 * o + 1], r, Je, Jk, Jx, (double*)nullptr);
+    if constexpr (sizeof(T) == 8) {
+      residual<M, double, true>(Kp, E, X, obs[2 * o], obs[2 * o + 1], r, Je, Jk, Jx, (double*)nullptr);
+    } else {
+      double dJe[2][6], dJk[2][K], dJx[2][3];
+      residual<M, double, false>(Kp, E, X, obs[2 * o], obs[2 * o + 1], r, dJe, dJk, dJx, (double*)nullptr);
+      T Ef[6], Kf[K], Xf[3], rf[2];
+      for (int i = 0; i < 6; ++i) Ef[i] = (T)E[i];
+      for (int i = 0; i < K; ++i) Kf[i] = (T)Kp[i];
+      for (int i = 0; i < 3; ++i) Xf[i] = (T)X[i];
+      residual<M, T, true>(Kf, Ef, Xf, (T)obs[2 * o], (T)obs[2 * o + 1], rf, Je, Jk, Jx, (T*)nullptr);
+    }
     double sr1;
     robust<double>(loss_type, a, r[0] * r[0] + r[1] * r[1], &sr1);
     const double rc0 = r[0] * sr1, rc1 = r[1] * sr1;
+    const T s = (T)sr1;
     for (int i = 0; i < 2; ++i) {
       for (int j = 0; j < 6; ++j) {
-        Je[i][j] *= sr1;
-        if (je) je[(o * 2 + i) * 6 + j] = Je[i][j];
+        Je[i][j] *= s;
+        if (je) je[(o * 2 + i) * 6 + j] = (double)Je[i][j];
       }
       for (int j = 0; j < K; ++j) {
-        Jk[i][j] *= sr1;
-        if (jk) jk[(o * 2 + i) * K + j] = Jk[i][j];
+        Jk[i][j] *= s;
+        if (jk) jk[(o * 2 + i) * K + j] = (double)Jk[i][j];
       }
       for (int j = 0; j < 3; ++j) {
-        Jx[i][j] *= sr1;
-        if (jx) jx[(o * 2 + i) * 3 + j] = Jx[i][j];
+        Jx[i][j] *= s;
+        if (jx) jx[(o * 2 + i) * 3 + j] = (double)Jx[i][j];
       }
     }
     if (grad) {
-      for (int j = 0; j < 6; ++j) atomicAdd(&grad[6 * (int64_t)c + j], Je[0][j] * rc0 + Je[1][j] * rc1);
-      for (int j = 0; j < K; ++j) atomicAdd(&grad[6 * nc + K * (int64_t)g + j], Jk[0][j] * rc0 + Jk[1][j] * rc1);
+      for (int j = 0; j < 6; ++j) atomicAdd(&grad[6 * (int64_t)c + j], (double)Je[0][j] * rc0 + (double)Je[1][j] * rc1);
+      for (int j = 0; j < K; ++j)
+        atomicAdd(&grad[6 * nc + K * (int64_t)g + j], (double)Jk[0][j] * rc0 + (double)Jk[1][j] * rc1);
       for (int j = 0; j < 3; ++j)
-        atomicAdd(&grad[6 * nc + K * ni + 3 * (int64_t)p + j], Jx[0][j] * rc0 + Jx[1][j] * rc1);
+        atomicAdd(&grad[6 * nc + K * ni + 3 * (int64_t)p + j], (double)Jx[0][j] * rc0 + (double)Jx[1][j] * rc1);
     }
   }
 }
@@ -389,8 +408,9 @@ gbba_status gbba_project_forward(gbba_handle* h, const gbba_problem* P, int32_t 
   });
 }
 
-gbba_status gbba_project_backward(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,
-                                  double* jac_extrinsic, double* jac_intrinsic, double* jac_point, double* gradient) {
+static gbba_status project_backward(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,
+                                    bool fp32, double* jac_extrinsic, double* jac_intrinsic, double* jac_point,
+                                    double* gradient) {
   const gbba_status pc = check_problem(P);
   if (pc != GBBA_SUCCESS) return pc;
   return guarded(h, nullptr, [&]() {
@@ -410,10 +430,14 @@ gbba_status gbba_project_backward(gbba_handle* h, const gbba_problem* P, int32_t
     cudaStream_t st = h->active;
     if (dg) GBBA_CUDA(cudaMemsetAsync(dg, 0, bg, st));
     const int grid = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(no, 1), 256), h->sm_count * 8));
+    auto run = [&](auto kern) {
+      kern<<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type, loss_scale,
+                                 dje, djk, djx, dg);
+    };
     switch (P->camera_model) {
-      case kPinholeF: k_backward<kPinholeF><<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type, loss_scale, dje, djk, djx, dg); break;
-      case kRadialK3: k_backward<kRadialK3><<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type, loss_scale, dje, djk, djx, dg); break;
-      default: k_backward<kBrownT2><<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type, loss_scale, dje, djk, djx, dg); break;
+      case kPinholeF: fp32 ? run(k_backward<kPinholeF, float>) : run(k_backward<kPinholeF, double>); break;
+      case kRadialK3: fp32 ? run(k_backward<kRadialK3, float>) : run(k_backward<kRadialK3, double>); break;
+      default: fp32 ? run(k_backward<kBrownT2, float>) : run(k_backward<kBrownT2, double>); break;
     }
     check_launch(h);
     const cudaMemcpyKind kind = P->memory == GBBA_MEMORY_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
@@ -424,6 +448,17 @@ gbba_status gbba_project_backward(gbba_handle* h, const gbba_problem* P, int32_t
     GBBA_CUDA(cudaStreamSynchronize(st));
     return GBBA_SUCCESS;
   });
+}
+
+gbba_status gbba_project_backward(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,
+                                  double* jac_extrinsic, double* jac_intrinsic, double* jac_point, double* gradient) {
+  return project_backward(h, P, loss_type, loss_scale, false, jac_extrinsic, jac_intrinsic, jac_point, gradient);
+}
+
+gbba_status gbba_project_backward_mixed(gbba_handle* h, const gbba_problem* P, int32_t loss_type, double loss_scale,
+                                        double* jac_extrinsic, double* jac_intrinsic, double* jac_point,
+                                        double* gradient) {
+  return project_backward(h, P, loss_type, loss_scale, true, jac_extrinsic, jac_intrinsic, jac_point, gradient);
 }
 
 }  // extern "C"

@@ -10,13 +10,16 @@
 // (Hestenes) Jacobi: rotations orthogonalise the columns, V accumulates them,
 // and the column of smallest norm gives the singular vector.
 //
-// FP32 production path: per track, the reference's linear system of
-// Triangulation::compute with unit weights, then Gauss-Newton steps on the
-// reprojection error; the block's observations are staged in shared memory
-// with coalesced loads and the camera table lives in shared memory.
+// The N-view and algebraic nullspaces are computed without forming the
+// 3n x (4+n) design: see nview_track below.  The same templated code runs in
+// FP64 (parity path) and in FP32 (production path, followed by Gauss-Newton
+// steps on the reprojection error; the block's observations are staged in
+// shared memory with coalesced loads and the camera table lives in shared
+// memory).
 #include <cstring>
 
 #include "gbba_internal.h"
+#include "gbtri_track.cuh"
 
 namespace gbba {
 
@@ -81,205 +84,7 @@ __global__ void k_dlt2(int64_t n, const double* P1, const double* P2, int64_t ps
   }
 }
 
-// ------------------------------------------------- FP64 N-view / algebraic (warp per track)
-// A is column-major in shared memory: column c at A + c * ldr, ldr >= rows.
-__device__ void warp_jacobi_nullspace(double* A, int ldr, int m, int n, double* V, double* x) {
-  const int lane = threadIdx.x & 31;
-  for (int idx = lane; idx < n * n; idx += 32) V[idx] = (idx / n == idx % n) ? 1.0 : 0.0;  // V column-major n x n
-  __syncwarp();
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    bool rotated = false;
-    for (int i = 0; i < n - 1; ++i)
-      for (int j = i + 1; j < n; ++j) {
-        double a = 0, b = 0, g = 0;
-        const double* ci = A + (size_t)i * ldr;
-        const double* cj = A + (size_t)j * ldr;
-        for (int r = lane; r < m; r += 32) {
-          a += ci[r] * ci[r];
-          b += cj[r] * cj[r];
-          g += ci[r] * cj[r];
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          a += __shfl_xor_sync(0xffffffffu, a, o);
-          b += __shfl_xor_sync(0xffffffffu, b, o);
-          g += __shfl_xor_sync(0xffffffffu, g, o);
-        }
-        if (g == 0.0 || fabs(g) <= 1e-15 * sqrt(a * b)) continue;
-        rotated = true;
-        const double zeta = (b - a) / (2.0 * g);
-        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-        double* wi = A + (size_t)i * ldr;
-        double* wj = A + (size_t)j * ldr;
-        for (int r = lane; r < m; r += 32) {
-          const double ui = wi[r], uj = wj[r];
-          wi[r] = c * ui - s * uj;
-          wj[r] = s * ui + c * uj;
-        }
-        double* vi = V + (size_t)i * n;
-        double* vj = V + (size_t)j * n;
-        for (int r = lane; r < n; r += 32) {
-          const double a0 = vi[r], a1 = vj[r];
-          vi[r] = c * a0 - s * a1;
-          vj[r] = s * a0 + c * a1;
-        }
-        __syncwarp();
-      }
-    if (!rotated) break;
-  }
-  // column of smallest norm
-  double bn = 1e300;
-  int best = 0;
-  for (int c = 0; c < n; ++c) {
-    double s = 0;
-    for (int r = lane; r < m; r += 32) s += A[(size_t)c * ldr + r] * A[(size_t)c * ldr + r];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (s < bn) {
-      bn = s;
-      best = c;
-    }
-  }
-  for (int r = lane; r < n; r += 32) x[r] = V[(size_t)best * n + r];
-  __syncwarp();
-}
-
-constexpr int kMaxViews = 32;  // GBTRI_NVIEW limit per track (3*32 rows x 36 columns)
-
-__global__ void __launch_bounds__(32) k_nview64(int method, const double* P, const int64_t* offs, const uint32_t* cam,
-                                                const double* xy, int64_t nt, double* X) {
-  extern __shared__ double sm[];
-  const int lane = threadIdx.x;
-  for (int64_t t = blockIdx.x; t < nt; t += gridDim.x) {
-    const int64_t b = offs[t];
-    const int n = (int)(offs[t + 1] - b);
-    double* A;
-    int m, nc, ldr;
-    if (method == 0) {
-      m = 3 * n;
-      nc = 4 + n;
-      ldr = 3 * kMaxViews;
-    } else {
-      m = 2 * n;
-      nc = 4;
-      ldr = 3 * kMaxViews;
-    }
-    A = sm;
-    double* V = sm + (size_t)ldr * (4 + kMaxViews);
-    double* x = V + (size_t)(4 + kMaxViews) * (4 + kMaxViews);
-    for (int idx = lane; idx < ldr * nc; idx += 32) A[idx] = 0.0;
-    __syncwarp();
-    for (int i = lane; i < n; i += 32) {
-      const double* Pi = P + 12 * (int64_t)cam[b + i];
-      const double px = xy[2 * (b + i)], py = xy[2 * (b + i) + 1];
-      if (method == 0) {  // [-P_i | x~_i e_i]
-        for (int r = 0; r < 3; ++r)
-          for (int c = 0; c < 4; ++c) A[(size_t)c * ldr + 3 * i + r] = -Pi[4 * r + c];
-        A[(size_t)(4 + i) * ldr + 3 * i + 0] = px;
-        A[(size_t)(4 + i) * ldr + 3 * i + 1] = py;
-        A[(size_t)(4 + i) * ldr + 3 * i + 2] = 1.0;
-      } else {  // rows [0,-1,y] P and [1,0,-x] P
-        for (int c = 0; c < 4; ++c) {
-          A[(size_t)c * ldr + 2 * i] = -Pi[4 + c] + py * Pi[8 + c];
-          A[(size_t)c * ldr + 2 * i + 1] = Pi[c] - px * Pi[8 + c];
-        }
-      }
-    }
-    __syncwarp();
-    warp_jacobi_nullspace(A, ldr, m, nc, V, x);
-    if (lane < 4) X[4 * t + lane] = x[lane];
-    __syncwarp();
-  }
-}
-
-// ------------------------------------------------------- FP64 iterated linear (thread per track)
-__device__ bool inv3(const double A[9], double Ai[9]) {
-  const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
-  const double det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-  if (!(fabs(det) > 0) || !isfinite(det)) return false;
-  const double id = 1.0 / det;
-  Ai[0] = c00 * id;
-  Ai[1] = (A[2] * A[7] - A[1] * A[8]) * id;
-  Ai[2] = (A[1] * A[5] - A[2] * A[4]) * id;
-  Ai[3] = c01 * id;
-  Ai[4] = (A[0] * A[8] - A[2] * A[6]) * id;
-  Ai[5] = (A[2] * A[3] - A[0] * A[5]) * id;
-  Ai[6] = c02 * id;
-  Ai[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-  Ai[8] = (A[0] * A[4] - A[1] * A[3]) * id;
-  return true;
-}
-
-__global__ void k_iterative64(const double* P, const int64_t* offs, const uint32_t* cam, const double* xy, int64_t nt,
-                              double* X, double* err) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = offs[t];
-    const int n = (int)(offs[t + 1] - b);
-    double Xc[3] = {0, 0, 0};
-    double w[kMaxViews];  // weights; tracks longer than kMaxViews reuse the last slot's rule below
-    for (int i = 0; i < kMaxViews; ++i) w[i] = 1.0;
-    for (int it = 0; it < 3; ++it) {
-      double AtA[9] = {0}, Atb[3] = {0};
-      for (int i = 0; i < n; ++i) {
-        const double* Pi = P + 12 * (int64_t)cam[b + i];
-        const double px = xy[2 * (b + i)], py = xy[2 * (b + i) + 1];
-        double wi;
-        if (it == 0) wi = 1.0;
-        else if (i < kMaxViews) wi = w[i];
-        else wi = 1.0 / (Pi[8] * Xc[0] + Pi[9] * Xc[1] + Pi[10] * Xc[2] + Pi[11]);
-        double v1[3], v2[3];
-        for (int j = 0; j < 3; ++j) {
-          v1[j] = wi * (Pi[j] - px * Pi[8 + j]);
-          v2[j] = wi * (Pi[4 + j] - py * Pi[8 + j]);
-          Atb[j] += wi * (v1[j] * (px * Pi[11] - Pi[3]) + v2[j] * (py * Pi[11] - Pi[7]));
-        }
-        for (int k = 0; k < 3; ++k)
-          for (int j = 0; j <= k; ++j) {
-            const double v = v1[j] * v1[k] + v2[j] * v2[k];
-            AtA[3 * j + k] += v;
-            if (j < k) AtA[3 * k + j] += v;
-          }
-      }
-      double Ai[9];
-      inv3(AtA, Ai);
-      for (int r = 0; r < 3; ++r) Xc[r] = Ai[3 * r] * Atb[0] + Ai[3 * r + 1] * Atb[1] + Ai[3 * r + 2] * Atb[2];
-      for (int i = 0; i < n && i < kMaxViews; ++i) {
-        const double* Pi = P + 12 * (int64_t)cam[b + i];
-        w[i] = 1.0 / (Pi[8] * Xc[0] + Pi[9] * Xc[1] + Pi[10] * Xc[2] + Pi[11]);
-      }
-    }
-    for (int r = 0; r < 3; ++r) X[3 * t + r] = Xc[r];
-    if (err) {
-      double e = 0;
-      for (int i = 0; i < n; ++i) {
-        const double* Pi = P + 12 * (int64_t)cam[b + i];
-        double h[3];
-        for (int r = 0; r < 3; ++r) h[r] = Pi[4 * r] * Xc[0] + Pi[4 * r + 1] * Xc[1] + Pi[4 * r + 2] * Xc[2] + Pi[4 * r + 3];
-        const double dx = xy[2 * (b + i)] - h[0] / h[2], dy = xy[2 * (b + i) + 1] - h[1] / h[2];
-        e += sqrt(dx * dx + dy * dy);
-      }
-      err[t] = e;
-    }
-  }
-}
-
 // ------------------------------------------------------- Gauss-Newton (templated)
-template <typename T>
-__device__ __forceinline__ bool inv3t(const T A[6], T Ai[6]) {  // symmetric packed [00,01,02,11,12,22]
-  const T c00 = A[3] * A[5] - A[4] * A[4], c01 = A[2] * A[4] - A[1] * A[5], c02 = A[1] * A[4] - A[2] * A[3];
-  const T det = A[0] * c00 + A[1] * c01 + A[2] * c02;
-  if (!(fabs((double)det) > 0) || !isfinite((double)det)) return false;
-  const T id = T(1) / det;
-  Ai[0] = c00 * id;
-  Ai[1] = c01 * id;
-  Ai[2] = c02 * id;
-  Ai[3] = (A[0] * A[5] - A[2] * A[2]) * id;
-  Ai[4] = (A[1] * A[2] - A[0] * A[4]) * id;
-  Ai[5] = (A[0] * A[3] - A[1] * A[1]) * id;
-  return true;
-}
-
 template <typename T>
 __device__ __forceinline__ void gn_accumulate(const T* Pi, const T X[3], T px, T py, T H[6], T g[3]) {
   T h[3];
@@ -328,12 +133,88 @@ __global__ void k_refine_gn64(const double* P, const int64_t* offs, const uint32
   }
 }
 
-// FP32 production kernel: 128 tracks per block, observations staged in shared memory.
+// Views of one track read straight from global memory (FP64 parity path).
+struct GlobalViews64 {
+  const double* P;
+  const uint32_t* cam;
+  const double* xy;
+  int64_t b;
+  __device__ void operator()(int j, const double** Pj, double* x, double* y) const {
+    *Pj = P + 12 * (int64_t)cam[b + j];
+    *x = xy[2 * (b + j)];
+    *y = xy[2 * (b + j) + 1];
+  }
+};
+
+// FP64 parity path, one thread per track: X [nt][4] (NVIEW / ALGEBRAIC) or
+// [nt][3] and Triangulation::error (ITERATIVE).
+__global__ void __launch_bounds__(128) k_nview64(int method, const double* __restrict__ P, const int64_t* __restrict__ offs,
+                                                 const uint32_t* __restrict__ cam, const double* __restrict__ xy,
+                                                 int64_t nt, double* __restrict__ X, double* __restrict__ err) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = offs[t];
+    const int n = (int)(offs[t + 1] - b);
+    const GlobalViews64 views{P, cam, xy, b};
+    if (method == 2) {
+      double Xc[3];
+      iterative_track<double>(views, n, Xc);
+#pragma unroll
+      for (int r = 0; r < 3; ++r) X[3 * t + r] = Xc[r];
+      if (err) {
+        // Triangulation::error: sum of the reprojection distances
+        double e = 0.0;
+        for (int i = 0; i < n; ++i) {
+          const double* Pi;
+          double px, py;
+          views(i, &Pi, &px, &py);
+          double hp[3];
+#pragma unroll
+          for (int r = 0; r < 3; ++r) hp[r] = Pi[4 * r] * Xc[0] + Pi[4 * r + 1] * Xc[1] + Pi[4 * r + 2] * Xc[2] + Pi[4 * r + 3];
+          const double dx = px - hp[0] / hp[2], dy = py - hp[1] / hp[2];
+          e += sqrt(dx * dx + dy * dy);
+        }
+        err[t] = e;
+      }
+      continue;
+    }
+    double Xh[4];
+    if (method == 0) nview_track<double>(views, n, Xh);
+    else algebraic_track<double>(views, n, Xh);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) X[4 * t + r] = Xh[r];
+  }
+}
+
+// FP32 production kernel: 128 tracks per block, a thread per track, the
+// block's observations staged in shared memory with coalesced loads and the
+// camera table in shared memory.  method: GBTRI_NVIEW (the reference's
+// TriangulateNView estimator, dehomogenised), GBTRI_NVIEW_ALGEBRAIC, or
+// GBTRI_ITERATIVE (Triangulation::compute(3)); then gn_steps Gauss-Newton
+// steps on the reprojection error.
 constexpr int kTriThreads = 128;
 constexpr int kTriStage = 4096;  // observations staged per block (12 B each)
 constexpr int kTriCams = 1024;   // camera table kept in shared memory up to this size
 
-__global__ void __launch_bounds__(kTriThreads) k_tri_f32(const float* __restrict__ P, int64_t ncam,
+struct StagedViews32 {
+  const float* sP;     // camera table in shared memory, or null
+  const float* gP;     // camera table in global memory
+  const uint32_t* scam;
+  const float2* sxy;
+  const uint32_t* gcam;
+  const float2* gxy;
+  uint32_t ob, b;
+  bool staged;
+  __device__ void operator()(int j, const float** Pj, float* x, float* y) const {
+    const uint32_t o = b + (uint32_t)j;
+    const uint32_t c = staged ? scam[o - ob] : gcam[o];
+    *Pj = sP ? sP + 12 * c : gP + 12 * (int64_t)c;
+    const float2 p = staged ? sxy[o - ob] : gxy[o];
+    *x = p.x;
+    *y = p.y;
+  }
+};
+
+__global__ void __launch_bounds__(kTriThreads) k_tri_f32(int method, const float* __restrict__ P, int64_t ncam,
                                                          const uint32_t* __restrict__ offs, const uint32_t* __restrict__ cam,
                                                          const float2* __restrict__ xy, int64_t nt, int gn_steps,
                                                          float* __restrict__ X, uint8_t* __restrict__ status,
@@ -359,47 +240,34 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_f32(const float* __restrict
   if (t >= nt) return;
   const uint32_t b = offs[t], e = offs[t + 1];
   const int n = (int)(e - b);
-  auto cam_of = [&](uint32_t o) -> const float* {
-    const uint32_t c = staged ? scam[o - ob] : cam[o];
-    return ncam_s ? sP + 12 * c : P + 12 * (int64_t)c;
-  };
-  auto xy_of = [&](uint32_t o) -> float2 { return staged ? sxy[o - ob] : xy[o]; };
+  const StagedViews32 views{ncam_s ? sP : nullptr, P, scam, sxy, cam, xy, ob, b, staged};
   float Xc[3] = {0.f, 0.f, 0.f};
   uint8_t st = n >= 2 ? 0 : 1;
   if (st == 0) {
-    float A[6] = {0, 0, 0, 0, 0, 0}, r[3] = {0, 0, 0}, Ai[6];
-    for (uint32_t o = b; o < e; ++o) {
-      const float* Pi = cam_of(o);
-      const float2 p = xy_of(o);
-      float v1[3], v2[3];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        v1[j] = Pi[j] - p.x * Pi[8 + j];
-        v2[j] = Pi[4 + j] - p.y * Pi[8 + j];
-      }
-      const float b1 = p.x * Pi[11] - Pi[3], b2 = p.y * Pi[11] - Pi[7];
-      A[0] += v1[0] * v1[0] + v2[0] * v2[0];
-      A[1] += v1[0] * v1[1] + v2[0] * v2[1];
-      A[2] += v1[0] * v1[2] + v2[0] * v2[2];
-      A[3] += v1[1] * v1[1] + v2[1] * v2[1];
-      A[4] += v1[1] * v1[2] + v2[1] * v2[2];
-      A[5] += v1[2] * v1[2] + v2[2] * v2[2];
-#pragma unroll
-      for (int j = 0; j < 3; ++j) r[j] += v1[j] * b1 + v2[j] * b2;
-    }
-    if (inv3t<float>(A, Ai)) {
-      Xc[0] = Ai[0] * r[0] + Ai[1] * r[1] + Ai[2] * r[2];
-      Xc[1] = Ai[1] * r[0] + Ai[3] * r[1] + Ai[4] * r[2];
-      Xc[2] = Ai[2] * r[0] + Ai[4] * r[1] + Ai[5] * r[2];
+    if (method == 2) {
+      if (!iterative_track<float>(views, n, Xc)) st = 1;
     } else {
-      st = 1;
+      float Xh[4];
+      if (method == 0) nview_track<float>(views, n, Xh);
+      else algebraic_track<float>(views, n, Xh);
+      const float nrm = fabsf(Xh[0]) + fabsf(Xh[1]) + fabsf(Xh[2]);
+      if (!(fabsf(Xh[3]) > 1e-6f * nrm)) {
+        st = 1;
+      } else {
+        const float iw = 1.f / Xh[3];
+        Xc[0] = Xh[0] * iw;
+        Xc[1] = Xh[1] * iw;
+        Xc[2] = Xh[2] * iw;
+      }
     }
   }
   for (int s = 0; s < gn_steps && st == 0; ++s) {
     float H[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0}, Hi[6];
-    for (uint32_t o = b; o < e; ++o) {
-      const float2 p = xy_of(o);
-      gn_accumulate<float>(cam_of(o), Xc, p.x, p.y, H, g);
+    for (int j = 0; j < n; ++j) {
+      const float* Pj;
+      float px, py;
+      views(j, &Pj, &px, &py);
+      gn_accumulate<float>(Pj, Xc, px, py, H, g);
     }
     if (!inv3t<float>(H, Hi)) {
       st = 1;
@@ -408,10 +276,13 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_f32(const float* __restrict
     gn_apply<float>(Hi, g, Xc);
   }
   float md = 3.402823466e38f;
-  for (uint32_t o = b; o < e; ++o) {
-    const float* Pi = cam_of(o);
-    md = fminf(md, Pi[8] * Xc[0] + Pi[9] * Xc[1] + Pi[10] * Xc[2] + Pi[11]);
+  for (int j = 0; j < n; ++j) {
+    const float* Pj;
+    float px, py;
+    views(j, &Pj, &px, &py);
+    md = fminf(md, Pj[8] * Xc[0] + Pj[9] * Xc[1] + Pj[10] * Xc[2] + Pj[11]);
   }
+  if (st == 0 && !(isfinite(Xc[0]) && isfinite(Xc[1]) && isfinite(Xc[2]))) st = 1;
   if (st == 0 && !(md > 0.f)) st = 2;
   X[3 * t] = Xc[0];
   X[3 * t + 1] = Xc[1];
@@ -566,10 +437,7 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
     int64_t no = 0;
     int max_len = 0;
     check_offsets(h, track_offsets, num_tracks, memory, &no, &max_len);
-    GBBA_REQUIRE(method != GBTRI_NVIEW || max_len <= kMaxViews, GBBA_ERROR_TOO_LARGE,
-                 "TriangulateNView path limited to 32 views per track");
-    GBBA_REQUIRE(method != GBTRI_NVIEW_ALGEBRAIC || max_len <= 48, GBBA_ERROR_TOO_LARGE,
-                 "algebraic N-view path limited to 48 views per track");
+    (void)max_len;  // any track length: the N-view reduction keeps O(1) state per track
     h->arena.reset();
     const int xo = method == 2 ? 3 : 4;
     h->arena.reserve(sizeof(double) * (12 * num_cameras + 2 * no + (xo + 1) * num_tracks) + sizeof(int64_t) * (num_tracks + 1) +
@@ -581,16 +449,8 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
     double* dX = out_view(h, X, xo * num_tracks, memory);
     double* derr = out_view(h, error, num_tracks, memory);
     check_cams(h, dcam, no, num_cameras);
-    if (method == GBTRI_ITERATIVE) {
-      k_iterative64<<<std::max(1, std::min<int>((int)ceil_div(num_tracks, 128), h->sm_count * 16)), 128, 0, h->active>>>(
-          dP, doff, dcam, dxy, num_tracks, dX, derr);
-    } else {
-      const size_t smem = sizeof(double) * ((size_t)3 * kMaxViews * (4 + kMaxViews) + (4 + kMaxViews) * (4 + kMaxViews) + 64);
-      static PerDeviceOnce once;
-      once.run([&] { GBBA_CUDA(cudaFuncSetAttribute(k_nview64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); });
-      k_nview64<<<(unsigned)std::min<int64_t>(num_tracks, (int64_t)h->sm_count * 32), 32, smem, h->active>>>(
-          method, dP, doff, dcam, dxy, num_tracks, dX);
-    }
+    k_nview64<<<std::max(1, std::min<int>((int)ceil_div(num_tracks, 128), h->sm_count * 16)), 128, 0, h->active>>>(
+        method, dP, doff, dcam, dxy, num_tracks, dX, method == GBTRI_ITERATIVE ? derr : nullptr);
     check_launch(h);
     out_back(h, X, dX, xo * num_tracks, memory);
     if (method == GBTRI_ITERATIVE) out_back(h, error, derr, num_tracks, memory);
@@ -599,10 +459,12 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
   });
 }
 
-gbba_status gbtri_nview_batched_f32(gbba_handle* h, const float* P, int64_t num_cameras, const uint32_t* track_offsets,
-                                    const uint32_t* camera_index, const float* xy, int64_t num_tracks, int32_t gn_steps,
-                                    float* X, uint8_t* status, float* min_depth, int32_t memory) {
-  if (num_tracks < 0 || num_cameras < 0 || gn_steps < 0 || !P || !track_offsets || !X) return GBBA_ERROR_INVALID_ARGUMENT;
+gbba_status gbtri_nview_batched_f32(gbba_handle* h, int32_t method, const float* P, int64_t num_cameras,
+                                    const uint32_t* track_offsets, const uint32_t* camera_index, const float* xy,
+                                    int64_t num_tracks, int32_t gn_steps, float* X, uint8_t* status, float* min_depth,
+                                    int32_t memory) {
+  if (method < 0 || method > 2 || num_tracks < 0 || num_cameras < 0 || gn_steps < 0 || !P || !track_offsets || !X)
+    return GBBA_ERROR_INVALID_ARGUMENT;
   if (num_tracks >= 0xFFFFFFFFLL) return GBBA_ERROR_TOO_LARGE;
   return tri_guard(h, [&]() {
     if (num_tracks == 0) return GBBA_SUCCESS;
@@ -626,7 +488,7 @@ gbba_status gbtri_nview_batched_f32(gbba_handle* h, const float* P, int64_t num_
       GBBA_CUDA(cudaFuncSetAttribute(k_tri_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tri_f32_smem(kTriCams)));
     });
     k_tri_f32<<<(unsigned)ceil_div(num_tracks, kTriThreads), kTriThreads, smem, h->active>>>(
-        dP, num_cameras, doff, dcam, reinterpret_cast<const float2*>(dxy), num_tracks, gn_steps, dX, dst, dmd);
+        method, dP, num_cameras, doff, dcam, reinterpret_cast<const float2*>(dxy), num_tracks, gn_steps, dX, dst, dmd);
     check_launch(h);
     out_back(h, X, dX, 3 * num_tracks, memory);
     out_back(h, status, dst, num_tracks, memory);

@@ -205,8 +205,8 @@ def measure_triangulation(h, torch, steps, warmup):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def run():
-        rc = h.lib.gbtri_nview_batched_f32(h.h, P.data_ptr(), P.shape[0], off.data_ptr(), cam.data_ptr(), xy.data_ptr(),
-                                           nt, 1, X.data_ptr(), st.data_ptr(), md.data_ptr(), abi.MEMORY_DEVICE)
+        rc = h.lib.gbtri_nview_batched_f32(h.h, abi.TRI_NVIEW, P.data_ptr(), P.shape[0], off.data_ptr(), cam.data_ptr(),
+                                           xy.data_ptr(), nt, 1, X.data_ptr(), st.data_ptr(), md.data_ptr(), abi.MEMORY_DEVICE)
         h.check(rc, "gbtri_nview_batched_f32")
 
     for _ in range(warmup):

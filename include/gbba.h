@@ -242,6 +242,18 @@ gbba_status gbba_project_backward(gbba_handle* handle, const gbba_problem* probl
                                   double* jac_extrinsic, double* jac_intrinsic,
                                   double* jac_point, double* gradient);
 
+/* The same contract for the Jacobian of the mixed-precision path
+ * (GBBA_PRECISION_MIXED): the FP32 instantiation of the hand-written adjoint
+ * that the mixed solve's Schur build evaluates, at FP32 copies of the
+ * parameters and observations, with the residual and the Corrector scale in
+ * FP64.  Outputs as for gbba_project_backward, widened to double.  Replaces
+ * the same ceres::Problem::Evaluate Jacobian (problem.h:392-468), at FP32
+ * accuracy. */
+gbba_status gbba_project_backward_mixed(gbba_handle* handle, const gbba_problem* problem,
+                                        int32_t loss_type, double loss_scale,
+                                        double* jac_extrinsic, double* jac_intrinsic,
+                                        double* jac_point, double* gradient);
+
 /* Forward projection that allocates nothing.  It has no counterpart in the
  * reference; it exists for callers that cannot call cudaMalloc -- a host
  * application whose device memory is already owned by its own pool

@@ -38,7 +38,7 @@ typedef enum gbtri_method {
 /* Per-track status of the FP32 path. */
 typedef enum gbtri_track_status {
   GBTRI_TRACK_OK = 0,
-  GBTRI_TRACK_DEGENERATE = 1,    /* fewer than 2 views or singular normal equations */
+  GBTRI_TRACK_DEGENERATE = 1,    /* fewer than 2 views, a point at infinity or singular equations */
   GBTRI_TRACK_BEHIND_CAMERA = 2  /* min depth over the track's views <= 0 */
 } gbtri_track_status;
 
@@ -58,22 +58,23 @@ gbba_status gbtri_dlt2_batched(gbba_handle* handle, int64_t n,
  * X: [num_tracks][4] (unit homogeneous) for GBTRI_NVIEW / _ALGEBRAIC,
  *    [num_tracks][3] for GBTRI_ITERATIVE.
  * error: GBTRI_ITERATIVE only, Triangulation::error(X) per track (sum of
- *    reprojection distances), or NULL.  Tracks are limited to
- *    GBTRI_MAX_TRACK_LENGTH views for GBTRI_NVIEW. */
-#define GBTRI_MAX_TRACK_LENGTH 64
+ *    reprojection distances), or NULL.  Tracks may have any length: the
+ *    nullspace is found from a per-track 4x4 reduction of the design, with
+ *    O(1) state per track, instead of an SVD of the (3n) x (4+n) matrix. */
 gbba_status gbtri_nview_batched(gbba_handle* handle, int32_t method,
                                 const double* P, int64_t num_cameras,
                                 const int64_t* track_offsets, const uint32_t* camera_index,
                                 const double* xy, int64_t num_tracks,
                                 double* X, double* error, int32_t memory);
 
-/* The production path: FP32 linear N-view triangulation (one pass of the
- * reference's weighted linear system with unit weights) followed by
- * `gn_steps` Gauss-Newton steps on the reprojection error.
- * track_offsets are uint32 [num_tracks+1]; outputs X [num_tracks][3],
- * status [num_tracks] (gbtri_track_status, may be NULL), min_depth
- * [num_tracks] (may be NULL). */
-gbba_status gbtri_nview_batched_f32(gbba_handle* handle,
+/* The production path in FP32: the same estimators as gbtri_nview_batched
+ * (`method`: GBTRI_NVIEW, the reference's TriangulateNView dehomogenised;
+ * GBTRI_NVIEW_ALGEBRAIC; GBTRI_ITERATIVE, Triangulation::compute(3)) followed
+ * by `gn_steps` Gauss-Newton steps on the reprojection error.
+ * track_offsets are uint32 [num_tracks+1]; outputs X [num_tracks][3]
+ * (Euclidean), status [num_tracks] (gbtri_track_status, may be NULL),
+ * min_depth [num_tracks] (may be NULL). */
+gbba_status gbtri_nview_batched_f32(gbba_handle* handle, int32_t method,
                                     const float* P, int64_t num_cameras,
                                     const uint32_t* track_offsets, const uint32_t* camera_index,
                                     const float* xy, int64_t num_tracks, int32_t gn_steps,

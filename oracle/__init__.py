@@ -132,6 +132,32 @@ def tri_linear_gn(P, offsets, cam, xy, gn_steps=1):
     return X, st, md
 
 
+def tri_gn_steps(P, offsets, cam, xy, X0, steps=1):
+    """FP64 Gauss-Newton steps on the reprojection error of each track, from
+    the Euclidean points X0 (numpy restatement; the step the triangulation
+    paths apply after their linear estimate): H = sum J^T J, g = sum J^T r over
+    the track's views, X <- X - H^-1 g."""
+    P = np.asarray(P, np.float64).reshape(-1, 3, 4)
+    off = np.asarray(offsets, np.int64)
+    cam = np.asarray(cam, np.int64)
+    xy = np.asarray(xy, np.float64).reshape(-1, 2)
+    X = np.array(X0, np.float64, copy=True)
+    tr = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    for _ in range(steps):
+        Pi = P[cam]
+        h = np.einsum("nij,nj->ni", Pi[:, :, :3], X[tr]) + Pi[:, :, 3]
+        u, v = h[:, 0] / h[:, 2], h[:, 1] / h[:, 2]
+        Ju = (Pi[:, 0, :3] - u[:, None] * Pi[:, 2, :3]) / h[:, 2:3]
+        Jv = (Pi[:, 1, :3] - v[:, None] * Pi[:, 2, :3]) / h[:, 2:3]
+        ru, rv = u - xy[:, 0], v - xy[:, 1]
+        H = np.zeros((len(X), 3, 3))
+        g = np.zeros((len(X), 3))
+        np.add.at(H, tr, Ju[:, :, None] * Ju[:, None, :] + Jv[:, :, None] * Jv[:, None, :])
+        np.add.at(g, tr, Ju * ru[:, None] + Jv * rv[:, None])
+        X = X - np.linalg.solve(H, g[:, :, None])[:, :, 0]
+    return X
+
+
 # ------------------------------------------------------------ reference harness
 def write_kv(path, items):
     with open(path, "w") as f:
@@ -173,7 +199,7 @@ def ref_run(mode, items, tmpdir, extra_args=()):
     return read_kv(out)
 
 
-def scene_to_kv(scene, options, layout=0, linear_solver=0, num_threads=1):
+def scene_to_kv(scene, options, layout=0, linear_solver=0, num_threads=1, preconditioner=0):
     """BA problem + options in the harness's input format."""
     model = int(scene["model"])
     d = {
@@ -187,6 +213,8 @@ def scene_to_kv(scene, options, layout=0, linear_solver=0, num_threads=1):
         "linear_solver": linear_solver, "max_num_iterations": options.max_num_iterations,
         "function_tolerance": options.function_tolerance, "gradient_tolerance": options.gradient_tolerance,
         "parameter_tolerance": options.parameter_tolerance, "num_threads": num_threads,
+        "preconditioner": preconditioner, "max_linear_solver_iterations": options.max_linear_solver_iterations,
+        "eta": options.eta,
     }
     if scene.get("camera_constant") is not None:
         d["camera_constant"] = scene["camera_constant"]

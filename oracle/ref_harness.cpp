@@ -212,7 +212,11 @@ static int RunBA(const KV& kv, const char* out) {
   BuildProblem(b, &problem, true);
   ceres::Solver::Options options;
   const int solver = (int)Get1(kv, "linear_solver", 0);
-  options.preconditioner_type = ceres::JACOBI;
+  // preconditioner: 0 = JACOBI (ceres's default), 1 = SCHUR_JACOBI (the block
+  // diagonal of the reduced camera system, which the GPU PCG implements)
+  options.preconditioner_type = (int)Get1(kv, "preconditioner", 0) == 1 ? ceres::SCHUR_JACOBI : ceres::JACOBI;
+  options.max_linear_solver_iterations = (int)Get1(kv, "max_linear_solver_iterations", 500);
+  options.eta = Get1(kv, "eta", 1e-1);
   if (solver == 0) {
     options.linear_solver_type = ceres::SPARSE_SCHUR;
     options.sparse_linear_algebra_library_type = ceres::CX_SPARSE;
@@ -245,6 +249,11 @@ static int RunBA(const KV& kv, const char* out) {
   w.put1("termination_type", (double)summary.termination_type);
   w.put1("usable", summary.IsSolutionUsable() ? 1 : 0);
   w.put1("total_time_s", summary.total_time_in_seconds);
+  {
+    std::vector<double> lin;
+    for (size_t i = 0; i < summary.iterations.size(); ++i) lin.push_back(summary.iterations[i].linear_solver_iterations);
+    w.put("iteration_linear_solver_iterations", lin);
+  }
   w.put1("minimizer_time_s", summary.minimizer_time_in_seconds);
   std::vector<double> costs, radii, succ;
   for (size_t i = 0; i < summary.iterations.size(); ++i) {

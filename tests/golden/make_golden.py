@@ -7,7 +7,8 @@ on small seeded inputs and stores inputs and outputs as .npz files.  Needs the
 reference sources, so it runs in the development container only; the
 fixtures it writes are committed and travel with the tests.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py            # every fixture
+    python tests/golden/make_golden.py tri_long   # named groups only
 """
 import importlib
 import os
@@ -91,10 +92,76 @@ def unit_test_scene(tmp):
     return sc, P
 
 
+def tri_tracks_f32(tmp):
+    """Tracks of the batched-triangulation workload's distributions (200
+    cameras on a sphere of radius 15, f in [800,1200], lengths 2-30, 1 px
+    noise), with P and the pixels rounded to FP32 before the reference sees
+    them, so that the FP32 path and the reference get identical inputs."""
+    tr = scenes.track_scene(num_cameras=200, num_tracks=6000, seed=22)
+    P = tr["P"].astype(np.float32).astype(np.float64)
+    xy = tr["xy"].astype(np.float32).astype(np.float64)
+    r = oracle.ref_run("tri", {"P": P, "track_offsets": tr["track_offsets"], "camera_index": tr["camera_index"],
+                               "xy": xy}, tmp)
+    save("tri_tracks_f32.npz", P=P.astype(np.float32), track_offsets=tr["track_offsets"].astype(np.uint32),
+         camera_index=tr["camera_index"].astype(np.uint8), xy=xy.astype(np.float32), X_true=tr["X_true"], **r)
+
+
+def tri_long(tmp):
+    """Tracks of 33-150 views (beyond a 32-view warp), as the global engine's
+    per-track loop can produce (sfm_global_engine.cpp:597-651)."""
+    tr = scenes.track_scene(num_cameras=160, num_tracks=40, seed=23, min_len=33, max_len=150)
+    r = oracle.ref_run("tri", {"P": tr["P"], "track_offsets": tr["track_offsets"],
+                               "camera_index": tr["camera_index"], "xy": tr["xy"]}, tmp)
+    save("tri_long.npz", P=tr["P"], track_offsets=tr["track_offsets"], camera_index=tr["camera_index"],
+         xy=tr["xy"], **r)
+
+
+def ba_iterative(tmp):
+    """ceres ITERATIVE_SCHUR with the SCHUR_JACOBI preconditioner (the block
+    diagonal of the reduced camera system, as the GPU PCG uses) on a per-camera
+    K3 scene whose intrinsics are held, so that both preconditioners are the
+    same 6x6 camera blocks; run to a tight function tolerance."""
+    sc = scenes.medium_scene(num_cameras=24, num_points=1200, seed=38)
+    sc["camera_constant"][1] = 1
+    sc["intrinsic_constant"] = np.ones(len(sc["intrinsics"]), np.uint8)
+    o = scenes.ba_options_for(sc, max_num_iterations=60, function_tolerance=1e-10)
+    r = oracle.ref_run("ba", oracle.scene_to_kv(sc, o, linear_solver=2, preconditioner=1), tmp)
+    save("ba_iterative_k3.npz", layout=0, loss=o.loss_type, loss_scale=o.loss_scale,
+         max_num_iterations=o.max_num_iterations, function_tolerance=o.function_tolerance, linear_solver=2,
+         **scene_arrays(sc), **{"ref_" + k: v for k, v in r.items()})
+
+
+def ba_windows(tmp):
+    """Local-BA windows of the batched workload (Brown-T2, one intrinsic group,
+    cameras 0 and 1 held) at 5, 20 and 40 cameras, solved by ceres
+    SPARSE_SCHUR with the call-site options."""
+    for cams, pts, seed in ((5, 200, 44), (20, 400, 45), (40, 600, 46)):
+        rng = np.random.default_rng(seed)
+        sc = scenes.local_problem(rng, cams, pts)
+        sc["camera_constant"][1] = 1
+        ba_case(tmp, f"window_{cams}", sc, max_num_iterations=100)
+
+
+GENERATORS = {
+    "tri_ring": lambda tmp: (tri_ring(tmp, 2, 12), tri_ring(tmp, 5, 6)),
+    "tri_noisy": tri_noisy,
+    "tri_tracks_f32": tri_tracks_f32,
+    "tri_long": tri_long,
+    "ba_iterative": ba_iterative,
+    "ba_windows": ba_windows,
+}
+
+
 def main():
     if not oracle.ref_available():
         raise SystemExit("oracle/_ref/ref_harness missing: run `make -C oracle ref` first")
     tmp = tempfile.mkdtemp()
+    only = sys.argv[1:]
+    if only:
+        # regenerate the named groups only (python make_golden.py tri_long ba_windows)
+        for name in only:
+            GENERATORS[name](tmp)
+        return
     tri_ring(tmp, 2, 12)
     tri_ring(tmp, 5, 6)
     tri_noisy(tmp)
@@ -134,6 +201,10 @@ def main():
     sc = scenes.ring_scene(num_cameras=4, num_points=15, seed=43, model=abi.PINHOLE_F)
     sc["extrinsics"][1, :3] = [1e-9, -2e-9, 5e-10]  # small-angle branch of AngleAxisRotatePoint
     eval_case(tmp, "pinhole_f", sc)
+    tri_tracks_f32(tmp)
+    tri_long(tmp)
+    ba_iterative(tmp)
+    ba_windows(tmp)
 
 
 if __name__ == "__main__":

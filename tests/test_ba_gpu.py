@@ -16,7 +16,7 @@ from test_oracle_golden import BA_CASES, EVAL_CASES, ba_options, corrected, dens
 pytestmark = pytest.mark.gpu
 
 
-def project(handle, abi, sc, loss=0, a=1.0, with_jac=True):
+def project(handle, abi, sc, loss=0, a=1.0, with_jac=True, mixed=False):
     hp = abi.HostProblem(sc)
     p = hp.struct()
     no = p.num_observations
@@ -31,8 +31,9 @@ def project(handle, abi, sc, loss=0, a=1.0, with_jac=True):
         ji = np.zeros((no, 2, k))
         jp = np.zeros((no, 2, 3))
         g = np.zeros(6 * p.num_cameras + k * p.num_intrinsics + 3 * p.num_points)
-        handle.check(handle.lib.gbba_project_backward(handle.h, C.byref(p), loss, a, je.ctypes.data, ji.ctypes.data,
-                                                      jp.ctypes.data, g.ctypes.data), "backward")
+        fn = handle.lib.gbba_project_backward_mixed if mixed else handle.lib.gbba_project_backward
+        handle.check(fn(handle.h, C.byref(p), loss, a, je.ctypes.data, ji.ctypes.data, jp.ctypes.data, g.ctypes.data),
+                     "backward")
         out.update(jac_extrinsic=je, jac_intrinsic=ji, jac_point=jp, gradient=g)
     return out
 
@@ -51,6 +52,69 @@ def test_forward_backward_match_ceres_autodiff(case, handle, abi):
     np.testing.assert_allclose(J, Jr, rtol=1e-9, atol=1e-9 * np.abs(Jr).max())
     np.testing.assert_allclose(ev["gradient"], g["ref_gradient"], rtol=1e-8,
                                atol=1e-9 * np.abs(g["ref_gradient"]).max())
+
+
+# FP32 Jacobian of the mixed path: each entry within 2e-5 of the largest
+# entry of its block type (extrinsic / intrinsic / point), i.e. a few hundred
+# FP32 ulps of the block scale, which covers the rounding of the FP32 adjoint
+# (rotation, distortion polynomial, division by depth) at pixel-scale values.
+FP32_JAC_TOL = 2e-5
+
+
+def assert_blocks_close(J, Jr, sc, k, tol):
+    nc, ni = len(sc["extrinsics"]), len(sc["intrinsics"])
+    for lo, hi in ((0, 6 * nc), (6 * nc, 6 * nc + k * ni), (6 * nc + k * ni, J.shape[1])):
+        ref = Jr[:, lo:hi]
+        scale = max(np.abs(ref).max(), 1e-300)
+        np.testing.assert_allclose(J[:, lo:hi], ref, rtol=0, atol=tol * scale)
+
+
+@pytest.mark.parametrize("case", EVAL_CASES)
+def test_fp32_jacobian_matches_ceres_autodiff(case, handle, abi):
+    """The FP32 Jacobian the mixed solve uses (gbba_project_backward_mixed)
+    against ceres AutoDiff through Problem::Evaluate on the reference functors
+    (autodiff_cost_function.h:202-211, problem.h:392-468)."""
+    g = load_golden(case)
+    sc = scene_from(g)
+    loss, a = int(g["loss"]), float(g["loss_scale"])
+    ev = project(handle, abi, sc, loss, a, mixed=True)
+    k = abi.MODEL_K[sc["model"]]
+    J = dense_jacobian(ev, sc, k)
+    Jr = g["ref_jacobian"].reshape(int(g["ref_jac_rows"][0]), int(g["ref_jac_cols"][0]))
+    assert_blocks_close(J, Jr, sc, k, FP32_JAC_TOL)
+    # gradient J^T r (FP32 J, FP64 r): relative to the largest gradient entry
+    np.testing.assert_allclose(ev["gradient"], g["ref_gradient"], rtol=0,
+                               atol=FP32_JAC_TOL * np.abs(g["ref_gradient"]).max() * 10)
+
+
+@pytest.mark.parametrize("model", [0, 1, 2])
+def test_fp32_jacobian_central_differences(model, handle, abi, scenes):
+    """The FP32 Jacobian against central differences of the FP64 residual on
+    the medium workload's distributions (per-camera K3 and Brown-T2)."""
+    sc = scenes.medium_scene(num_cameras=4, num_points=12, seed=57 + model, model=model)
+    ev = project(handle, abi, sc, mixed=True)
+    k = abi.MODEL_K[model]
+    J = dense_jacobian(ev, sc, k)
+    Jfd = central_differences(handle, abi, sc)
+    assert_blocks_close(J, Jfd, sc, k, FP32_JAC_TOL)
+
+
+def central_differences(handle, abi, sc):
+    base = {f: sc[f].copy() for f in ("extrinsics", "intrinsics", "points")}
+    cols = []
+    for f in ("extrinsics", "intrinsics", "points"):
+        for idx in range(base[f].size):
+            h = 1e-6 * max(1.0, abs(base[f].flat[idx]))
+            plus = dict(sc)
+            minus = dict(sc)
+            plus[f] = base[f].copy()
+            minus[f] = base[f].copy()
+            plus[f].flat[idx] += h
+            minus[f].flat[idx] -= h
+            rp = project(handle, abi, plus, with_jac=False)["residuals"].ravel()
+            rm = project(handle, abi, minus, with_jac=False)["residuals"].ravel()
+            cols.append((rp - rm) / (2 * h))
+    return np.stack(cols, 1)
 
 
 @pytest.mark.parametrize("model", [0, 1, 2])
@@ -256,6 +320,67 @@ def test_iterative_schur_reaches_dense_minimum(precision, handle, abi, scenes):
     i, _ = solve(handle, abi, sc, scenes.ba_options_for(sc, linear_solver=abi.SOLVER_ITERATIVE_SCHUR, **kw))
     assert i.usable and i.linear_solver_iterations > 0
     assert abs(i.final_cost - d.final_cost) <= 1e-7 * d.final_cost, (i.final_cost, d.final_cost)
+
+
+def test_iterative_schur_matches_ceres_iterative_schur(handle, abi):
+    """Block-Jacobi PCG against ceres ITERATIVE_SCHUR with SCHUR_JACOBI
+    (iterative_schur_complement_solver.cc:65-182, conjugate_gradients_solver.cc)
+    on the same scene with the same forcing sequence (eta = 0.1) and stopping
+    rule.  Intrinsics are held, so both preconditioners are the inverse 6x6
+    camera blocks of S.  The truncated CG steps of two implementations differ
+    in rounding, so the trajectories agree closely but not bit for bit: the
+    first LM step's cost to 1e-6, the cost after 60 iterations to 1e-7."""
+    g = load_golden("ba_iterative_k3.npz")
+    sc = scene_from(g)
+    o = ba_options(abi, g)
+    o.linear_solver = abi.SOLVER_ITERATIVE_SCHUR
+    o.function_tolerance = float(g["function_tolerance"])
+    s, _ = solve(handle, abi, sc, o)
+    ref = g["ref_iteration_cost"]
+    assert s.usable and s.linear_solver_iterations > 0
+    assert abs(s.initial_cost - ref[0]) <= 1e-11 * ref[0]
+    o1 = ba_options(abi, g)
+    o1.linear_solver = abi.SOLVER_ITERATIVE_SCHUR
+    o1.max_num_iterations = 1
+    s1, _ = solve(handle, abi, sc, o1)
+    assert abs(s1.final_cost - ref[1]) <= 1e-6 * ref[1], (s1.final_cost, ref[1])
+    assert abs(s.final_cost - g["ref_final_cost"][0]) <= 1e-7 * g["ref_final_cost"][0], \
+        (s.final_cost, g["ref_final_cost"][0])
+    # the CG work per LM step is of the same size as ceres's
+    ref_cg = g["ref_iteration_linear_solver_iterations"].sum()
+    assert 0.5 * ref_cg <= s.linear_solver_iterations <= 2.0 * ref_cg, (s.linear_solver_iterations, ref_cg)
+
+
+WINDOW_CASES = ["ba_window_5.npz", "ba_window_20.npz", "ba_window_40.npz"]
+
+
+def test_batched_windows_match_ceres(handle, abi):
+    """Local-BA windows of the batched workload (Brown-T2, 5/20/40 cameras)
+    in one gbba_solve_batched launch against ceres SPARSE_SCHUR on each: the
+    FP64 kernel follows ceres's LM iteration by iteration (same iteration
+    count, final cost to 1e-8 -- its FP64 reductions are atomic, so the
+    rounding order varies), and the mixed kernel reaches ceres's final cost
+    within 1e-6 (run with function tolerance 1e-8)."""
+    gs = [load_golden(c) for c in WINDOW_CASES]
+    scs = [scene_from(g) for g in gs]
+    o64 = ba_options(abi, gs[0])
+    st, sums, prms = batched_solve(handle, abi, scs, o64)
+    assert st == abi.SUCCESS
+    for g, s, prm in zip(gs, sums, prms):
+        ref = g["ref_final_cost"][0]
+        assert s.usable and abs(s.initial_cost - g["ref_initial_cost"][0]) <= 1e-11 * g["ref_initial_cost"][0]
+        assert s.num_iterations == len(g["ref_iteration_cost"]) - 1
+        assert abs(s.final_cost - ref) <= 1e-8 * ref, (s.final_cost, ref)
+        np.testing.assert_allclose(prm["points"].ravel(), g["ref_points"], rtol=0, atol=1e-5)
+    o32 = ba_options(abi, gs[0])
+    o32.precision = abi.PRECISION_MIXED
+    o32.function_tolerance = 1e-8
+    o32.max_num_iterations = 200
+    st, sums, _ = batched_solve(handle, abi, scs, o32)
+    assert st == abi.SUCCESS
+    for g, s in zip(gs, sums):
+        ref = g["ref_final_cost"][0]
+        assert s.usable and s.final_cost <= ref * (1 + 1e-6), (s.final_cost, ref)
 
 
 def batched_solve(handle, abi, scenes_list, opts):

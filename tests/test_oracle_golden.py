@@ -27,7 +27,10 @@ def scene_from(g):
     return sc
 
 
-BA_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "ba_*.npz")))
+# ceres SPARSE_SCHUR solves (ba_iterative_* are ceres ITERATIVE_SCHUR runs,
+# compared separately)
+BA_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "ba_*.npz"))
+                  if not os.path.basename(p).startswith("ba_iterative"))
 EVAL_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "eval_*.npz")))
 
 

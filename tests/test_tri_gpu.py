@@ -1,8 +1,8 @@
 """GPU triangulation through the C ABI against the reference's golden outputs
 and the oracle.  Tolerances: FP64 paths 1e-9 (relative to the coordinate
 scale; homogeneous vectors compared up to their unspecified sign); the FP32
-production path against its FP64 twin in the oracle: 2e-4 absolute on points
-in [-3,3]^3 (FP32 normal equations), status codes exact."""
+production path against the reference's FP64 outputs on the same FP32 inputs
+(see assert_fp32_close), status codes exact."""
 import numpy as np
 import pytest
 
@@ -80,7 +80,7 @@ def test_reference_unit_test_assertions_on_gpu(handle, abi):
         assert np.abs(h[..., :2] / h[..., 2:3] - xy.reshape(6, 5, 2)).max() < 1e-9
 
 
-def f32_path(handle, abi, tr, gn_steps=1):
+def f32_path(handle, abi, tr, gn_steps=1, method=0):
     nt = len(tr["track_offsets"]) - 1
     P32 = np.ascontiguousarray(tr["P"], np.float32)
     off = np.ascontiguousarray(tr["track_offsets"], np.uint32)
@@ -89,22 +89,101 @@ def f32_path(handle, abi, tr, gn_steps=1):
     X = np.zeros((nt, 3), np.float32)
     st = np.zeros(nt, np.uint8)
     md = np.zeros(nt, np.float32)
-    handle.check(handle.lib.gbtri_nview_batched_f32(handle.h, P32.ctypes.data, len(P32), off.ctypes.data,
+    handle.check(handle.lib.gbtri_nview_batched_f32(handle.h, method, P32.ctypes.data, len(P32), off.ctypes.data,
                                                     cam.ctypes.data, xy.ctypes.data, nt, gn_steps, X.ctypes.data,
                                                     st.ctypes.data, md.ctypes.data, abi.MEMORY_HOST), "f32")
     return X, st, md
 
 
-def test_fp32_path_matches_fp64_twin(handle, abi, scenes, oracle_mod):
-    tr = scenes.track_scene(num_cameras=200, num_tracks=20000, seed=2)
-    X, st, md = f32_path(handle, abi, tr)
-    Xo, sto, mdo = oracle_mod.tri_linear_gn(tr["P"], tr["track_offsets"], tr["camera_index"], tr["xy"], 1)
-    assert np.array_equal(st, sto)
-    assert np.abs(X - Xo).max() < 2e-4
-    np.testing.assert_allclose(md, mdo, rtol=1e-4)
-    # and the estimate is as good as the reference's N-view DLT: error vs ground truth
-    e32 = np.linalg.norm(X - tr["X_true"], axis=1)
-    assert np.median(e32) < 0.01
+def euclid(Xh):
+    return Xh[:, :3] / Xh[:, 3:]
+
+
+def point_error(X, ref):
+    return np.abs(X - ref).max(1) / np.maximum(1.0, np.abs(ref).max(1))
+
+
+# FP32 against the reference on identical (FP32-representable) inputs, points
+# in [-3,3]^3: median 1e-5, 99th percentile 5e-5, worst track 5e-3 (short
+# tracks with near-parallel rays); the per-track FP32 rounding of the same
+# code run on the CPU is 1.7e-6 median, 9.3e-6 p99, 9.7e-4 worst.
+def assert_fp32_close(X, ref):
+    err = point_error(X.astype(np.float64), ref)
+    assert np.median(err) < 1e-5 and np.quantile(err, 0.99) < 5e-5 and err.max() < 5e-3, \
+        (np.median(err), np.quantile(err, 0.99), err.max())
+
+
+@pytest.mark.parametrize("method,key", [(0, "nview_h"), (1, "algebraic_h"), (2, "iterative_e")])
+def test_fp32_path_matches_reference(method, key, handle, abi):
+    """The FP32 production kernel without refinement reproduces the
+    reference's own estimator (TriangulateNView / TriangulateNViewAlgebraic /
+    Triangulation::compute(3), triangulation_nview.cpp:8-121) on 6,000 tracks
+    of the batched workload's distributions (200 cameras, lengths 2-30,
+    1 px noise)."""
+    g = load_golden("tri_tracks_f32.npz")
+    nt = len(g["track_offsets"]) - 1
+    tr = {k: g[k] for k in ("P", "track_offsets", "camera_index", "xy")}
+    X, st, md = f32_path(handle, abi, tr, gn_steps=0, method=method)
+    ref = g[key].reshape(nt, -1)
+    ref = euclid(ref) if ref.shape[1] == 4 else ref
+    assert (st == abi.TRACK_OK).all()
+    assert_fp32_close(X, ref)
+
+
+def test_fp32_nview_gauss_newton_matches_fp64(handle, abi):
+    """The production configuration (FP32 N-view + one Gauss-Newton step)
+    against the FP64 oracle of the same: the reference's TriangulateNView
+    output, dehomogenised, then one FP64 Gauss-Newton step."""
+    import oracle
+    g = load_golden("tri_tracks_f32.npz")
+    nt = len(g["track_offsets"]) - 1
+    tr = {k: g[k] for k in ("P", "track_offsets", "camera_index", "xy")}
+    X, st, md = f32_path(handle, abi, tr, gn_steps=1, method=0)
+    ref = oracle.tri_gn_steps(g["P"], g["track_offsets"], g["camera_index"], g["xy"],
+                              euclid(g["nview_h"].reshape(nt, 4)), 1)
+    assert (st == abi.TRACK_OK).all()
+    assert_fp32_close(X, ref)
+    # the step lowers the reprojection error against the linear estimate
+    e_lin = np.linalg.norm(euclid(g["nview_h"].reshape(nt, 4)) - g["X_true"], axis=1)
+    e_gn = np.linalg.norm(X - g["X_true"], axis=1)
+    assert np.median(e_gn) <= np.median(e_lin)
+
+
+def test_fp64_long_tracks_match_reference(handle, abi):
+    """Tracks of 33-150 views (no length limit): all three FP64 estimators
+    against the reference at 1e-9."""
+    g = load_golden("tri_long.npz")
+    P = g["P"].reshape(-1, 12)
+    off = g["track_offsets"].astype(np.int64)
+    cam = g["camera_index"].astype(np.uint32)
+    xy = g["xy"].reshape(-1, 2)
+    nt = len(off) - 1
+    assert np.diff(off).min() > 32
+    for method, key in ((abi.TRI_NVIEW, "nview_h"), (abi.TRI_NVIEW_ALGEBRAIC, "algebraic_h")):
+        st, X, _ = nview(handle, abi, method, P, off, cam, xy)
+        assert st == 0
+        assert same_up_to_sign(X, g[key].reshape(nt, 4), 1e-9), key
+    st, X, err = nview(handle, abi, abi.TRI_ITERATIVE, P, off, cam, xy)
+    assert st == 0
+    np.testing.assert_allclose(X, g["iterative_e"].reshape(nt, 3), rtol=1e-9, atol=1e-9)
+    np.testing.assert_allclose(err, g["iterative_error"], rtol=1e-6)
+
+
+def test_fp32_path_full_size_properties(handle, abi, scenes):
+    """At the full batched size (1,000,000 tracks), properties that do not
+    need an oracle: every track triangulates, the N-view estimate lies within
+    a small distance of the ground truth, and a track's result does not depend
+    on the batch it is in (first 5,000 tracks alone = the same tracks in the
+    full batch)."""
+    tr = scenes.track_scene(seed=2)
+    X, st, md = f32_path(handle, abi, tr, gn_steps=1, method=0)
+    assert (st == abi.TRACK_OK).mean() > 0.999
+    err = np.linalg.norm(X - tr["X_true"], axis=1)
+    assert np.median(err) < 0.01
+    sub = {"P": tr["P"], "track_offsets": tr["track_offsets"][:5001], "camera_index": tr["camera_index"],
+           "xy": tr["xy"]}
+    Xs, sts, _ = f32_path(handle, abi, sub, gn_steps=1, method=0)
+    np.testing.assert_array_equal(Xs, X[:5000])
 
 
 def test_fp32_path_edge_cases(handle, abi):
@@ -125,19 +204,10 @@ def test_fp32_path_edge_cases(handle, abi):
     xy = [proj(Xg, 0), proj(Xb, 0), proj(Xb, 1), proj(Xg, 0), proj(Xg, 1)]
     tr = {"P": P, "track_offsets": np.array([0, 1, 3, 3, 5]), "camera_index": np.array([0, 0, 1, 0, 1], np.uint32),
           "xy": np.array(xy)}
-    X, st, md = f32_path(handle, abi, tr, gn_steps=2)
-    assert list(st) == [abi.TRACK_DEGENERATE, abi.TRACK_BEHIND_CAMERA, abi.TRACK_DEGENERATE, abi.TRACK_OK]
-    assert np.abs(X[3] - Xg).max() < 1e-4
-
-
-def test_nview_too_long_track_rejected(handle, abi):
-    n = 40
-    P = np.tile(np.eye(3, 4).ravel(), (n, 1))
-    off = np.array([0, n])
-    cam = np.arange(n, dtype=np.uint32)
-    xy = np.zeros((n, 2))
-    st, _, _ = nview(handle, abi, abi.TRI_NVIEW, P, off, cam, xy)
-    assert st == abi.ERROR_TOO_LARGE
+    for method in (0, 1, 2):
+        X, st, md = f32_path(handle, abi, tr, gn_steps=2, method=method)
+        assert list(st) == [abi.TRACK_DEGENERATE, abi.TRACK_BEHIND_CAMERA, abi.TRACK_DEGENERATE, abi.TRACK_OK]
+        assert np.abs(X[3] - Xg).max() < 1e-4
 
 
 def test_refine_gn_fp64(handle, abi, scenes, oracle_mod):
