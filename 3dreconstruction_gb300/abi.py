@@ -104,6 +104,10 @@ class GbbaOptions(C.Structure):
         ("stream", C.c_void_p),
         ("fp64_polish_iterations", C.c_int32),
         ("schur_build", C.c_int32),
+        ("trace_cost", C.c_void_p),
+        ("trace_time_s", C.c_void_p),
+        ("trace_capacity", C.c_int32),
+        ("trace_reserved", C.c_int32),
     ]
 
 
@@ -303,6 +307,8 @@ def declare_gbba(lib):
     lib.gbba_project_backward_mixed.restype = C.c_int
     lib.gbba_project_forward_noalloc.argtypes = [P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp]
     lib.gbba_project_forward_noalloc.restype = C.c_int
+    lib.gbba_last_kernel_time.argtypes = [vp, vp]
+    lib.gbba_last_kernel_time.restype = C.c_int
     lib.gbtri_dlt2_batched.argtypes = [vp, C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
     lib.gbtri_dlt2_batched.restype = C.c_int
     lib.gbtri_nview_batched.argtypes = [vp, C.c_int32, vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp, C.c_int32]
@@ -318,7 +324,7 @@ def declare_gbba(lib):
 # Every symbol the C-ABI headers declare (checked by the CPU tests).
 EXPORTED_SYMBOLS = (
     "gbba_create", "gbba_destroy", "gbba_default_options", "gbba_status_string",
-    "gbba_abi_version", "gbba_launch_count", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
+    "gbba_abi_version", "gbba_launch_count", "gbba_last_kernel_time", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
     "gbba_project_forward", "gbba_project_backward", "gbba_project_backward_mixed", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
 )

@@ -258,6 +258,8 @@ gbba_status gbba_create(int device, gbba_handle** out) {
     GBBA_CUDA(cudaStreamCreateWithPriority(&h->side, cudaStreamNonBlocking, least));
     GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_main, cudaEventDisableTiming));
     GBBA_CUDA(cudaEventCreateWithFlags(&h->ev_side, cudaEventDisableTiming));
+    GBBA_CUDA(cudaEventCreate(&h->ev_k0));
+    GBBA_CUDA(cudaEventCreate(&h->ev_k1));
     GBBA_CUDA(cudaHostAlloc((void**)&h->pinned, 256 * sizeof(double), cudaHostAllocDefault));
     GBBA_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device));
   } catch (const Error& e) {
@@ -279,12 +281,30 @@ void gbba_destroy(gbba_handle* h) {
   if (h->side) cudaStreamSynchronize(h->side);
   if (h->ev_main) cudaEventDestroy(h->ev_main);
   if (h->ev_side) cudaEventDestroy(h->ev_side);
+  if (h->ev_k0) cudaEventDestroy(h->ev_k0);
+  if (h->ev_k1) cudaEventDestroy(h->ev_k1);
   if (h->side) cudaStreamDestroy(h->side);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
 }
 
 int64_t gbba_launch_count(const gbba_handle* h) { return h ? h->launches : 0; }
+
+gbba_status gbba_last_kernel_time(gbba_handle* h, double* seconds) {
+  if (!h || !seconds) return GBBA_ERROR_INVALID_ARGUMENT;
+  if (!h->kernel_timed) return GBBA_ERROR_NOT_SUPPORTED;
+  if (cudaSetDevice(h->device) != cudaSuccess) {
+    cudaGetLastError();
+    return GBBA_ERROR_CUDA;
+  }
+  float ms = 0.0f;
+  if (cudaEventElapsedTime(&ms, h->ev_k0, h->ev_k1) != cudaSuccess) {
+    cudaGetLastError();
+    return GBBA_ERROR_CUDA;
+  }
+  *seconds = ms * 1e-3;
+  return GBBA_SUCCESS;
+}
 
 gbba_status gbba_solve(gbba_handle* h, const gbba_problem* P, const gbba_options* o, gbba_summary* sum) {
   if (!o || !sum) return GBBA_ERROR_INVALID_ARGUMENT;

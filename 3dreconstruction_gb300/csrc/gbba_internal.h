@@ -119,6 +119,9 @@ struct gbba_handle {
   int prio_hi = 0;
   // observation pairs per work item of the camera-pair products (gbba_autotune)
   int pair_chunk = 128;
+  // device time of the main kernel of the last triangulation call
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
+  bool kernel_timed = false;
 };
 
 namespace gbba {

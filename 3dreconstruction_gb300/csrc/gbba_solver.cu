@@ -1778,6 +1778,7 @@ struct Solve {
   void* rec = nullptr;
   bool dense = true;
   int schur_build = GBBA_SCHUR_BUILD_AUTO;  // gbba_options::schur_build
+  double t_origin = 0.0;                     // start of the gbba_solve call (trace times)
   // iterative Schur (PCG) state
   double *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr, *pcg_b = nullptr;
   double *pcg_y = nullptr, *pcg_minv = nullptr, *pcg_part = nullptr;
@@ -2470,6 +2471,13 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     sum->final_cost = cost;
     return GBBA_ERROR_NUMERICAL;
   }
+  auto trace = [&](int i, double c) {
+    if (o->trace_capacity > i && i >= 0) {
+      if (o->trace_cost) o->trace_cost[i] = c;
+      if (o->trace_time_s) o->trace_time_s[i] = now_s() - s.t_origin;
+    }
+  };
+  trace(0, cost);
   double gmax = 0, x_norm = 0;
   const double tj0 = now_s();
   linearize(true, &gmax, &x_norm);
@@ -2705,6 +2713,7 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       success = relative_decrease > o->min_relative_decrease;
       if (success) cost = new_cost;
     }
+    trace(iteration, cost);
     if (success) {
       ++sum->num_successful_steps;
       radius = radius / std::max(1.0 / 3.0, 1.0 - std::pow(2.0 * relative_decrease - 1.0, 3));
@@ -2754,6 +2763,7 @@ gbba_status solve_impl(gbba_handle* h, const gbba_problem* P, const gbba_options
     return GBBA_SUCCESS;
   }
   Solve s{};
+  s.t_origin = t0;
   setup(h, P, o, s);
   gbba_status st = GBBA_SUCCESS;
   const bool fp64 = o->precision == GBBA_PRECISION_FP64;
@@ -2779,6 +2789,8 @@ gbba_status solve_impl(gbba_handle* h, const gbba_problem* P, const gbba_options
     o2.max_num_iterations = o->fp64_polish_iterations;
     o2.function_tolerance = o->function_tolerance * 1e-3;
     o2.parameter_tolerance = o->parameter_tolerance * 1e-3;
+    o2.trace_cost = o2.trace_time_s = nullptr;
+    o2.trace_capacity = 0;
     gbba_summary s2{};
     const gbba_status st2 = solve_impl(h, P, &o2, &s2);
     if (st2 == GBBA_SUCCESS && s2.usable) {

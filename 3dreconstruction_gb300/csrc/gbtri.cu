@@ -117,7 +117,8 @@ __device__ __forceinline__ void gn_apply(const T Hi[6], const T g[3], T X[3]) {
 }
 
 __global__ void k_refine_gn64(const double* P, const int64_t* offs, const uint32_t* cam, const double* xy, int64_t nt,
-                              int steps, double* X) {
+                              int steps, double* X, const unsigned int* __restrict__ bad) {
+  if (*bad) return;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = offs[t];
     const int n = (int)(offs[t + 1] - b);
@@ -150,7 +151,9 @@ struct GlobalViews64 {
 // [nt][3] and Triangulation::error (ITERATIVE).
 __global__ void __launch_bounds__(128) k_nview64(int method, const double* __restrict__ P, const int64_t* __restrict__ offs,
                                                  const uint32_t* __restrict__ cam, const double* __restrict__ xy,
-                                                 int64_t nt, double* __restrict__ X, double* __restrict__ err) {
+                                                 int64_t nt, double* __restrict__ X, double* __restrict__ err,
+                                                 const unsigned int* __restrict__ bad) {
+  if (*bad) return;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = offs[t];
     const int n = (int)(offs[t + 1] - b);
@@ -218,7 +221,9 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_f32(int method, const float
                                                          const uint32_t* __restrict__ offs, const uint32_t* __restrict__ cam,
                                                          const float2* __restrict__ xy, int64_t nt, int gn_steps,
                                                          float* __restrict__ X, uint8_t* __restrict__ status,
-                                                         float* __restrict__ min_depth) {
+                                                         float* __restrict__ min_depth,
+                                                         const unsigned int* __restrict__ bad) {
+  if (*bad) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   float* sP = reinterpret_cast<float*>(smraw);                                   // [ncam_s][12]
   const int ncam_s = ncam <= kTriCams ? (int)ncam : 0;
@@ -336,67 +341,67 @@ void out_back(gbba_handle* h, T* user, const T* dev, size_t count, int memory) {
   GBBA_CUDA(cudaMemcpyAsync(user, dev, count * sizeof(T), cudaMemcpyDeviceToHost, h->active));
 }
 
-// Device check of CSR offsets: offs[0] == 0, non-decreasing; returns the total
-// and the longest track.  info = {error, max_len, total_lo, total_hi}.
+// One pass over a batch's CSR offsets and camera indices: offs[0] == 0,
+// non-decreasing offsets, every camera index below ncam (the camera index
+// array holds offs[nt] entries).  Sets bit 0 (offsets) or bit 1 (camera
+// index) of *err.  The triangulation kernels that follow on the stream read
+// *err first and do nothing when it is set, so a bad batch is never indexed;
+// the host reads *err once, after them.
 template <typename Off>
-__global__ void k_check_offsets(const Off* offs, int64_t nt, unsigned int* info) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+__global__ void k_check_tracks(const Off* __restrict__ offs, int64_t nt, const uint32_t* __restrict__ cam,
+                               int64_t ncam, unsigned int* __restrict__ err) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  bool bad_off = false, bad_cam = false;
+  for (int64_t t = i0; t < nt; t += stride) {
     const int64_t a = (int64_t)offs[t], b = (int64_t)offs[t + 1];
-    if (b < a || (t == 0 && a != 0)) atomicExch(&info[0], 1u);
-    else atomicMax(&info[1], (unsigned int)(b - a > 0x7fffffff ? 0x7fffffff : b - a));
-    if (t == nt - 1) {
-      info[2] = (unsigned int)(b & 0xffffffff);
-      info[3] = (unsigned int)(b >> 32);
-    }
+    if (b < a || (t == 0 && a != 0)) bad_off = true;
   }
+  const int64_t no = (int64_t)offs[nt];
+  for (int64_t o = i0; o < no; o += stride)
+    if (cam[o] >= ncam) bad_cam = true;
+  if (bad_off) atomicOr(err, 1u);
+  if (bad_cam) atomicOr(err, 2u);
+}
+
+// Observation count of a batch (offs[nt]): read on the host for host memory
+// (the copies need it), not needed for device memory.
+template <typename Off>
+int64_t host_total(const Off* offs, int64_t nt, int memory) {
+  if (memory == GBBA_MEMORY_DEVICE) return 0;
+  GBBA_REQUIRE(offs[0] == 0 && (int64_t)offs[nt] >= 0, GBBA_ERROR_INVALID_ARGUMENT,
+               "track_offsets must start at 0 and be non-decreasing");
+  return (int64_t)offs[nt];
 }
 
 template <typename Off>
-void check_offsets(gbba_handle* h, const Off* offs, int64_t nt, int memory, int64_t* total, int* max_len) {
-  if (memory == GBBA_MEMORY_DEVICE) {
-    unsigned int* info = nullptr;
-    GBBA_CUDA(cudaMallocAsync((void**)&info, 4 * sizeof(unsigned int), h->active));
-    GBBA_CUDA(cudaMemsetAsync(info, 0, 4 * sizeof(unsigned int), h->active));
-    k_check_offsets<Off><<<std::max(1, std::min<int>((int)ceil_div(nt, 256), h->sm_count * 8)), 256, 0, h->active>>>(offs, nt, info);
-    check_launch(h);
-    unsigned int hi[4];
-    GBBA_CUDA(cudaMemcpyAsync(hi, info, sizeof(hi), cudaMemcpyDeviceToHost, h->active));
-    GBBA_CUDA(cudaFreeAsync(info, h->active));
-    GBBA_CUDA(cudaStreamSynchronize(h->active));
-    GBBA_REQUIRE(hi[0] == 0, GBBA_ERROR_INVALID_ARGUMENT, "track_offsets must start at 0 and be non-decreasing");
-    *max_len = (int)hi[1];
-    *total = (int64_t)hi[2] | ((int64_t)hi[3] << 32);
-    return;
-  }
-  std::vector<Off> ho(nt + 1);
-  std::memcpy(ho.data(), offs, sizeof(Off) * (nt + 1));
-  GBBA_REQUIRE(ho[0] == 0, GBBA_ERROR_INVALID_ARGUMENT, "track_offsets[0] must be 0");
-  int ml = 0;
-  for (int64_t t = 0; t < nt; ++t) {
-    GBBA_REQUIRE(ho[t + 1] >= ho[t], GBBA_ERROR_INVALID_ARGUMENT, "track_offsets must be non-decreasing");
-    ml = std::max<int>(ml, (int)(ho[t + 1] - ho[t]));
-  }
-  *total = (int64_t)ho[nt];
-  *max_len = ml;
+unsigned int* launch_check(gbba_handle* h, const Off* doff, int64_t nt, const uint32_t* dcam, int64_t ncam) {
+  unsigned int* err = h->arena.take<unsigned int>(1);
+  GBBA_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned int), h->active));
+  k_check_tracks<Off><<<std::max(1, std::min<int>((int)ceil_div(nt, 256), h->sm_count * 8)), 256, 0, h->active>>>(
+      doff, nt, dcam, ncam, err);
+  check_launch(h);
+  return err;
 }
 
-__global__ void k_check_cam(const uint32_t* cam, int64_t n, int64_t ncam, int* err) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    if (cam[i] >= ncam) atomicExch(err, 1);
-}
-
-void check_cams(gbba_handle* h, const uint32_t* dcam, int64_t n, int64_t ncam) {
-  int* err = h->arena.take<int>(1);
-  GBBA_CUDA(cudaMemsetAsync(err, 0, sizeof(int), h->active));
-  if (n > 0) {
-    k_check_cam<<<std::max(1, std::min<int>((int)ceil_div(n, 256), h->sm_count * 8)), 256, 0, h->active>>>(dcam, n, ncam, err);
-    check_launch(h);
-  }
-  int herr = 0;
-  GBBA_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, h->active));
+// Waits for the call's work and turns the check bits into a status.
+void finish_check(gbba_handle* h, const unsigned int* err) {
+  unsigned int* hp = reinterpret_cast<unsigned int*>(h->pinned + 128);
+  GBBA_CUDA(cudaMemcpyAsync(hp, err, sizeof(unsigned int), cudaMemcpyDeviceToHost, h->active));
   GBBA_CUDA(cudaStreamSynchronize(h->active));
-  GBBA_REQUIRE(herr == 0, GBBA_ERROR_INVALID_ARGUMENT, "camera_index out of range");
+  GBBA_REQUIRE((*hp & 1u) == 0, GBBA_ERROR_INVALID_ARGUMENT, "track_offsets must start at 0 and be non-decreasing");
+  GBBA_REQUIRE((*hp & 2u) == 0, GBBA_ERROR_INVALID_ARGUMENT, "camera_index out of range");
 }
+
+// Device time of the call's main kernel, kept in the handle (gbba_last_kernel_time).
+struct KernelTimer {
+  gbba_handle* h;
+  explicit KernelTimer(gbba_handle* hh) : h(hh) { GBBA_CUDA(cudaEventRecord(h->ev_k0, h->active)); }
+  void stop() {
+    GBBA_CUDA(cudaEventRecord(h->ev_k1, h->active));
+    h->kernel_timed = true;
+  }
+};
 
 }  // namespace
 
@@ -434,10 +439,7 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
     return GBBA_ERROR_INVALID_ARGUMENT;
   return tri_guard(h, [&]() {
     if (num_tracks == 0) return GBBA_SUCCESS;
-    int64_t no = 0;
-    int max_len = 0;
-    check_offsets(h, track_offsets, num_tracks, memory, &no, &max_len);
-    (void)max_len;  // any track length: the N-view reduction keeps O(1) state per track
+    const int64_t no = host_total(track_offsets, num_tracks, memory);
     h->arena.reset();
     const int xo = method == 2 ? 3 : 4;
     h->arena.reserve(sizeof(double) * (12 * num_cameras + 2 * no + (xo + 1) * num_tracks) + sizeof(int64_t) * (num_tracks + 1) +
@@ -448,13 +450,15 @@ gbba_status gbtri_nview_batched(gbba_handle* h, int32_t method, const double* P,
     const double* dxy = in_view(h, xy, 2 * no, memory);
     double* dX = out_view(h, X, xo * num_tracks, memory);
     double* derr = out_view(h, error, num_tracks, memory);
-    check_cams(h, dcam, no, num_cameras);
+    const unsigned int* bad = launch_check(h, doff, num_tracks, dcam, num_cameras);
+    KernelTimer timer(h);
     k_nview64<<<std::max(1, std::min<int>((int)ceil_div(num_tracks, 128), h->sm_count * 16)), 128, 0, h->active>>>(
-        method, dP, doff, dcam, dxy, num_tracks, dX, method == GBTRI_ITERATIVE ? derr : nullptr);
+        method, dP, doff, dcam, dxy, num_tracks, dX, method == GBTRI_ITERATIVE ? derr : nullptr, bad);
+    timer.stop();
     check_launch(h);
     out_back(h, X, dX, xo * num_tracks, memory);
     if (method == GBTRI_ITERATIVE) out_back(h, error, derr, num_tracks, memory);
-    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    finish_check(h, bad);
     return GBBA_SUCCESS;
   });
 }
@@ -468,9 +472,7 @@ gbba_status gbtri_nview_batched_f32(gbba_handle* h, int32_t method, const float*
   if (num_tracks >= 0xFFFFFFFFLL) return GBBA_ERROR_TOO_LARGE;
   return tri_guard(h, [&]() {
     if (num_tracks == 0) return GBBA_SUCCESS;
-    int64_t no = 0;
-    int max_len = 0;
-    check_offsets(h, track_offsets, num_tracks, memory, &no, &max_len);
+    const int64_t no = host_total(track_offsets, num_tracks, memory);
     h->arena.reset();
     h->arena.reserve(sizeof(float) * (12 * num_cameras + 2 * no + 4 * num_tracks) + sizeof(uint32_t) * (num_tracks + 1 + no) +
                      num_tracks + 16 * 256);
@@ -481,19 +483,22 @@ gbba_status gbtri_nview_batched_f32(gbba_handle* h, int32_t method, const float*
     float* dX = out_view(h, X, 3 * num_tracks, memory);
     uint8_t* dst = out_view(h, status, num_tracks, memory);
     float* dmd = out_view(h, min_depth, num_tracks, memory);
-    check_cams(h, dcam, no, num_cameras);
+    const unsigned int* bad = launch_check(h, doff, num_tracks, dcam, num_cameras);
     const size_t smem = tri_f32_smem(num_cameras);
     static PerDeviceOnce once;
     once.run([] {
       GBBA_CUDA(cudaFuncSetAttribute(k_tri_f32, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tri_f32_smem(kTriCams)));
     });
+    KernelTimer timer(h);
     k_tri_f32<<<(unsigned)ceil_div(num_tracks, kTriThreads), kTriThreads, smem, h->active>>>(
-        method, dP, num_cameras, doff, dcam, reinterpret_cast<const float2*>(dxy), num_tracks, gn_steps, dX, dst, dmd);
+        method, dP, num_cameras, doff, dcam, reinterpret_cast<const float2*>(dxy), num_tracks, gn_steps, dX, dst, dmd,
+        bad);
+    timer.stop();
     check_launch(h);
     out_back(h, X, dX, 3 * num_tracks, memory);
     out_back(h, status, dst, num_tracks, memory);
     out_back(h, min_depth, dmd, num_tracks, memory);
-    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    finish_check(h, bad);
     return GBBA_SUCCESS;
   });
 }
@@ -504,9 +509,7 @@ gbba_status gbtri_refine_gn(gbba_handle* h, const double* P, int64_t num_cameras
   if (num_tracks < 0 || steps < 0 || !P || !track_offsets || !X) return GBBA_ERROR_INVALID_ARGUMENT;
   return tri_guard(h, [&]() {
     if (num_tracks == 0) return GBBA_SUCCESS;
-    int64_t no = 0;
-    int max_len = 0;
-    check_offsets(h, track_offsets, num_tracks, memory, &no, &max_len);
+    const int64_t no = host_total(track_offsets, num_tracks, memory);
     h->arena.reset();
     h->arena.reserve(sizeof(double) * (12 * num_cameras + 2 * no + 3 * num_tracks) + sizeof(int64_t) * (num_tracks + 1) +
                      sizeof(uint32_t) * no + 16 * 256);
@@ -515,12 +518,14 @@ gbba_status gbtri_refine_gn(gbba_handle* h, const double* P, int64_t num_cameras
     const uint32_t* dcam = in_view(h, camera_index, no, memory);
     const double* dxy = in_view(h, xy, 2 * no, memory);
     double* dX = const_cast<double*>(in_view(h, (const double*)X, 3 * num_tracks, memory));
-    check_cams(h, dcam, no, num_cameras);
+    const unsigned int* bad = launch_check(h, doff, num_tracks, dcam, num_cameras);
+    KernelTimer timer(h);
     k_refine_gn64<<<std::max(1, std::min<int>((int)ceil_div(num_tracks, 128), h->sm_count * 16)), 128, 0, h->active>>>(
-        dP, doff, dcam, dxy, num_tracks, steps, dX);
+        dP, doff, dcam, dxy, num_tracks, steps, dX, bad);
+    timer.stop();
     check_launch(h);
     out_back(h, X, dX, 3 * num_tracks, memory);
-    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    finish_check(h, bad);
     return GBBA_SUCCESS;
   });
 }

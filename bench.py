@@ -17,16 +17,20 @@ Metric: observations x LM iterations per second (higher is better).
              refined parameters are inside the timed region.
   roofline   the Schur elimination phase (the HBM-bound kernels that build
              S: point records, camera-pair products, merges, camera rhs):
-             its algorithmic bytes per execution / its event-timed duration.
-  factor_roofline  the dense FP32 Cholesky of S (a latency-bound chain of
-             64-wide panels): n^3/3 flops / its event-timed duration against
-             the FP32 SIMT peak.
-  time_to_cost  plain FP64 GPU path run to convergence (ceres's stopping
-             rule) gives C*; the mixed path with the same options and no
-             FP64 polish is timed to its final cost and checked against
-             (1+1e-6) C*.  The mixed run finished by its FP64 polish (at most
-             10 iterations, each a plain-FP64 iteration) is reported beside
-             it.
+             compulsory bytes per execution / its event-timed duration, with
+             compulsory bytes N_o (2s + 4 + 3 p_c s) + N_p 9s + nnzb(S) p_c^2 s
+             (s = 4 B, p_c = 12, nnzb(S) = covisible camera-pair blocks).
+  factor_roofline  the dense FP32 Cholesky of S: n^3/3 flops / its
+             event-timed duration.
+  time_to_cost  C* = final cost of the plain FP64 GPU path with ceres's
+             stopping rule; every solver's time to (1+1e-6) C* is read from
+             its per-iteration cost/time trace (first iteration at or below
+             the target); a tight-tolerance FP64 run shows how far C* is
+             from the minimum.
+  triangulation  the batched FP32 triangulation (1,000,000 tracks): the
+             whole call, and the main kernel's compulsory bytes over its
+             device time (gbba_last_kernel_time) as a roofline fraction.
+  batched    gbba_solve_batched on the 4,096 local-BA windows.
   cpu_baseline  the CPU oracle (restatement of ceres LM + dense Schur,
              OpenMP over the host cores) on a bounded sample: 1 LM iteration.
 
@@ -53,24 +57,35 @@ METRIC = "BA obs x LM-iterations per second (mixed-precision GB300 path), time-t
 UNIT = "obs*iter/s"
 
 
-def algorithmic_schur_bytes(no, np_, n_red, p_c, s):
-    """Compulsory DRAM bytes of one Schur-elimination phase (one LM iteration).
+def covisible_blocks(point_index, camera_index, num_cameras):
+    """nnzb(S): camera-pair blocks (a >= b) that share at least one point,
+    diagonal blocks included."""
+    pt = np.asarray(point_index, np.int64)
+    cam = np.asarray(camera_index, np.int64)
+    order = np.argsort(pt, kind="stable")
+    pt, cam = pt[order], cam[order]
+    seg_start = np.r_[0, np.flatnonzero(np.diff(pt)) + 1]
+    first = np.repeat(seg_start, np.diff(np.r_[seg_start, len(pt)]))
+    cnt = np.arange(len(pt)) - first + 1  # partners j <= i inside the point's segment
+    a = np.repeat(np.arange(len(pt)), cnt)
+    b = np.repeat(first, cnt) + (np.arange(cnt.sum()) - np.repeat(np.cumsum(cnt) - cnt, cnt))
+    ca, cb = cam[a], cam[b]
+    key = np.maximum(ca, cb) * num_cameras + np.minimum(ca, cb)
+    seen = np.zeros(num_cameras * num_cameras, bool)
+    seen[key] = True
+    return int(seen.sum())
 
-    The phase is k_schur_point_rec (one warp per point: Jacobian, V, V^-1,
-    per-observation records), k_schur_pairs + k_pair_merge (the camera-pair
-    products W_a^T V^-1 W_b, summed in a fixed order) and k_rhs_camera.
-    Reads: observations (x,y FP64 = 16 B) + camera/intrinsic/point index
-    (3 x 4 B) per observation; point parameters (24 B), Jacobi scale and LM
-    diagonal (2 x 3 x 8 B) and CSR offset (4 B) per point; camera-side
-    parameters (p_c x 8 B per camera).  Writes: the per-observation record
-    (Jc 2p_c, W 3p_c, W V^-1 3p_c, q p_c, Jp 6, r 2 values = 9p_c + 8) and
-    V^-1, g_p (9 values) per point; the lower triangle of S (n^2/2) and rhs
-    (n).  The pair products read W and W V^-1 of every observation once
-    (6 p_c values).  s = bytes per value of the phase's arithmetic type."""
-    n_cam = n_red // p_c if p_c else 0
-    reads = no * (16 + 12) + np_ * (24 + 48 + 4) + n_cam * p_c * 8 + no * 6 * p_c * s
-    writes = no * (9 * p_c + 8) * s + np_ * 9 * s + (n_red * n_red // 2) * s + n_red * s
-    return reads + writes
+
+def algorithmic_schur_bytes(no, np_, nnzb, p_c, s):
+    """Compulsory DRAM bytes of one Schur-elimination phase (one LM iteration),
+    the unit of work being one observation in one LM iteration:
+        N_o (2s obs + 4 index + 3 p_c s W block written)
+      + N_p (3s point + 6s symmetric V^-1)
+      + nnzb(S) p_c^2 s  (the camera-pair blocks of S written once)
+    s = bytes per value of the phase's arithmetic type (4 for the mixed path);
+    everything else the implementation reads or writes (its per-observation
+    records, partial sums, re-reads) is traffic, not algorithmic bytes."""
+    return no * (2 * s + 4 + 3 * p_c * s) + np_ * (3 * s + 6 * s) + nnzb * p_c * p_c * s
 
 
 def factor_flops(n_red):
@@ -78,10 +93,12 @@ def factor_flops(n_red):
     return n_red ** 3 / 3.0 + 2.0 * n_red ** 2
 
 
-# DRAM bytes (read + write) of one Schur phase on the medium workload: ncu's
-# dram__bytes_read.sum + dram__bytes_write.sum summed over the phase's four
-# kernels (profiles/schur_phase_medium.md).
-SCHUR_TRAFFIC_PER_PHASE = 4.96e9
+# DRAM bytes (read + write) per observation of one Schur phase, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum summed over the
+# phase's kernels) of the current kernels on the medium workload; multiplied
+# by the observation count (the phase's traffic grows with the observations).
+SCHUR_TRAFFIC_PER_OBS = None
+SCHUR_TRAFFIC_SOURCE = "not captured for the current kernels"
 
 # FP32 SIMT peak of a GB300: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
@@ -186,7 +203,7 @@ def tri_algorithmic_bytes(no, nt):
     return no * (8 + 4) + nt * (4 + 12 + 1 + 4)
 
 
-def measure_triangulation(h, torch, steps, warmup):
+def measure_triangulation(h, torch, steps, warmup, peak):
     """The batched-triangulation workload (1,000,000 tracks, 200 cameras,
     lengths 2-30, FP32 linear N-view + 1 Gauss-Newton step), device-resident."""
     scenes = importlib.import_module("3dreconstruction_gb300.scenes")
@@ -212,7 +229,7 @@ def measure_triangulation(h, torch, steps, warmup):
     for _ in range(warmup):
         run()
     torch.cuda.synchronize()
-    times = []
+    times, ktimes = [], []
     for _ in range(steps):
         flush.zero_()  # evict L2 between timed launches
         e0 = torch.cuda.Event(enable_timing=True)
@@ -223,12 +240,21 @@ def measure_triangulation(h, torch, steps, warmup):
         e1.record(stream)
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1) / 1e3)
+        kt = ctypes.c_double()
+        h.check(h.lib.gbba_last_kernel_time(h.h, ctypes.byref(kt)), "gbba_last_kernel_time")
+        ktimes.append(kt.value)
     t = float(np.median(times))
+    kt = float(np.median(ktimes))
     ok = float((st == 0).float().mean().item())
-    return {"workload": "tracks1m: 1,000,000 tracks, 200 cameras, lengths U{2..30}, FP32 linear + 1 GN step",
+    alg = tri_algorithmic_bytes(no, nt)
+    return {"workload": "tracks1m: 1,000,000 tracks, 200 cameras, lengths U{2..30}, FP32 N-view + 1 GN step",
             "tracks_per_s": nt / t, "obs_per_s": no / t, "ms_per_call": t * 1e3,
-            "note": "whole C-ABI call incl. offset validation on the host; device-resident inputs, L2 flushed",
-            "algorithmic_bytes": tri_algorithmic_bytes(no, nt), "tracks_ok_frac": ok}
+            "note": "whole C-ABI call (input check kernel, triangulation kernel, status read-back); "
+                    "device-resident inputs, L2 flushed between calls",
+            "algorithmic_bytes": alg, "tracks_ok_frac": ok,
+            "roofline": {"kernel": "k_tri_f32", "bound": "hbm", "achieved": alg / kt / 1e9, "peak": peak,
+                         "unit": "GB/s", "frac": alg / kt / 1e9 / peak, "kernel_ms": kt * 1e3,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}}
 
 
 def _local_window(args):
@@ -245,8 +271,8 @@ def measure_batched(h, abi, windows, seed=4):
     checked window by window against (1 + 1e-6) C*: with function tolerance
     1e-8 and at most 200 iterations (the time-to-cost run: in the flat valleys
     of some windows the 1e-6 rule stops a solver anywhere in a band a few 1e-6
-    wide, so the mixed run converges further), and with the FP64 run's own
-    settings for comparison.  Times are whole C-ABI calls from host buffers."""
+    wide, so the mixed run converges further).
+    Times are whole C-ABI calls from host buffers."""
     import multiprocessing as mp
     t0 = time.perf_counter()
     with mp.get_context("spawn").Pool(min(16, os.cpu_count() or 1)) as pool:
@@ -273,12 +299,74 @@ def measure_batched(h, abi, windows, seed=4):
     out = {"workload": f"local{windows}: {windows} windows, cameras U{{5..40}}, points U{{200..5000}}, Brown-T2, "
                        "one intrinsic group, cameras 0 and 1 held",
            "observations": int(nobs.sum()), "generation_s": gen_s, "fp64": fp64}
-    for name, ftol, iters in (("mixed", 1e-8, 200), ("mixed_fp64_stopping_rule", 1e-6, 100)):
+    for name, ftol, iters in (("mixed", 1e-8, 200),):
         r, costs = run(abi.PRECISION_MIXED, ftol, iters)
         r["function_tolerance"], r["max_num_iterations"] = ftol, iters
         r["reaches_cstar_frac"] = float(np.mean(costs <= cstar * (1 + 1e-6)))
         r["speedup_vs_fp64"] = fp64["seconds"] / r["seconds"]
         out[name] = r
+    return out
+
+
+def trace_time_to(trace_cost, trace_time, n, target):
+    """Wall time of the first traced iteration whose cost is <= target, or None."""
+    for i in range(n):
+        if trace_cost[i] <= target:
+            return float(trace_time[i])
+    return None
+
+
+def time_to_cost(h, abi, scene, dp, pristine, st, sptr, max_iters):
+    """Time to cost as the wall time until cost <= (1 + 1e-6) C*, with C* the
+    final cost of the plain FP64 GPU path run with ceres's stopping rule
+    (function tolerance 1e-6).  Every solve records its cost and wall time
+    after each LM iteration (gbba_options.trace_*), and each solver's time is
+    the first traced time at or below the target.  A plain FP64 run with a
+    1e-10 function tolerance gives the tight minimum, so that the distance of
+    C* from the minimum is visible."""
+    import torch
+    cap = max_iters + 2
+    out = {}
+    runs = (("fp64", abi.PRECISION_FP64, 0, 1e-6), ("fp64_tight", abi.PRECISION_FP64, 0, 1e-10),
+            ("mixed", abi.PRECISION_MIXED, 0, 1e-6), ("mixed_fp64_polish", abi.PRECISION_MIXED, 10, 1e-6))
+    traces = {}
+    for name, prec, polish, ftol in runs:
+        for f, v in pristine.items():
+            getattr(dp, f).copy_(v)
+        o = solve_options(scene, max_iters, prec, stream=sptr, tol=True)
+        o.fp64_polish_iterations = polish
+        o.function_tolerance = ftol
+        tc, tt = np.zeros(cap), np.zeros(cap)
+        o.trace_cost, o.trace_time_s, o.trace_capacity = tc.ctypes.data, tt.ctypes.data, cap
+        summ = abi.GbbaSummary()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.check(h.lib.gbba_solve(h.h, ctypes.byref(st), ctypes.byref(o), ctypes.byref(summ)), "time to cost")
+        torch.cuda.synchronize()
+        out[name] = {"seconds": time.perf_counter() - t0, "final_cost": summ.final_cost,
+                     "iterations": summ.num_iterations, "termination": summ.termination_type,
+                     "function_tolerance": ftol}
+        traces[name] = (tc, tt, min(cap, summ.num_iterations + 1))
+    cstar = out["fp64"]["final_cost"]
+    target = cstar * (1 + 1e-6)
+    out["c_star"] = cstar
+    out["target"] = target
+    out["c_star_above_tight_minimum"] = cstar / out["fp64_tight"]["final_cost"] - 1.0
+    for name in ("fp64", "fp64_tight", "mixed"):
+        tc, tt, n = traces[name]
+        out[name]["time_to_target_s"] = trace_time_to(tc, tt, n, target)
+    # the polished run's last iterations are the FP64 polish, which is not
+    # traced: its time to target is its whole wall time when it ends there
+    out["mixed_fp64_polish"]["time_to_target_s"] = (out["mixed_fp64_polish"]["seconds"]
+                                                    if out["mixed_fp64_polish"]["final_cost"] <= target else None)
+    t64 = out["fp64"]["time_to_target_s"]
+    for name in ("mixed", "mixed_fp64_polish"):
+        tm = out[name]["time_to_target_s"]
+        out[name]["reaches_target"] = tm is not None
+        out[name]["speedup_vs_fp64"] = (t64 / tm) if (t64 and tm) else None
+    out["speedup"] = out["mixed"]["speedup_vs_fp64"]
+    out["definition"] = ("wall time (setup included) until the accepted cost first reaches (1 + 1e-6) C*, "
+                         "C* = final cost of plain FP64 with ceres's stopping rule; per-iteration trace")
     return out
 
 
@@ -438,7 +526,9 @@ def run_ours(args):
             pass
         peak = float(peaks.get("hbm_gbs", 6800.0))
         p_c = 12
-        alg = algorithmic_schur_bytes(no, len(scene["points"]), n_red, p_c, 4)
+        nnzb = covisible_blocks(scene["point_index"], scene["camera_index"], len(scene["extrinsics"]))
+        alg = algorithmic_schur_bytes(no, len(scene["points"]), nnzb, p_c, 4)
+        traffic = SCHUR_TRAFFIC_PER_OBS * no if SCHUR_TRAFFIC_PER_OBS else None
         per_phase_s = schur_t / max(1, iters)
         achieved = alg / per_phase_s / 1e9
         per_factor_s = factor_t / max(1, iters)
@@ -462,8 +552,10 @@ def run_ours(args):
                          "frac": achieved / peak,
                          "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback",
                          "algorithmic_bytes_per_launch": alg, "launch_ms": per_phase_s * 1e3,
+                         "algorithmic_inputs": {"observations": no, "points": len(scene["points"]),
+                                                "covisible_blocks": nnzb, "p_c": p_c, "bytes_per_value": 4},
                          "kernel_launches_per_phase": int(phase_launches),
-                         "traffic": SCHUR_TRAFFIC_PER_PHASE},
+                         "traffic": traffic, "traffic_source": SCHUR_TRAFFIC_SOURCE},
             "factor_roofline": {"kernel": "dense Cholesky of S + triangular solves (FP32, blocked, NB=64)",
                                 "bound": "fp32 simt", "achieved": ff / per_factor_s / 1e12,
                                 "peak": FP32_SIMT_TFLOPS, "unit": "TFLOP/s",
@@ -473,28 +565,9 @@ def run_ours(args):
         }
     # ---- time to cost: plain FP64 GPU to convergence (C*), mixed to (1+1e-6) C*
     if args.time_to_cost and rank == 0:
-        ttc = {}
-        for name, prec, polish in (("fp64", abi.PRECISION_FP64, 0), ("mixed", abi.PRECISION_MIXED, 0),
-                                   ("mixed_fp64_polish", abi.PRECISION_MIXED, 10)):
-            for f, v in pristine.items():
-                getattr(dp, f).copy_(v)
-            o = solve_options(scene, args.ttc_iters, prec, stream=sptr, tol=True)
-            o.fp64_polish_iterations = polish
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            h.check(h.lib.gbba_solve(h.h, ctypes.byref(st), ctypes.byref(o), ctypes.byref(summ)), "ttc")
-            torch.cuda.synchronize()
-            ttc[name] = {"seconds": time.perf_counter() - t0, "final_cost": summ.final_cost,
-                         "iterations": summ.num_iterations, "termination": summ.termination_type}
-        cstar = ttc["fp64"]["final_cost"]
-        for name in ("mixed", "mixed_fp64_polish"):
-            ttc[name]["reaches_cstar"] = bool(ttc[name]["final_cost"] <= cstar * (1 + 1e-6))
-            ttc[name]["speedup"] = ttc["fp64"]["seconds"] / ttc[name]["seconds"]
-        ttc["mixed_reaches_cstar"] = ttc["mixed"]["reaches_cstar"]
-        ttc["speedup"] = ttc["mixed"]["speedup"]
-        line["time_to_cost"] = ttc
+        line["time_to_cost"] = time_to_cost(h, abi, scene, dp, pristine, st, sptr, args.ttc_iters)
     if rank == 0 and args.triangulation:
-        line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup)
+        line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup, peak)
     if rank == 0 and args.batched_windows > 0:
         line["batched"] = measure_batched(h, abi, args.batched_windows)
     if rank == 0 and args.cpu_baseline:
@@ -519,7 +592,7 @@ def main():
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")
-    ap.add_argument("--batched-windows", type=int, default=512,
+    ap.add_argument("--batched-windows", type=int, default=4096,
                     help="windows of the batched local-BA measurement (0: skip)")
     args = ap.parse_args()
     if args.warmup < 3:

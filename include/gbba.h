@@ -154,6 +154,16 @@ typedef struct gbba_options {
                                              LM iterations continue from its solution with function and
                                              parameter tolerances 1000x tighter (0 = off): 10 */
   int32_t schur_build;                    /* gbba_schur_build: GBBA_SCHUR_BUILD_AUTO */
+  /* Optional per-iteration trace, host memory (NULL = off): entry i holds the
+   * cost at the accepted parameters after LM iteration i (entry 0: the
+   * initial cost; ceres's IterationSummary::cost) and the wall time in
+   * seconds since the call began, setup included.  At most trace_capacity
+   * entries are written (summary.num_iterations + 1 when they fit); the
+   * iterations of the optional FP64 polish are not traced. */
+  double* trace_cost;
+  double* trace_time_s;
+  int32_t trace_capacity;
+  int32_t trace_reserved;
 } gbba_options;
 
 typedef struct gbba_summary {
@@ -189,6 +199,11 @@ const char* gbba_status_string(gbba_status status);
 int gbba_abi_version(void);
 /* Number of CUDA kernel launches issued through this handle so far. */
 int64_t gbba_launch_count(const gbba_handle* handle);
+/* Device time (CUDA events on the call's stream) of the main kernel of the
+ * handle's last triangulation call (gbtri_*), without its input check and
+ * copies; GBBA_ERROR_NOT_SUPPORTED before any such call.  No counterpart in
+ * the reference, which has no device kernels: it serves roofline accounting. */
+gbba_status gbba_last_kernel_time(gbba_handle* handle, double* seconds);
 
 /* Refine extrinsics, intrinsics and points in place: the replacement of
  * ceres::Solve with SPARSE_SCHUR/DENSE_SCHUR on the reference problems.

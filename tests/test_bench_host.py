@@ -33,16 +33,26 @@ def test_clock_record_without_samples_is_none():
     assert bench.ClockSampler.summarize(["[N/A], [N/A]\n"]) is None
 
 
-def test_algorithmic_schur_bytes_counts_each_stream_once():
-    # one observation, one point, one camera with p_c = 12, n = 12, FP32
-    no, np_, n, p_c, s = 1, 1, 12, 12, 4
-    reads = no * (16 + 12) + np_ * (24 + 48 + 4) + 1 * p_c * 8 + no * 6 * p_c * s
-    writes = no * (9 * p_c + 8) * s + np_ * 9 * s + (n * n // 2) * s + n * s
-    assert bench.algorithmic_schur_bytes(no, np_, n, p_c, s) == reads + writes
-    # linear in the observations at a fixed camera system
+def test_algorithmic_schur_bytes_follow_the_survey_formula():
+    # N_o (2s + 4 + 3 p_c s) + N_p (3s + 6s) + nnzb(S) p_c^2 s
+    no, np_, nnzb, p_c, s = 1_999_428, 200_000, 125_250, 12, 4
+    expect = no * (2 * s + 4 + 3 * p_c * s) + np_ * 9 * s + nnzb * p_c * p_c * s
+    assert bench.algorithmic_schur_bytes(no, np_, nnzb, p_c, s) == expect
+    assert abs(expect - 0.3912e9) < 0.001e9  # the medium workload's 0.391 GB
     a = bench.algorithmic_schur_bytes(1000, 100, 600, 12, 4)
     b = bench.algorithmic_schur_bytes(2000, 100, 600, 12, 4)
-    assert b - a == 1000 * (16 + 12 + 6 * 12 * 4 + (9 * 12 + 8) * 4)
+    assert b - a == 1000 * (8 + 4 + 3 * 12 * 4)
+
+
+def test_covisible_blocks_counts_camera_pairs_once():
+    # point 0 seen by cameras 0, 2, 3; point 1 by 2, 3; point 2 by 1
+    pt = [0, 0, 0, 1, 1, 2]
+    cam = [0, 2, 3, 2, 3, 1]
+    # diagonal (0,0) (1,1) (2,2) (3,3) + (2,0) (3,0) (3,2)
+    assert bench.covisible_blocks(pt, cam, 4) == 7
+    # order of the observations does not matter
+    perm = [5, 3, 0, 4, 1, 2]
+    assert bench.covisible_blocks([pt[i] for i in perm], [cam[i] for i in perm], 4) == 7
 
 
 def test_factor_flops():

@@ -222,3 +222,21 @@ def test_refine_gn_fp64(handle, abi, scenes, oracle_mod):
                                             xy.ctypes.data, len(off) - 1, 2, X.ctypes.data, abi.MEMORY_HOST), "gn")
     X2, _, _ = oracle_mod.tri_linear_gn(tr["P"], tr["track_offsets"], tr["camera_index"], tr["xy"], 2)
     np.testing.assert_allclose(X, X2, atol=1e-9)
+
+
+def test_invalid_tracks_rejected(handle, abi):
+    """Decreasing offsets and out-of-range camera indices are reported as
+    invalid arguments; the check kernel runs before the triangulation kernel,
+    which then reads nothing of the batch."""
+    P = np.tile(np.eye(3, 4).ravel(), (3, 1))
+    xy = np.zeros((6, 2))
+    cam = np.array([0, 1, 2, 0, 1, 2], np.uint32)
+    st, _, _ = nview(handle, abi, abi.TRI_NVIEW, P, np.array([0, 5, 3, 6]), cam, xy)
+    assert st == abi.ERROR_INVALID_ARGUMENT
+    bad = cam.copy()
+    bad[4] = 7
+    st, _, _ = nview(handle, abi, abi.TRI_ITERATIVE, P, np.array([0, 3, 6]), bad, xy)
+    assert st == abi.ERROR_INVALID_ARGUMENT
+    tr = {"P": P, "track_offsets": np.array([0, 3, 6]), "camera_index": bad, "xy": xy}
+    with pytest.raises(Exception):
+        f32_path(handle, abi, tr)
