@@ -19,7 +19,10 @@
 // then the backward substitution L^T x = y, right-looking by block rows:
 //   trsv_bwd(k): x_k = L_kk^-T y_k; y_j -= L_kj^T x_k for j < k.
 // A non-positive pivot sets *flag (LINEAR_SOLVER_FAILURE in ceres terms).
+#include <type_traits>
+
 #include "gbba_internal.h"
+#include "gbba_umma.cuh"
 
 namespace gbba {
 
@@ -549,6 +552,57 @@ __global__ void __launch_bounds__(256) k_syrk_wide(T* __restrict__ S, int64_t ld
     }
 }
 
+// The same trailing update on the tensor cores (FP32 path): one CTA per
+// 128 x 128 output tile of the same enumeration as k_syrk_wide, acc = X_i X_j^T
+// over the panel's 64 columns by tcgen05 kind::tf32 MMAs in 3xTF32 (FP32
+// accuracy), accumulated in tensor memory; the epilogue subtracts it from S.
+// Rows of a tile beyond the matrix edge are staged as zeros and not stored;
+// quarters above the diagonal are not stored.  A bounded wait that runs out
+// sets *flag = 6 (the step is then rejected) and the tile is left alone.
+constexpr int kSyrkTcThreads = 256;
+__global__ void __launch_bounds__(kSyrkTcThreads) k_syrk_tc(float* __restrict__ S, int64_t ld, int kb, int first,
+                                                            int nb, int* __restrict__ flag) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  umma::GemmSmem& g = *reinterpret_cast<umma::GemmSmem*>(smem_raw);
+  const int64_t t = blockIdx.x;
+  int64_t R = (int64_t)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while ((R + 1) * (R + 2) / 2 <= t) ++R;
+  while (R * (R + 1) / 2 > t) --R;
+  const int64_t C = t - R * (R + 1) / 2;
+  const int64_t ib0 = first + 2 * R, jb0 = first + 2 * C;
+  const int rows_i = ib0 + 1 < nb ? 2 * NB : NB, rows_j = jb0 + 1 < nb ? 2 * NB : NB;
+  const int64_t c0 = (int64_t)kb * NB;
+  umma::gemm_setup(g, 128);
+  const bool ok = umma::gemm_tile<kSyrkTcThreads>(g, 0, S + ib0 * NB * ld + c0, ld, S + jb0 * NB * ld + c0, ld, NB / umma::kChunk,
+                                  rows_i, rows_j);
+  if (ok) {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = 32 * (w & 3) + lane;       // tile row = tensor-memory lane
+    const int qj = w >> 2;                   // column half: 64-tile jb0 + qj
+    const int64_t rb = ib0 + (r >> 6), cb = jb0 + qj;
+    if (rb < nb && cb < nb && rb >= cb) {
+      float* row = S + (rb * NB + (r & 63)) * ld + cb * NB;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float v[32];
+        umma::tmem_ld32(g.tmem_base + ((uint32_t)(32 * (w & 3)) << 16) + 64 * qj + 32 * h, v);
+#pragma unroll
+        for (int e = 0; e < 32; e += 4) {
+          float4 c = *reinterpret_cast<float4*>(row + 32 * h + e);
+          c.x -= v[e];
+          c.y -= v[e + 1];
+          c.z -= v[e + 2];
+          c.w -= v[e + 3];
+          *reinterpret_cast<float4*>(row + 32 * h + e) = c;
+        }
+      }
+    }  // (the condition is uniform over a warp, as the warp-collective tcgen05.ld requires)
+  } else if (threadIdx.x == 0) {
+    atomicExch(flag, 6);
+  }
+  umma::gemm_teardown(g, 128);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64_t ld, int kb, const T* __restrict__ Linv_all,
                                                   T* __restrict__ b, T* __restrict__ x) {
@@ -602,6 +656,9 @@ void dense_cholesky_prepare() {
     GBBA_CUDA(cudaFuncSetAttribute(k_trsv_bwd<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
     GBBA_CUDA(cudaFuncSetAttribute(k_syrk_wide<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)wide_smem_bytes<T>()));
+    if (std::is_same<T, float>::value)
+      GBBA_CUDA(cudaFuncSetAttribute(k_syrk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(umma::GemmSmem)));
   });
 }
 
@@ -645,8 +702,11 @@ void launch_hi(gbba_handle* h, bool pdl, void (*k)(Exp...), unsigned grid, unsig
 // column k+1), and the side stream starts step k once panel k is solved.
 // The side stream is joined back before the backward substitution, so the
 // sequence can be captured.
-template <typename T>
-void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st) {
+// kTensor: the trailing update on the tensor cores (k_syrk_tc, FP32 only) or
+// on the FP32/FP64 pipes (k_syrk_wide).
+template <typename T, bool kTensor>
+void dense_cholesky_solve_impl(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag,
+                               cudaStream_t st) {
   const int nb = (int)(n_pad / NB);
   const size_t sm = dense_smem_bytes<T>(), psm = potrf_smem_bytes<T>();
   dense_cholesky_prepare<T>();
@@ -664,7 +724,11 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
       GBBA_CUDA(cudaEventRecord(h->ev_main, st));
       GBBA_CUDA(cudaStreamWaitEvent(h->side, h->ev_main, 0));
       const int64_t tw = rem / 2;  // 128-tiles per side over the 64-tiles k+2..nb-1
-      k_syrk_wide<T><<<(unsigned)(tw * (tw + 1) / 2), 256, wide_smem_bytes<T>(), h->side>>>(S, n_pad, k, k + 2, nb);
+      if constexpr (kTensor)
+        k_syrk_tc<<<(unsigned)(tw * (tw + 1) / 2), kSyrkTcThreads, sizeof(umma::GemmSmem), h->side>>>(
+            S, n_pad, k, k + 2, nb, flag);
+      else
+        k_syrk_wide<T><<<(unsigned)(tw * (tw + 1) / 2), 256, wide_smem_bytes<T>(), h->side>>>(S, n_pad, k, k + 2, nb);
       check_launch(h);
       GBBA_CUDA(cudaEventRecord(h->ev_side, h->side));
       side_pending = true;
@@ -681,6 +745,13 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
   }
 }
 
+template <typename T>
+void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st) {
+  dense_cholesky_solve_impl<T, std::is_same<T, float>::value>(h, S, n_pad, b, x, Linv_all, flag, st);
+}
+
+template void dense_cholesky_solve_impl<float, false>(gbba_handle*, float*, int64_t, float*, float*, float*, int*,
+                                                      cudaStream_t);
 template void dense_cholesky_prepare<double>();
 template void dense_cholesky_prepare<float>();
 template void dense_cholesky_solve<double>(gbba_handle*, double*, int64_t, double*, double*, double*, int*, cudaStream_t);

@@ -44,6 +44,9 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
 template <typename T>
 void dense_cholesky_prepare();
 
+// Tile width of the dense factorisation, which S's size is padded to.
+static int64_t dense_tile(int) { return 64; }
+
 static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -1853,7 +1856,7 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.S = a.template take<char>((size_t)n_s * n_s * tsize);
   s.rhs = a.template take<char>((size_t)s.n_pad * tsize);
   s.zsol = a.template take<char>((size_t)s.n_pad * tsize);
-  s.Linv = a.template take<char>((size_t)n_s * 64 * tsize);
+  s.Linv = a.template take<char>((size_t)n_s * dense_tile(s.precision) * tsize);
   s.Vinv = a.template take<char>((size_t)s.np * 6 * tsize);
   s.gpv = a.template take<char>((size_t)s.np * 3 * tsize);
   s.part_mcc = a.template take<double>(s.nb_pt);
@@ -1922,7 +1925,7 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   for (int64_t c = 0; c < nc; ++c) n_max += cc[c] ? 0 : free_e;
   for (int64_t g = 0; g < ni; ++g) n_max += ic[g] ? 0 : free_i;
   s.n_red = n_max;
-  s.n_pad = ceil_div(std::max<int64_t>(n_max, 1), 64) * 64;
+  s.n_pad = ceil_div(std::max<int64_t>(n_max, 1), dense_tile(s.precision)) * dense_tile(s.precision);
   s.dense = o->linear_solver == GBBA_SOLVER_DENSE_SCHUR ||
             (o->linear_solver == GBBA_SOLVER_AUTO && s.n_pad <= (int64_t)o->dense_schur_max_size + 64);
   s.nb_obs = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(no, 1), 256), h->sm_count * 8));
@@ -1992,7 +1995,7 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
       }
   }
   s.n_red = col;
-  s.n_pad = ceil_div(std::max<int64_t>(col, 1), 64) * 64;
+  s.n_pad = ceil_div(std::max<int64_t>(col, 1), dense_tile(s.precision)) * dense_tile(s.precision);
 
   // counting sort of observations by point (input order kept within a point)
   scan_offsets(h, counts, s.pt_off, np, chunks, st);
