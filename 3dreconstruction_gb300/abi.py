@@ -170,7 +170,7 @@ def default_options(**kw):
     o.max_linear_solver_iterations = 500
     o.dense_schur_max_size = 16384
     o.eta = 0.1
-    o.refinement_interval = 8
+    o.refinement_interval = 10
     o.use_cuda_graphs = 1
     o.stream = None
     o.fp64_polish_iterations = 10

@@ -45,7 +45,7 @@ template <typename T>
 void dense_cholesky_prepare();
 
 // Tile width of the dense factorisation, which S's size is padded to.
-static int64_t dense_tile(int) { return 64; }
+constexpr int64_t kDenseTile = 64;
 
 static double now_s() {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -1065,6 +1065,18 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
 // The operator data (W, V^-1, U) are in the compute type T, the PCG vectors
 // and every accumulation are FP64.
 
+// Scalars of the device-resident CG loop (see k_pcg_direction and the other
+// k_pcg_* kernels below).
+struct PcgState {
+  double rho[2];  // r.z of the iterations with even / odd number
+  double Q0;      // quadratic model of the previous iteration
+  double tol_r;   // |r| termination threshold (r_tolerance |b|; negative = off)
+  int it;         // iteration being run (1-based); the count when done
+  int done;       // nonzero: the loop has ended
+  int failure;    // LINEAR_SOLVER_FAILURE (rho, beta or alpha not usable)
+  int pad;
+};
+
 // Camera diagonal blocks U_c = sum Jc^T Jc, the preconditioner block
 // (U_c + D_c^2 - sum (W V^-1) W^T)^-1 (identity on held coordinates); one warp per camera.
 template <int B, typename T>
@@ -1158,10 +1170,12 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
                                                     const int32_t* __restrict__ ext_col,
                                                     const int32_t* __restrict__ intr_col,
                                                     const int32_t* __restrict__ cam_group, int K, int64_t np,
-                                                    const double* __restrict__ x, double* __restrict__ y) {
+                                                    const double* __restrict__ x, double* __restrict__ y,
+                                                    const PcgState* __restrict__ ps, int reset_period) {
   using R = Rec<B>;
   const int lane = threadIdx.x & 31;
   const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
   if (p >= np) return;
   double t[3] = {0.0, 0.0, 0.0};
   for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
@@ -1197,48 +1211,121 @@ __global__ void __launch_bounds__(128) k_spmv_camera(const uint32_t* __restrict_
                                                      const int32_t* __restrict__ cam_group, int K, int64_t nc,
                                                      const double* __restrict__ diag_c,
                                                      const double* __restrict__ radius, const double* __restrict__ x,
-                                                     const double* __restrict__ y, double* __restrict__ out) {
+                                                     const double* __restrict__ y, double* __restrict__ out,
+                                                     double* __restrict__ part, const PcgState* __restrict__ ps,
+                                                     int reset_period) {
   using R = Rec<B>;
-  const int lane = threadIdx.x & 31;
+  __shared__ double pdot[4];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (c >= nc) return;
-  double acc[B];
+  if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
+  double xo = 0.0;  // this lane's x . out (the partials of p.q)
+  if (c < nc) {
+    double acc[B];
 #pragma unroll
-  for (int i = 0; i < B; ++i) acc[i] = 0.0;
-  for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
-    const uint32_t o = cam_obs[q];
-    const T* r = rec + (int64_t)o * R::kSize;
-    const double* yp = y + 3 * (int64_t)pt[o];
-    const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
+    for (int i = 0; i < B; ++i) acc[i] = 0.0;
+    for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+      const uint32_t o = cam_obs[q];
+      const T* r = rec + (int64_t)o * R::kSize;
+      const double* yp = y + 3 * (int64_t)pt[o];
+      const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
 #pragma unroll
-    for (int i = 0; i < B; ++i)
-      acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
-  }
-#pragma unroll
-  for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
-  if (lane < B) {
-    double v = acc[0];
-#pragma unroll
-    for (int i = 1; i < B; ++i)
-      if (lane == i) v = acc[i];
-    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
-    if (ci >= 0) {
-      double u = diag_c[ci] / *radius * x[ci];
-      for (int j = 0; j < B; ++j) {
-        const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
-        if (cj >= 0) u += (double)U[c * B * B + lane * B + j] * x[cj];
-      }
-      out[ci] = v + u;
+      for (int i = 0; i < B; ++i)
+        acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
     }
+#pragma unroll
+    for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
+    if (lane < B) {
+      double v = acc[0];
+#pragma unroll
+      for (int i = 1; i < B; ++i)
+        if (lane == i) v = acc[i];
+      const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
+      if (ci >= 0) {
+        double u = diag_c[ci] / *radius * x[ci];
+        for (int j = 0; j < B; ++j) {
+          const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
+          if (cj >= 0) u += (double)U[c * B * B + lane * B + j] * x[cj];
+        }
+        out[ci] = v + u;
+        xo = x[ci] * (v + u);
+      }
+    }
+  }
+  if (!part) return;
+  xo = warp_sum(xo);
+  if (lane == 0) pdot[warp] = xo;
+  __syncthreads();
+  if (threadIdx.x == 0) part[blockIdx.x] = (pdot[0] + pdot[1]) + (pdot[2] + pdot[3]);
+}
+
+// ---- device-resident CG (ceres ConjugateGradientsSolver::Solve,
+// internal/ceres/conjugate_gradients_solver.cc:66-248): the scalars live in a
+// PcgState on the device, every kernel of an iteration returns at once when
+// `done` is set, and every reduction is a fixed-order sum of per-block
+// partials that each consuming block repeats, so no kernel needs the host.
+
+// Fixed-order sum over a block of 256 threads (result in every thread).
+__device__ __forceinline__ double block_sum256(double v, double* sh) {
+  v = warp_sum(v);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) t += sh[w];
+  return t;
+}
+// Sum of n per-block partials in a fixed order (every thread of a 256-thread block).
+__device__ __forceinline__ double sum_partials(const double* __restrict__ part, int n, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += 256) v += part[i];
+  return block_sum256(v, sh);
+}
+
+// b = rhs (widened), x = 0, r = b; partials of |b|^2.
+template <typename T>
+__global__ void __launch_bounds__(256) k_pcg_init(const T* __restrict__ rhs, double* __restrict__ b,
+                                                  double* __restrict__ x, double* __restrict__ r, int64_t n,
+                                                  double* __restrict__ part) {
+  __shared__ double sh[8];
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (double)rhs[i];
+    b[i] = v;
+    r[i] = v;
+    x[i] = 0.0;
+    acc += v * v;
+  }
+  acc = block_sum256(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+__global__ void __launch_bounds__(256) k_pcg_start(const double* __restrict__ part, int nb, double r_tolerance,
+                                                   PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  const double bb = sum_partials(part, nb, sh);
+  if (threadIdx.x == 0) {
+    ps->rho[0] = ps->rho[1] = 1.0;
+    ps->Q0 = 0.0;  // x = 0
+    ps->tol_r = r_tolerance * sqrt(bb);
+    ps->it = 1;
+    ps->failure = 0;
+    ps->done = bb > 0.0 ? 0 : 1;  // |b| = 0: x = 0 is the solution
   }
 }
 
-// z_c = Minv_c r_c, one thread per camera.
+// z = M r (block-Jacobi) and partials of r.z; one thread per camera.
 template <int B>
-__global__ void k_precond(const double* __restrict__ Minv, const int32_t* __restrict__ ext_col,
-                          const int32_t* __restrict__ intr_col, const int32_t* __restrict__ cam_group, int K,
-                          int64_t nc, const double* __restrict__ r, double* __restrict__ z) {
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(256) k_pcg_precond(const double* __restrict__ Minv, const int32_t* __restrict__ ext_col,
+                                                     const int32_t* __restrict__ intr_col,
+                                                     const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                     const double* __restrict__ r, double* __restrict__ z,
+                                                     double* __restrict__ part, const PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  if (ps->done) return;
+  double acc = 0.0;
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c < nc) {
     int col[B];
     double rv[B];
 #pragma unroll
@@ -1254,58 +1341,111 @@ __global__ void k_precond(const double* __restrict__ Minv, const int32_t* __rest
 #pragma unroll
       for (int j = 0; j < B; ++j) v += Mi[i * B + j] * rv[j];
       z[col[i]] = v;
+      acc += rv[i] * v;
     }
   }
+  acc = block_sum256(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
 
-// Two dot products with per-block partials: part[b] = a1.b1, part[nb + b] = a2.b2.
-__global__ void k_dot2(const double* a1, const double* b1, const double* a2, const double* b2, int64_t n, double* part) {
-  __shared__ double sh[2][8];
-  double s1 = 0.0, s2 = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    s1 += a1[i] * b1[i];
-    if (a2) s2 += a2[i] * b2[i];
-  }
-  s1 = warp_sum(s1);
-  s2 = warp_sum(s2);
-  if ((threadIdx.x & 31) == 0) {
-    sh[0][threadIdx.x >> 5] = s1;
-    sh[1][threadIdx.x >> 5] = s2;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t1 = 0.0, t2 = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-      t1 += sh[0][w];
-      t2 += sh[1][w];
+// rho = r.z; p = z (first iteration) or z + beta p.
+__global__ void __launch_bounds__(256) k_pcg_direction(int64_t n, const double* __restrict__ z, double* __restrict__ p,
+                                                       const double* __restrict__ part, int nb,
+                                                       PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  if (ps->done) return;
+  const double rho = sum_partials(part, nb, sh);
+  const int it = ps->it;
+  const double last = ps->rho[(it - 1) & 1];
+  const double beta = it > 1 ? rho / last : 0.0;
+  const bool fail = rho == 0.0 || !isfinite(rho) || (it > 1 && (beta == 0.0 || !isfinite(beta)));
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (fail) {
+      ps->failure = 1;
+      ps->done = 1;
+    } else {
+      ps->rho[it & 1] = rho;
     }
-    part[blockIdx.x] = t1;
-    part[gridDim.x + blockIdx.x] = t2;
   }
-}
-
-// p = z + beta p
-__global__ void k_axpby(double* p, const double* z, double beta, int64_t n) {
+  if (fail) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+    p[i] = it > 1 ? z[i] + beta * p[i] : z[i];
 }
-// x += alpha p; r = reset ? b - q : r - alpha q  (q holds S x when reset)
-__global__ void k_update_xr(double* x, double* r, const double* p, const double* q, const double* b, double alpha,
-                            int reset, int64_t n) {
+
+// alpha = rho / p.q; x += alpha p; r -= alpha q (except on residual-reset
+// iterations, whose r is recomputed as b - S x).
+__global__ void __launch_bounds__(256) k_pcg_step(int64_t n, double* __restrict__ x, double* __restrict__ r,
+                                                  const double* __restrict__ p, const double* __restrict__ q,
+                                                  const double* __restrict__ part, int nb, int period,
+                                                  PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  if (ps->done) return;
+  const double pq = sum_partials(part, nb, sh);
+  const int it = ps->it;
+  const double alpha = ps->rho[it & 1] / pq;
+  const bool indefinite = pq <= 0.0 || isinf(pq);
+  const bool stop = indefinite || isinf(alpha);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && stop) {
+    ps->failure = indefinite ? 0 : 1;  // indefinite: no more progress can be made (not a failure)
+    ps->done = 1;
+  }
+  if (stop) return;
+  const bool reset = it % period == 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
     if (!reset) r[i] -= alpha * q[i];
   }
 }
-__global__ void k_sub(double* r, const double* b, const double* q, int64_t n) {
+
+// Residual-reset iterations: r = b - q (q = S x).
+__global__ void __launch_bounds__(256) k_pcg_reset(int64_t n, double* __restrict__ r, const double* __restrict__ b,
+                                                   const double* __restrict__ q, int period,
+                                                   const PcgState* __restrict__ ps) {
+  if (ps->done || ps->it % period != 0) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     r[i] = b[i] - q[i];
 }
-// t[i] = b[i] + r[i]  (for Q = -x.(b + r))
-__global__ void k_add(double* t, const double* b, const double* r, int64_t n) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    t[i] = b[i] + r[i];
+
+// Partials of x.(b + r) (the quadratic model) and r.r.
+__global__ void __launch_bounds__(256) k_pcg_model(int64_t n, const double* __restrict__ x, const double* __restrict__ b,
+                                                   const double* __restrict__ r, double* __restrict__ part,
+                                                   const PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  if (ps->done) return;
+  double q = 0.0, rr = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    q += x[i] * (b[i] + r[i]);
+    rr += r[i] * r[i];
+  }
+  q = block_sum256(q, sh);
+  rr = block_sum256(rr, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = q;
+    part[gridDim.x + blockIdx.x] = rr;
+  }
 }
+
+// Terminations of the iteration: zeta = it (Q1 - Q0) / Q1 < eta (Nash's
+// truncated-Newton rule), |r| <= tol_r, or the iteration limit.
+__global__ void __launch_bounds__(256) k_pcg_terminate(const double* __restrict__ part, int nb, double eta,
+                                                       int max_iterations, PcgState* __restrict__ ps) {
+  __shared__ double sh[8];
+  if (ps->done) return;
+  const double Q1 = -sum_partials(part, nb, sh);
+  const double rr = sum_partials(part + nb, nb, sh);
+  if (threadIdx.x == 0) {
+    const int it = ps->it;
+    const double zeta = it * (Q1 - ps->Q0) / Q1;
+    if (zeta < eta) {
+      ps->done = 1;
+    } else {
+      ps->Q0 = Q1;
+      if (sqrt(rr) <= ps->tol_r || it >= max_iterations) ps->done = 1;
+      else ps->it = it + 1;
+    }
+  }
+}
+
 template <typename T, typename U2>
 __global__ void k_convert(const T* a, U2* b, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1785,6 +1925,10 @@ struct Solve {
   // iterative Schur (PCG) state
   double *pcg_x = nullptr, *pcg_r = nullptr, *pcg_z = nullptr, *pcg_p = nullptr, *pcg_q = nullptr, *pcg_b = nullptr;
   double *pcg_y = nullptr, *pcg_minv = nullptr, *pcg_part = nullptr;
+  int64_t pcg_part_n = 0;  // per-block partials of one reduction (two arrays of this size)
+  PcgState* pcg_state = nullptr;
+  cudaGraphExec_t pcg_graph = nullptr;  // one chunk of CG iterations
+  int64_t pcg_chunk_launches = 0;
   void* pcg_u = nullptr;
   int nb_pcg = 0;
 };
@@ -1856,7 +2000,7 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.S = a.template take<char>((size_t)n_s * n_s * tsize);
   s.rhs = a.template take<char>((size_t)s.n_pad * tsize);
   s.zsol = a.template take<char>((size_t)s.n_pad * tsize);
-  s.Linv = a.template take<char>((size_t)n_s * dense_tile(s.precision) * tsize);
+  s.Linv = a.template take<char>((size_t)n_s * kDenseTile * tsize);
   s.Vinv = a.template take<char>((size_t)s.np * 6 * tsize);
   s.gpv = a.template take<char>((size_t)s.np * 3 * tsize);
   s.part_mcc = a.template take<double>(s.nb_pt);
@@ -1925,7 +2069,7 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
   for (int64_t c = 0; c < nc; ++c) n_max += cc[c] ? 0 : free_e;
   for (int64_t g = 0; g < ni; ++g) n_max += ic[g] ? 0 : free_i;
   s.n_red = n_max;
-  s.n_pad = ceil_div(std::max<int64_t>(n_max, 1), dense_tile(s.precision)) * dense_tile(s.precision);
+  s.n_pad = ceil_div(std::max<int64_t>(n_max, 1), kDenseTile) * kDenseTile;
   s.dense = o->linear_solver == GBBA_SOLVER_DENSE_SCHUR ||
             (o->linear_solver == GBBA_SOLVER_AUTO && s.n_pad <= (int64_t)o->dense_schur_max_size + 64);
   s.nb_obs = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(no, 1), 256), h->sm_count * 8));
@@ -1995,7 +2139,7 @@ static void setup(gbba_handle* h, const gbba_problem* P, const gbba_options* o, 
       }
   }
   s.n_red = col;
-  s.n_pad = ceil_div(std::max<int64_t>(col, 1), dense_tile(s.precision)) * dense_tile(s.precision);
+  s.n_pad = ceil_div(std::max<int64_t>(col, 1), kDenseTile) * kDenseTile;
 
   // counting sort of observations by point (input order kept within a point)
   scan_offsets(h, counts, s.pt_off, np, chunks, st);
@@ -2109,7 +2253,9 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     s.pcg_y = A.take<double>(3 * np);
     s.pcg_minv = A.take<double>((size_t)nc * B * B);
     s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
-    s.pcg_part = A.take<double>(4096);
+    s.pcg_part_n = std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1);
+    s.pcg_part = A.take<double>(2 * s.pcg_part_n);
+    s.pcg_state = A.take<PcgState>(1);
     s.nb_pcg = 256;
     uint32_t* cam_keys = A.take<uint32_t>(no);
     uint32_t* iota = A.take<uint32_t>(no);
@@ -2237,6 +2383,17 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
 // the block-Jacobi preconditioner: residual reset every 10 iterations (the
 // reset recomputes b - S x with FP64 accumulation), termination on the
 // q-tolerance zeta < eta; r_tolerance is disabled as in the LM strategy.
+// Block-Jacobi PCG on the implicit Schur complement: ceres's CG
+// (conjugate_gradients_solver.cc:66-248) with the per-solve options the LM
+// strategy passes (levenberg_marquardt_strategy.cc:88-96: q_tolerance = eta,
+// r_tolerance = -1, i.e. the residual-norm test off), the residual recomputed
+// as b - S x every options.refinement_interval iterations (ceres's
+// residual_reset_period), FP64 vectors and reductions over the stored FP32 /
+// FP64 operator blocks.  The loop runs on the device: the host launches
+// chunks of kPcgChunk iterations (replayed from a CUDA graph) and reads the
+// `done` flag once per chunk.
+constexpr int kPcgChunk = 4;
+
 template <int M, typename T>
 static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   gbba_handle* h = s.h;
@@ -2244,97 +2401,80 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   constexpr int B = 6 + Model<M>::K;
   const int64_t n = s.n_red;
   const int nbv = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), s.nb_pcg));
-  const int gv = nbv;
-  std::vector<double> hp(2 * nbv);
-  auto dot2 = [&](const double* a1, const double* b1, const double* a2, const double* b2, double* d1, double* d2) {
-    k_dot2<<<nbv, 256, 0, st>>>(a1, b1, a2, b2, n, s.pcg_part);
-    check_launch(h);
-    GBBA_CUDA(cudaMemcpyAsync(hp.data(), s.pcg_part, sizeof(double) * 2 * nbv, cudaMemcpyDeviceToHost, st));
-    GBBA_CUDA(cudaStreamSynchronize(st));
-    double t1 = 0.0, t2 = 0.0;
-    for (int i = 0; i < nbv; ++i) {
-      t1 += hp[i];
-      t2 += hp[nbv + i];
-    }
-    *d1 = t1;
-    if (d2) *d2 = t2;
-  };
-  auto spmv = [&](const double* x, double* out) {
+  const int nbc = (int)std::max<int64_t>(1, ceil_div(s.nc, 256));      // k_pcg_precond blocks
+  const int nbs = (int)std::max<int64_t>(1, ceil_div(s.nc * 32, 128));  // k_spmv_camera blocks
+  const int period = std::max(1, o->refinement_interval);
+  PcgState* ps = s.pcg_state;
+  double* part_a = s.pcg_part;                 // r.z, then p.q
+  double* part_b = s.pcg_part + s.pcg_part_n;  // |b|^2, then the model and r.r
+  k_pcg_init<T><<<nbv, 256, 0, st>>>((const T*)s.rhs, s.pcg_b, s.pcg_x, s.pcg_r, n, part_b);
+  check_launch(h);
+  k_pcg_start<<<1, 256, 0, st>>>(part_b, nbv, -1.0, ps);
+  check_launch(h);
+  auto spmv = [&](const double* x, double* out, double* part, int reset) {
     if (s.np > 0) {
       k_spmv_point<B, T><<<(unsigned)ceil_div(s.np * 32, 128), 128, 0, st>>>(
-          s.pt_off, s.cam, (const T*)s.rec, (const T*)s.Vinv, s.ext_col, s.intr_col, s.cam_group, s.k, s.np, x, s.pcg_y);
+          s.pt_off, s.cam, (const T*)s.rec, (const T*)s.Vinv, s.ext_col, s.intr_col, s.cam_group, s.k, s.np, x, s.pcg_y,
+          ps, reset);
       check_launch(h);
     }
-    k_spmv_camera<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
+    k_spmv_camera<B, T><<<(unsigned)nbs, 128, 0, st>>>(
         s.cam_off, s.cam_obs, s.pt, (const T*)s.rec, (const T*)s.pcg_u, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc,
-        s.diag_c, s.radius, x, s.pcg_y, out);
+        s.diag_c, s.radius, x, s.pcg_y, out, part, ps, reset);
     check_launch(h);
   };
-  T* zsol = (T*)s.zsol;
-  k_convert<T, double><<<gv, 256, 0, st>>>((const T*)s.rhs, s.pcg_b, n);
-  check_launch(h);
-  GBBA_CUDA(cudaMemsetAsync(s.pcg_x, 0, sizeof(double) * n, st));
-  double bb = 0.0;
-  dot2(s.pcg_b, s.pcg_b, nullptr, nullptr, &bb, nullptr);
-  if (!(bb > 0.0)) {
-    GBBA_CUDA(cudaMemsetAsync(zsol, 0, sizeof(T) * s.n_pad, st));
-    return;
-  }
-  GBBA_CUDA(cudaMemcpyAsync(s.pcg_r, s.pcg_b, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
-  double rho = 1.0, Q0 = 0.0;
-  bool failure = false;
-  int it = 1;
-  for (;; ++it) {
-    k_precond<B><<<(unsigned)std::max<int64_t>(1, ceil_div(s.nc, 128)), 128, 0, st>>>(
-        s.pcg_minv, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.pcg_r, s.pcg_z);
+  auto iteration = [&]() {
+    k_pcg_precond<B><<<nbc, 256, 0, st>>>(s.pcg_minv, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.pcg_r,
+                                          s.pcg_z, part_a, ps);
     check_launch(h);
-    const double last_rho = rho;
-    dot2(s.pcg_r, s.pcg_z, nullptr, nullptr, &rho, nullptr);
-    if (rho == 0.0 || std::isinf(rho) || std::isnan(rho)) {
-      failure = true;
-      break;
-    }
-    if (it == 1) {
-      GBBA_CUDA(cudaMemcpyAsync(s.pcg_p, s.pcg_z, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+    k_pcg_direction<<<nbv, 256, 0, st>>>(n, s.pcg_z, s.pcg_p, part_a, nbc, ps);
+    check_launch(h);
+    spmv(s.pcg_p, s.pcg_q, part_a, 0);
+    k_pcg_step<<<nbv, 256, 0, st>>>(n, s.pcg_x, s.pcg_r, s.pcg_p, s.pcg_q, part_a, nbs, period, ps);
+    check_launch(h);
+    spmv(s.pcg_x, s.pcg_q, nullptr, period);  // residual reset: q = S x (only when it % period == 0)
+    k_pcg_reset<<<nbv, 256, 0, st>>>(n, s.pcg_r, s.pcg_b, s.pcg_q, period, ps);
+    check_launch(h);
+    k_pcg_model<<<nbv, 256, 0, st>>>(n, s.pcg_x, s.pcg_b, s.pcg_r, part_b, ps);
+    check_launch(h);
+    k_pcg_terminate<<<1, 256, 0, st>>>(part_b, nbv, o->eta, o->max_linear_solver_iterations, ps);
+    check_launch(h);
+  };
+  // one chunk of iterations as a graph, captured on first use in this solve
+  if (o->use_cuda_graphs && !s.pcg_graph) {
+    const int64_t l0 = h->launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      for (int i = 0; i < kPcgChunk; ++i) iteration();
+      GBBA_CUDA(cudaStreamEndCapture(st, &g));
+      GBBA_CUDA(cudaGraphInstantiate(&s.pcg_graph, g, 0));
+      cudaGraphDestroy(g);
+      s.pcg_chunk_launches = h->launches - l0;
     } else {
-      const double beta = rho / last_rho;
-      if (beta == 0.0 || std::isinf(beta) || std::isnan(beta)) {
-        failure = true;
-        break;
-      }
-      k_axpby<<<gv, 256, 0, st>>>(s.pcg_p, s.pcg_z, beta, n);
-      check_launch(h);
+      cudaGetLastError();
     }
-    spmv(s.pcg_p, s.pcg_q);
-    double pq = 0.0;
-    dot2(s.pcg_p, s.pcg_q, nullptr, nullptr, &pq, nullptr);
-    if (pq <= 0.0 || std::isinf(pq) || std::isnan(pq)) break;  // no further progress
-    const double alpha = rho / pq;
-    if (std::isinf(alpha)) {
-      failure = true;
-      break;
-    }
-    const int reset = (it % 10 == 0) ? 1 : 0;
-    k_update_xr<<<gv, 256, 0, st>>>(s.pcg_x, s.pcg_r, s.pcg_p, s.pcg_q, s.pcg_b, alpha, reset, n);
-    check_launch(h);
-    if (reset) {
-      spmv(s.pcg_x, s.pcg_q);
-      k_sub<<<gv, 256, 0, st>>>(s.pcg_r, s.pcg_b, s.pcg_q, n);
-      check_launch(h);
-    }
-    k_add<<<gv, 256, 0, st>>>(s.pcg_z, s.pcg_b, s.pcg_r, n);
-    check_launch(h);
-    double xq = 0.0;
-    dot2(s.pcg_x, s.pcg_z, nullptr, nullptr, &xq, nullptr);
-    const double Q1 = -xq;
-    const double zeta = it * (Q1 - Q0) / Q1;
-    if (zeta < o->eta) break;
-    Q0 = Q1;
-    if (it >= o->max_linear_solver_iterations) break;
+    h->launches = l0;  // captured, not yet run
   }
-  sum->linear_solver_iterations += it;
-  if (failure) GBBA_CUDA(cudaMemsetAsync(s.flag, 5, sizeof(int), st));
-  k_convert<double, T><<<gv, 256, 0, st>>>(s.pcg_x, zsol, n);
+  int* hdone = reinterpret_cast<int*>(h->pinned + 160);
+  for (int launched = 0;; launched += kPcgChunk) {
+    if (s.pcg_graph) {
+      GBBA_CUDA(cudaGraphLaunch(s.pcg_graph, st));
+      count_launch(h, (int)s.pcg_chunk_launches);
+    } else {
+      for (int i = 0; i < kPcgChunk; ++i) iteration();
+    }
+    GBBA_CUDA(cudaMemcpyAsync(hdone, &ps->done, sizeof(int), cudaMemcpyDeviceToHost, st));
+    GBBA_CUDA(cudaStreamSynchronize(st));
+    // the device stops at max_linear_solver_iterations; this bound only
+    // guards against a state that never reports done
+    if (*hdone || launched > o->max_linear_solver_iterations + kPcgChunk) break;
+  }
+  PcgState* hs = reinterpret_cast<PcgState*>(h->pinned + 168);
+  GBBA_CUDA(cudaMemcpyAsync(hs, ps, sizeof(PcgState), cudaMemcpyDeviceToHost, st));
+  GBBA_CUDA(cudaStreamSynchronize(st));
+  sum->linear_solver_iterations += hs->it;
+  if (hs->failure) GBBA_CUDA(cudaMemsetAsync(s.flag, 5, sizeof(int), st));
+  k_convert<double, T><<<nbv, 256, 0, st>>>(s.pcg_x, (T*)s.zsol, n);
   check_launch(h);
 }
 
@@ -2744,6 +2884,10 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   for (int i = 0; i < 6; ++i) cudaEventDestroy(ev[i]);
   for (int i = 0; i < 5; ++i)
     if (graphs[i]) cudaGraphExecDestroy(graphs[i]);
+  if (s.pcg_graph) {
+    cudaGraphExecDestroy(s.pcg_graph);
+    s.pcg_graph = nullptr;
+  }
   sum->termination_type = term;
   sum->usable = term != GBBA_FAILURE ? 1 : 0;
   sum->final_cost = cost;

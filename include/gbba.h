@@ -147,7 +147,9 @@ typedef struct gbba_options {
   int32_t max_linear_solver_iterations;   /* 500 (PCG) */
   int32_t dense_schur_max_size;           /* AUTO switches to PCG above this S size: 16384 */
   double eta;                             /* 0.1: PCG forcing sequence (ceres q-tolerance) */
-  int32_t refinement_interval;            /* mixed PCG: FP64 residual recompute every k steps: 8 */
+  int32_t refinement_interval;            /* PCG: every this many iterations the residual is recomputed
+                                             as b - S x (FP64 accumulation) instead of updated (ceres's
+                                             residual_reset_period): 10 */
   int32_t use_cuda_graphs;                /* 1: capture the per-iteration launch sequence */
   void* stream;                           /* cudaStream_t, or NULL for the handle's stream */
   int32_t fp64_polish_iterations;         /* mixed path: after it stops, at most this many plain-FP64
