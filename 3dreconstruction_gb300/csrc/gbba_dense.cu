@@ -752,6 +752,8 @@ void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Li
 
 template void dense_cholesky_solve_impl<float, false>(gbba_handle*, float*, int64_t, float*, float*, float*, int*,
                                                       cudaStream_t);
+template void dense_cholesky_solve_impl<float, true>(gbba_handle*, float*, int64_t, float*, float*, float*, int*,
+                                                     cudaStream_t);
 template void dense_cholesky_prepare<double>();
 template void dense_cholesky_prepare<float>();
 template void dense_cholesky_solve<double>(gbba_handle*, double*, int64_t, double*, double*, double*, int*, cudaStream_t);
