@@ -2224,7 +2224,8 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p1.take<double>(3 * np);
     p1.take<double>((size_t)nc * B * B);
     p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
-    p1.take<double>(4096);
+    p1.take<double>(2 * std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1));  // PCG partial sums
+    p1.take<PcgState>(1);
     size_t cam_sort_bytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, cam_sort_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
                                     (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)no, 0, key_bits(nc));
@@ -2297,7 +2298,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p2.take<uint32_t>(nk);
     p2.take<uint32_t>(1);
     if (A.used + p2.used + 4096 > A.capacity) {  // grow and redo phase 1
-      phase2_guess = p2.used;
+      phase2_guess = p2.used + (A.used > p1.used ? A.used - p1.used : 0);
       A.release();
       continue;
     }
@@ -2376,13 +2377,11 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     s.pair_path = true;
     return;
   }
+  // every attempt fell short of the pair list's size: never continue with a
+  // half-built workspace
+  throw Error{GBBA_ERROR_OUT_OF_MEMORY, "camera-pair workspace could not be sized"};
 }
 
-// Restatement of ceres ConjugateGradientsSolver::Solve (internal/ceres/
-// conjugate_gradients_solver.cc:66-248) on the implicit Schur complement with
-// the block-Jacobi preconditioner: residual reset every 10 iterations (the
-// reset recomputes b - S x with FP64 accumulation), termination on the
-// q-tolerance zeta < eta; r_tolerance is disabled as in the LM strategy.
 // Block-Jacobi PCG on the implicit Schur complement: ceres's CG
 // (conjugate_gradients_solver.cc:66-248) with the per-solve options the LM
 // strategy passes (levenberg_marquardt_strategy.cc:88-96: q_tolerance = eta,
