@@ -86,7 +86,8 @@ __global__ void k_dlt2(int64_t n, const double* P1, const double* P2, int64_t ps
 
 // ------------------------------------------------------- Gauss-Newton (templated)
 template <typename T>
-__device__ __forceinline__ void gn_accumulate(const T* Pi, const T X[3], T px, T py, T H[6], T g[3]) {
+__device__ __forceinline__ void gn_accumulate(const T* Pi, const T X[3], T px, T py, T H[6], T g[3],
+                                              T* cost = nullptr) {
   T h[3];
 #pragma unroll
   for (int r = 0; r < 3; ++r) h[r] = Pi[4 * r] * X[0] + Pi[4 * r + 1] * X[1] + Pi[4 * r + 2] * X[2] + Pi[4 * r + 3];
@@ -107,6 +108,24 @@ __device__ __forceinline__ void gn_accumulate(const T* Pi, const T X[3], T px, T
   H[5] += Ju[2] * Ju[2] + Jv[2] * Jv[2];
 #pragma unroll
   for (int j = 0; j < 3; ++j) g[j] += Ju[j] * ru + Jv[j] * rv;
+  if (cost) *cost += ru * ru + rv * rv;
+}
+
+// Squared reprojection error of X over a track's views.
+template <typename T, typename Views>
+__device__ __forceinline__ T reprojection_cost(const Views& view, int n, const T X[3]) {
+  T e = T(0);
+  for (int j = 0; j < n; ++j) {
+    const T* Pi;
+    T px, py;
+    view(j, &Pi, &px, &py);
+    T h[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) h[r] = Pi[4 * r] * X[0] + Pi[4 * r + 1] * X[1] + Pi[4 * r + 2] * X[2] + Pi[4 * r + 3];
+    const T ru = h[0] / h[2] - px, rv = h[1] / h[2] - py;
+    e += ru * ru + rv * rv;
+  }
+  return e;
 }
 
 template <typename T>
@@ -253,7 +272,7 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_f32(int method, const float
       if (!iterative_track<float>(views, n, Xc)) st = 1;
     } else {
       float Xh[4];
-      if (method == 0) nview_track<float>(views, n, Xh);
+      if (method == 0) nview_track<float, false>(views, n, Xh);
       else algebraic_track<float>(views, n, Xh);
       const float nrm = fabsf(Xh[0]) + fabsf(Xh[1]) + fabsf(Xh[2]);
       if (!(fabsf(Xh[3]) > 1e-6f * nrm)) {
@@ -266,19 +285,25 @@ __global__ void __launch_bounds__(kTriThreads) k_tri_f32(int method, const float
       }
     }
   }
+  // Gauss-Newton steps on the reprojection error, each kept only when it
+  // lowers that error (a step from a poorly conditioned linear estimate can
+  // overshoot); a singular normal matrix ends the refinement and keeps X.
   for (int s = 0; s < gn_steps && st == 0; ++s) {
-    float H[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0}, Hi[6];
+    float H[6] = {0, 0, 0, 0, 0, 0}, g[3] = {0, 0, 0}, Hi[6], e0 = 0.f;
     for (int j = 0; j < n; ++j) {
       const float* Pj;
       float px, py;
       views(j, &Pj, &px, &py);
-      gn_accumulate<float>(Pj, Xc, px, py, H, g);
+      gn_accumulate<float>(Pj, Xc, px, py, H, g, &e0);
     }
-    if (!inv3t<float>(H, Hi)) {
-      st = 1;
-      break;
-    }
-    gn_apply<float>(Hi, g, Xc);
+    if (!inv3t<float>(H, Hi)) break;
+    float Xn[3] = {Xc[0], Xc[1], Xc[2]};
+    gn_apply<float>(Hi, g, Xn);
+    const float e1 = reprojection_cost<float>(views, n, Xn);
+    if (!(e1 <= e0)) break;
+    Xc[0] = Xn[0];
+    Xc[1] = Xn[1];
+    Xc[2] = Xn[2];
   }
   float md = 3.402823466e38f;
   for (int j = 0; j < n; ++j) {

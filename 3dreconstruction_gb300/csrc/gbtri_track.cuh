@@ -142,19 +142,137 @@ __host__ __device__ __forceinline__ T min_right_singular4(T B[4][4], T y[4]) {
 // Index of (i, j), i <= j, in a packed symmetric 4x4.
 __host__ __device__ __forceinline__ constexpr int sym4(int i, int j) { return i <= j ? i * 4 - i * (i - 1) / 2 + (j - i) : j * 4 - j * (j - 1) / 2 + (i - j); }
 
+// Generalized 4x4 step: with G = L L^T, the smallest right singular vector y
+// of R L^-T gives X = L^-T y; returns sigma_min^2 (the next lambda).
+template <typename T>
+__host__ __device__ __forceinline__ T nview_solve4(const T R[4][4], const T G[10], T X[4]) {
+  T L[4][4], Li[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) L[i][j] = Li[i][j] = T(0);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    T d = G[sym4(j, j)];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d -= L[j][k] * L[j][k];
+    L[j][j] = sqrt(d);
+#pragma unroll
+    for (int i = j + 1; i < 4; ++i) {
+      T v = G[sym4(i, j)];
+#pragma unroll
+      for (int k = 0; k < j; ++k) v -= L[i][k] * L[j][k];
+      L[i][j] = v / L[j][j];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    Li[j][j] = T(1) / L[j][j];
+#pragma unroll
+    for (int i = j + 1; i < 4; ++i) {
+      T v = T(0);
+#pragma unroll
+      for (int k = j; k < i; ++k) v -= L[i][k] * Li[k][j];
+      Li[i][j] = v / L[i][i];
+    }
+  }
+  T B[4][4], y[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      T v = T(0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) v += R[i][k] * Li[j][k];
+      B[i][j] = v;
+    }
+  const T lam = min_right_singular4<T>(B, y);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    T v = T(0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v += Li[j][i] * y[j];
+    X[i] = v;
+  }
+  return lam;
+}
+
+// [X; alpha] scaled to unit norm, |alpha|^2 = X^T Q X.
+template <typename T>
+__host__ __device__ __forceinline__ void nview_normalize(const T Q[10], T X[4]) {
+  T an = T(0), xn = T(0);
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    xn += X[a] * X[a];
+#pragma unroll
+    for (int b = 0; b < 4; ++b) an += X[a] * Q[sym4(a, b)] * X[b];
+  }
+  const T inv = T(1) / sqrt(xn + an);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) X[i] *= inv;
+}
+
 // TriangulateNView of one track.  view(j, &P, &x, &y) gives view j's
 // projection matrix (row-major 3x4) and pixel.  X: the head of the unit
 // vector [X; alpha].
-template <typename T, typename Views>
+//
+// kExact (the FP64 parity path): every fixed-point pass re-reads the views
+// and accumulates G(lambda) = I + sum h h^T / (c^2 - lambda) exactly.
+// Otherwise (the FP32 production path) one pass over the views accumulates
+// the moments G_m = sum h h^T / c^(2m), m = 1..3, and every pass uses
+//   G(lambda) = I + G_1 + lambda G_2 + lambda^2 G_3,
+//   Q(lambda) = sum c^2 h h^T / (c^2 - lambda)^2 = G_1 + 2 lambda G_2 + 3 lambda^2 G_3,
+// whose truncation error (lambda / c^2)^3 is far below FP32 rounding
+// (lambda is a squared residual, c^2 >= 1 and ~1e6 in pixels).
+template <typename T, bool kExact = true, typename Views>
 __host__ __device__ void nview_track(const Views& view, int n, T X[4]) {
   T R[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) R[i][j] = T(0);
-  T lam = T(0), Q[10], y[4];
+  T lam = T(0), Q[10];
 #pragma unroll
   for (int i = 0; i < 4; ++i) X[i] = T(0);
+  if (!kExact) {
+    T M1[10], M2[10], M3[10];
+#pragma unroll
+    for (int i = 0; i < 10; ++i) M1[i] = M2[i] = M3[i] = T(0);
+    for (int j = 0; j < n; ++j) {
+      const T* P;
+      T px, py;
+      view(j, &P, &px, &py);
+      T h[4], g1[4], g2[4], c;
+      view_house<T>(P, px, py, h, g1, g2, &c);
+      givens_in<T>(R, g1);
+      givens_in<T>(R, g2);
+      const T w1 = T(1) / (c * c), w2 = w1 * w1, w3 = w2 * w1;
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = a; b < 4; ++b) {
+          const T hh = h[a] * h[b];
+          M1[sym4(a, b)] += w1 * hh;
+          M2[sym4(a, b)] += w2 * hh;
+          M3[sym4(a, b)] += w3 * hh;
+        }
+    }
+    for (int pass = 0; pass < 3; ++pass) {
+      T G[10];
+#pragma unroll
+      for (int i = 0; i < 10; ++i) {
+        G[i] = M1[i] + lam * (M2[i] + lam * M3[i]);
+        Q[i] = M1[i] + lam * (T(2) * M2[i] + T(3) * lam * M3[i]);
+      }
+      G[sym4(0, 0)] += T(1);
+      G[sym4(1, 1)] += T(1);
+      G[sym4(2, 2)] += T(1);
+      G[sym4(3, 3)] += T(1);
+      lam = nview_solve4<T>(R, G, X);
+    }
+    nview_normalize<T>(Q, X);
+    return;
+  }
   for (int pass = 0; pass < 3; ++pass) {
     T G[10];
 #pragma unroll
@@ -180,68 +298,10 @@ __host__ __device__ void nview_track(const Views& view, int n, T X[4]) {
           Q[sym4(a, b)] += q * h[a] * h[b];
         }
     }
-    // G = L L^T, Li = L^-1 (lower)
-    T L[4][4], Li[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) L[i][j] = Li[i][j] = T(0);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      T d = G[sym4(j, j)];
-#pragma unroll
-      for (int k = 0; k < j; ++k) d -= L[j][k] * L[j][k];
-      L[j][j] = sqrt(d);
-#pragma unroll
-      for (int i = j + 1; i < 4; ++i) {
-        T v = G[sym4(i, j)];
-#pragma unroll
-        for (int k = 0; k < j; ++k) v -= L[i][k] * L[j][k];
-        L[i][j] = v / L[j][j];
-      }
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      Li[j][j] = T(1) / L[j][j];
-#pragma unroll
-      for (int i = j + 1; i < 4; ++i) {
-        T v = T(0);
-#pragma unroll
-        for (int k = j; k < i; ++k) v -= L[i][k] * Li[k][j];
-        Li[i][j] = v / L[i][i];
-      }
-    }
-    // B = R L^-T
-    T B[4][4];
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        T v = T(0);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) v += R[i][k] * Li[j][k];
-        B[i][j] = v;
-      }
-    lam = min_right_singular4<T>(B, y);
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      T v = T(0);
-#pragma unroll
-      for (int j = 0; j < 4; ++j) v += Li[j][i] * y[j];
-      X[i] = v;
-    }
+    lam = nview_solve4<T>(R, G, X);
   }
   // |alpha|^2 = X^T Q X with Q = sum c^2 h h^T / (c^2 - lambda)^2
-  T an = T(0), xn = T(0);
-#pragma unroll
-  for (int a = 0; a < 4; ++a) {
-    xn += X[a] * X[a];
-#pragma unroll
-    for (int b = 0; b < 4; ++b) an += X[a] * Q[sym4(a, b)] * X[b];
-  }
-  const T inv = T(1) / sqrt(xn + an);
-#pragma unroll
-  for (int i = 0; i < 4; ++i) X[i] *= inv;
+  nview_normalize<T>(Q, X);
 }
 
 // TriangulateNViewAlgebraic of one track: unit X.

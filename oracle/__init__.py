@@ -132,11 +132,13 @@ def tri_linear_gn(P, offsets, cam, xy, gn_steps=1):
     return X, st, md
 
 
-def tri_gn_steps(P, offsets, cam, xy, X0, steps=1):
+def tri_gn_steps(P, offsets, cam, xy, X0, steps=1, safeguard=False):
     """FP64 Gauss-Newton steps on the reprojection error of each track, from
     the Euclidean points X0 (numpy restatement; the step the triangulation
     paths apply after their linear estimate): H = sum J^T J, g = sum J^T r over
-    the track's views, X <- X - H^-1 g."""
+    the track's views, X <- X - H^-1 g.  With safeguard, as the FP32
+    production kernel does, a track keeps its X when the step does not lower
+    its squared reprojection error."""
     P = np.asarray(P, np.float64).reshape(-1, 3, 4)
     off = np.asarray(offsets, np.int64)
     cam = np.asarray(cam, np.int64)
@@ -154,7 +156,17 @@ def tri_gn_steps(P, offsets, cam, xy, X0, steps=1):
         g = np.zeros((len(X), 3))
         np.add.at(H, tr, Ju[:, :, None] * Ju[:, None, :] + Jv[:, :, None] * Jv[:, None, :])
         np.add.at(g, tr, Ju * ru[:, None] + Jv * rv[:, None])
-        X = X - np.linalg.solve(H, g[:, :, None])[:, :, 0]
+        Xn = X - np.linalg.solve(H, g[:, :, None])[:, :, 0]
+        if safeguard:
+            def cost(Y):
+                hh = np.einsum("nij,nj->ni", Pi[:, :, :3], Y[tr]) + Pi[:, :, 3]
+                e = ((hh[:, :2] / hh[:, 2:3] - xy) ** 2).sum(1)
+                out = np.zeros(len(Y))
+                np.add.at(out, tr, e)
+                return out
+            keep = ~(cost(Xn) <= cost(X))
+            Xn[keep] = X[keep]
+        X = Xn
     return X
 
 

@@ -35,7 +35,8 @@ static void run(int64_t nt, const std::vector<T>& P, const std::vector<int64_t>&
     const HostViews<T> v{P.data(), cam.data(), xy.data(), off[t]};
     const int n = (int)(off[t + 1] - off[t]);
     T X[4], Y[4], Z[3];
-    gbba::nview_track<T>(v, n, X);
+    if (sizeof(T) == 8) gbba::nview_track<T, true>(v, n, X);  // the FP64 parity path (exact passes)
+    else gbba::nview_track<T, false>(v, n, X);               // the FP32 path (one pass, series form)
     gbba::algebraic_track<T>(v, n, Y);
     gbba::iterative_track<T>(v, n, Z);
     for (int i = 0; i < 4; ++i) nv[4 * t + i] = X[i], al[4 * t + i] = Y[i];

@@ -131,16 +131,17 @@ def test_fp32_path_matches_reference(method, key, handle, abi):
 
 
 def test_fp32_nview_gauss_newton_matches_fp64(handle, abi):
-    """The production configuration (FP32 N-view + one Gauss-Newton step)
-    against the FP64 oracle of the same: the reference's TriangulateNView
-    output, dehomogenised, then one FP64 Gauss-Newton step."""
+    """The production configuration (FP32 N-view + one Gauss-Newton step,
+    kept when it lowers the reprojection error) against the FP64 oracle of the
+    same: the reference's TriangulateNView output, dehomogenised, then one
+    FP64 Gauss-Newton step with the same safeguard."""
     import oracle
     g = load_golden("tri_tracks_f32.npz")
     nt = len(g["track_offsets"]) - 1
     tr = {k: g[k] for k in ("P", "track_offsets", "camera_index", "xy")}
     X, st, md = f32_path(handle, abi, tr, gn_steps=1, method=0)
     ref = oracle.tri_gn_steps(g["P"], g["track_offsets"], g["camera_index"], g["xy"],
-                              euclid(g["nview_h"].reshape(nt, 4)), 1)
+                              euclid(g["nview_h"].reshape(nt, 4)), 1, safeguard=True)
     assert (st == abi.TRACK_OK).all()
     assert_fp32_close(X, ref)
     # the step lowers the total squared reprojection error of the linear estimate
@@ -180,7 +181,7 @@ def test_fp32_path_full_size_properties(handle, abi, scenes):
     full batch)."""
     tr = scenes.track_scene(seed=2)
     X, st, md = f32_path(handle, abi, tr, gn_steps=1, method=0)
-    assert (st == abi.TRACK_OK).mean() > 0.999
+    assert (st != abi.TRACK_OK).sum() <= 10  # at most a few near-degenerate geometries in 1M
     err = np.linalg.norm(X - tr["X_true"], axis=1)
     assert np.median(err) < 0.01
     sub = {"P": tr["P"], "track_offsets": tr["track_offsets"][:5001], "camera_index": tr["camera_index"],
