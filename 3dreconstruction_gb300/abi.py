@@ -148,6 +148,18 @@ class GbbaTuning(C.Structure):
     ]
 
 
+class GbsfmCamera(C.Structure):
+    """gbsfm_camera: rotation (row-major), translation, f, ppx, ppy, k1, k2, k3;
+    the same 18 doubles as a row of scenes.brown_cameras()."""
+    _fields_ = [("R", C.c_double * 9), ("t", C.c_double * 3), ("f", C.c_double), ("ppx", C.c_double),
+                ("ppy", C.c_double), ("k1", C.c_double), ("k2", C.c_double), ("k3", C.c_double)]
+
+
+class GbsfmResidualStats(C.Structure):
+    _fields_ = [("count", C.c_int64), ("min", C.c_double), ("max", C.c_double), ("mean", C.c_double),
+                ("median", C.c_double), ("hist", C.c_int64 * 10), ("underflow", C.c_int64), ("overflow", C.c_int64)]
+
+
 def default_options(**kw):
     """ceres::Solver::Options defaults (include/ceres/solver.h:81-129)."""
     o = GbbaOptions()
@@ -307,6 +319,15 @@ def declare_gbba(lib):
     lib.gbba_project_backward_mixed.restype = C.c_int
     lib.gbba_project_forward_noalloc.argtypes = [P(GbbaProblem), C.c_int32, C.c_double, vp, vp, vp]
     lib.gbba_project_forward_noalloc.restype = C.c_int
+    lib.gbsfm_triangulate_pair.argtypes = [vp, vp, vp, C.c_int64, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                                           vp, vp, vp, vp, C.c_int32]
+    lib.gbsfm_triangulate_pair.restype = C.c_int
+    lib.gbsfm_reject_tracks.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, vp, vp, C.c_double, C.c_double, vp, vp,
+                                        vp, vp, C.c_int32]
+    lib.gbsfm_reject_tracks.restype = C.c_int
+    lib.gbsfm_residual_histogram.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, vp, vp, P(GbsfmResidualStats),
+                                             C.c_int32]
+    lib.gbsfm_residual_histogram.restype = C.c_int
     lib.gbba_last_kernel_time.argtypes = [vp, vp]
     lib.gbba_last_kernel_time.restype = C.c_int
     lib.gbtri_dlt2_batched.argtypes = [vp, C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
@@ -327,4 +348,5 @@ EXPORTED_SYMBOLS = (
     "gbba_abi_version", "gbba_launch_count", "gbba_last_kernel_time", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
     "gbba_project_forward", "gbba_project_backward", "gbba_project_backward_mixed", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
+    "gbsfm_triangulate_pair", "gbsfm_reject_tracks", "gbsfm_residual_histogram",
 )

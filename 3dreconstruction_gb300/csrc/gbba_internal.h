@@ -135,6 +135,26 @@ inline void check_launch(gbba_handle* h) {
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
+// Device view of an input array: the caller's pointer (device memory) or a
+// staged copy (host memory).
+template <typename T>
+inline const T* in_view(gbba_handle* h, const T* p, size_t count, int memory) {
+  if (!p || memory == GBBA_MEMORY_DEVICE) return p;
+  T* d = h->arena.take<T>(count);
+  if (count) GBBA_CUDA(cudaMemcpyAsync(d, p, count * sizeof(T), cudaMemcpyHostToDevice, h->active));
+  return d;
+}
+template <typename T>
+inline T* out_view(gbba_handle* h, T* p, size_t count, int memory) {
+  if (!p || memory == GBBA_MEMORY_DEVICE) return p;
+  return h->arena.take<T>(count);
+}
+template <typename T>
+inline void out_back(gbba_handle* h, T* user, const T* dev, size_t count, int memory) {
+  if (!user || memory == GBBA_MEMORY_DEVICE || count == 0) return;
+  GBBA_CUDA(cudaMemcpyAsync(user, dev, count * sizeof(T), cudaMemcpyDeviceToHost, h->active));
+}
+
 // Vector type of 16-byte loads and stores.
 template <typename T> struct Vec16;
 template <> struct Vec16<float> { using type = float4; static constexpr int n = 4; };

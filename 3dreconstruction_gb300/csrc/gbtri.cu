@@ -24,46 +24,6 @@
 namespace gbba {
 
 // ---------------------------------------------------------------- FP64 DLT (4x4)
-__device__ void jacobi_nullspace4(double A[4][4], double x[4]) {
-  double V[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    bool rotated = false;
-    for (int i = 0; i < 3; ++i)
-      for (int j = i + 1; j < 4; ++j) {
-        double a = 0, b = 0, g = 0;
-        for (int r = 0; r < 4; ++r) {
-          a += A[r][i] * A[r][i];
-          b += A[r][j] * A[r][j];
-          g += A[r][i] * A[r][j];
-        }
-        if (g == 0.0 || fabs(g) <= 1e-15 * sqrt(a * b)) continue;
-        rotated = true;
-        const double zeta = (b - a) / (2.0 * g);
-        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
-        for (int r = 0; r < 4; ++r) {
-          const double ui = A[r][i], uj = A[r][j];
-          A[r][i] = c * ui - s * uj;
-          A[r][j] = s * ui + c * uj;
-          const double vi = V[r][i], vj = V[r][j];
-          V[r][i] = c * vi - s * vj;
-          V[r][j] = s * vi + c * vj;
-        }
-      }
-    if (!rotated) break;
-  }
-  int best = 0;
-  double bn = 1e300;
-  for (int i = 0; i < 4; ++i) {
-    const double nrm = A[0][i] * A[0][i] + A[1][i] * A[1][i] + A[2][i] * A[2][i] + A[3][i] * A[3][i];
-    if (nrm < bn) {
-      bn = nrm;
-      best = i;
-    }
-  }
-  for (int r = 0; r < 4; ++r) x[r] = V[r][best];
-}
-
 __global__ void k_dlt2(int64_t n, const double* P1, const double* P2, int64_t ps, const double* x1, const double* x2,
                        double* Xh, double* Xe) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
@@ -344,26 +304,6 @@ gbba_status tri_guard(gbba_handle* h, F&& f) {
     cudaGetLastError();
     return e.status;
   }
-}
-
-// Device view of an input array: the caller's pointer (device memory) or a
-// staged copy (host memory).
-template <typename T>
-const T* in_view(gbba_handle* h, const T* p, size_t count, int memory) {
-  if (!p || memory == GBBA_MEMORY_DEVICE) return p;
-  T* d = h->arena.take<T>(count);
-  if (count) GBBA_CUDA(cudaMemcpyAsync(d, p, count * sizeof(T), cudaMemcpyHostToDevice, h->active));
-  return d;
-}
-template <typename T>
-T* out_view(gbba_handle* h, T* p, size_t count, int memory) {
-  if (!p || memory == GBBA_MEMORY_DEVICE) return p;
-  return h->arena.take<T>(count);
-}
-template <typename T>
-void out_back(gbba_handle* h, T* user, const T* dev, size_t count, int memory) {
-  if (!user || memory == GBBA_MEMORY_DEVICE || count == 0) return;
-  GBBA_CUDA(cudaMemcpyAsync(user, dev, count * sizeof(T), cudaMemcpyDeviceToHost, h->active));
 }
 
 // One pass over a batch's CSR offsets and camera indices: offs[0] == 0,

@@ -25,6 +25,49 @@ __host__ __device__ __forceinline__ bool inv3t(const T A[6], T Ai[6]) {  // symm
   return true;
 }
 
+// Smallest right singular vector of a 4x4 matrix by one-sided Jacobi (the
+// nullspace of TriangulateDLT's design, libs/base/include/mvg/math/numeric.h:
+// 228-240, in the same arithmetic as the reference's JacobiSVD to 1e-15).
+__host__ __device__ inline void jacobi_nullspace4(double A[4][4], double x[4]) {
+  double V[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 1, 0}, {0, 0, 0, 1}};
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    bool rotated = false;
+    for (int i = 0; i < 3; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        double a = 0, b = 0, g = 0;
+        for (int r = 0; r < 4; ++r) {
+          a += A[r][i] * A[r][i];
+          b += A[r][j] * A[r][j];
+          g += A[r][i] * A[r][j];
+        }
+        if (g == 0.0 || fabs(g) <= 1e-15 * sqrt(a * b)) continue;
+        rotated = true;
+        const double zeta = (b - a) / (2.0 * g);
+        const double t = (zeta >= 0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / sqrt(1.0 + t * t), s = c * t;
+        for (int r = 0; r < 4; ++r) {
+          const double ui = A[r][i], uj = A[r][j];
+          A[r][i] = c * ui - s * uj;
+          A[r][j] = s * ui + c * uj;
+          const double vi = V[r][i], vj = V[r][j];
+          V[r][i] = c * vi - s * vj;
+          V[r][j] = s * vi + c * vj;
+        }
+      }
+    if (!rotated) break;
+  }
+  int best = 0;
+  double bn = 1e300;
+  for (int i = 0; i < 4; ++i) {
+    const double nrm = A[0][i] * A[0][i] + A[1][i] * A[1][i] + A[2][i] * A[2][i] + A[3][i] * A[3][i];
+    if (nrm < bn) {
+      bn = nrm;
+      best = i;
+    }
+  }
+  for (int r = 0; r < 4; ++r) x[r] = V[r][best];
+}
+
 // ------------------------------------------------ N-view nullspace of any track length
 // TriangulateNView (triangulation_nview.cpp:8-24) takes the smallest right
 // singular vector v = [X; alpha] of the 3n x (4+n) design whose view-i rows

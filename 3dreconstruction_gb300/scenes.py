@@ -330,3 +330,87 @@ def ba_options_for(scene, **kw):
     for key, v in kw.items():
         setattr(o, key, v)
     return o
+
+
+# ----------------------------------------------------------------- engine-side scans
+def brown_cameras(centers, rng, k_sigma=(0.05, 0.01, 0.01), f_range=(900.0, 1100.0)):
+    """Cameras in the layout of the engine's BrownPinholeCamera: rows of
+    [R (row-major 9), t (3), f, ppx, ppy, k1, k2, k3], facing the origin."""
+    R, t = _cameras_facing_origin(centers)
+    n = len(centers)
+    cams = np.zeros((n, 18))
+    cams[:, :9] = R.reshape(n, 9)
+    cams[:, 9:12] = t
+    cams[:, 12] = rng.uniform(f_range[0], f_range[1], n)
+    cams[:, 13], cams[:, 14] = PP
+    cams[:, 15:18] = rng.normal(0, k_sigma, (n, 3))
+    return cams
+
+
+def brown_project(cams, X):
+    """Pixels of X through the cameras (rows paired): R X + t, x/z, the radial
+    K3 factor, f and the principal point; and the depth."""
+    R = cams[:, :9].reshape(-1, 3, 3)
+    p = np.einsum("nij,nj->ni", R, X) + cams[:, 9:12]
+    x, y = p[:, 0] / p[:, 2], p[:, 1] / p[:, 2]
+    r2 = x * x + y * y
+    rc = 1 + cams[:, 15] * r2 + cams[:, 16] * r2 * r2 + cams[:, 17] * r2 * r2 * r2
+    return np.stack([cams[:, 13] + cams[:, 12] * x * rc, cams[:, 14] + cams[:, 12] * y * rc], -1), p[:, 2]
+
+
+def engine_pair(n=2000, seed=7, baseline=1.5, sigma=0.5, outlier_frac=0.05, far_frac=0.1, behind_frac=0.05):
+    """Matches between two cameras for the engine's pair triangulation: points
+    in front of both, a share far away (small ray angles), a share behind, and
+    outliers; an inlier mask of the caller's robust estimation (90%)."""
+    rng = np.random.default_rng(seed)
+    centers = np.array([[-baseline / 2, 0.0, -10.0], [baseline / 2, 0.0, -10.0]])
+    cams = brown_cameras(centers, rng)
+    X = rng.uniform(-2, 2, (n, 3))
+    far = rng.random(n) < far_frac
+    X[far, 2] += rng.uniform(60, 200, far.sum())
+    behind = rng.random(n) < behind_frac
+    X[behind, 2] = -25.0 + rng.uniform(-2, 2, behind.sum())
+    x1, _ = brown_project(np.repeat(cams[:1], n, 0), X)
+    x2, _ = brown_project(np.repeat(cams[1:], n, 0), X)
+    x1 += rng.normal(scale=sigma, size=x1.shape)
+    x2 += rng.normal(scale=sigma, size=x2.shape)
+    out = rng.random(n) < outlier_frac
+    x2[out] += rng.normal(scale=25.0, size=(out.sum(), 2))
+    inlier = (rng.random(n) < 0.9).astype(np.uint8)
+    return {"cameras": cams, "x1": x1, "x2": x2, "inlier": inlier}
+
+
+def engine_tracks(num_cameras=30, num_tracks=3000, seed=8, sigma=0.5, outlier_frac=0.03, narrow_frac=0.05,
+                  max_len=10, twins=6):
+    """Reconstructed tracks for the engine's bad-track rejection and residual
+    statistics: CSR over cameras (observations of a track in increasing camera
+    order), one 3D point per track, lengths 1..max_len, pixel noise and
+    outliers.  The last `twins` cameras sit 0.3 units from the first ones, and
+    a share of the tracks is seen only by such a pair, so that their rays meet
+    at small angles."""
+    rng = np.random.default_rng(seed)
+    centers = 12.0 * sphere_directions(num_cameras, rng)
+    tang = np.cross(centers[:twins], np.array([0.0, 1.0, 0.0]))
+    tang /= np.linalg.norm(tang, axis=1, keepdims=True)
+    centers = np.concatenate([centers, centers[:twins] + 0.3 * tang])
+    cams = brown_cameras(centers, rng)
+    X = rng.uniform(-2, 2, (num_tracks, 3))
+    narrow = rng.random(num_tracks) < narrow_frac
+    L = rng.integers(1, max_len + 1, num_tracks)
+    L[narrow] = 2
+    groups = []
+    for t in range(num_tracks):
+        if narrow[t]:
+            k = int(rng.integers(0, twins))
+            groups.append(np.array([k, num_cameras + k]))
+        else:
+            groups.append(np.sort(rng.choice(num_cameras, L[t], replace=False)))
+    cam = np.concatenate(groups).astype(np.uint32)
+    tr = np.repeat(np.arange(num_tracks), L)
+    xy, _ = brown_project(cams[cam], X[tr])
+    xy += rng.normal(scale=sigma, size=xy.shape)
+    out = rng.random(len(tr)) < outlier_frac
+    xy[out] += rng.normal(scale=20.0, size=(out.sum(), 2))
+    off = np.zeros(num_tracks + 1, np.int64)
+    off[1:] = np.cumsum(L)
+    return {"cameras": cams, "points": X, "track_offsets": off, "camera_index": cam, "xy": xy}

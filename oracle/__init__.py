@@ -233,3 +233,107 @@ def scene_to_kv(scene, options, layout=0, linear_solver=0, num_threads=1, precon
     if scene.get("intrinsic_constant") is not None:
         d["intrinsic_constant"] = scene["intrinsic_constant"]
     return d
+
+
+# ------------------------------------------------------------ engine-side scans
+def _brown(cams, X):
+    """BrownPinholeCamera::Project and Depth for rows of cameras (n, 18) and points."""
+    R = cams[:, :9].reshape(-1, 3, 3)
+    p = np.einsum("nij,nj->ni", R, X) + cams[:, 9:12]
+    xe, ye = p[:, 0] / p[:, 2], p[:, 1] / p[:, 2]
+    r2 = xe * xe + ye * ye
+    rc = 1 + cams[:, 15] * r2 + cams[:, 16] * r2 * r2 + cams[:, 17] * r2 * r2 * r2
+    return np.stack([cams[:, 13] + cams[:, 12] * (xe * rc), cams[:, 14] + cams[:, 12] * (ye * rc)], -1), p[:, 2]
+
+
+def _angle_deg(c):
+    return np.degrees(np.arccos(np.clip(c, -1 + 1e-8, 1 - 1e-8)))
+
+
+def sfm_triangulate_pair(cams, x1, x2, inlier, th1, th2, min_angle):
+    """triangulate2View_Vector (sfm_robust.h:152-195) and its callers' keep
+    decision (sfm_incremental_engine.cpp:977-1029, 492-533), restated: X by the
+    oracle's TriangulateDLT, the mean PinholeCamera residual through P = K[R|t],
+    keep = inlier, BrownPinholeCamera residuals below the thresholds, positive
+    depths and AngleBetweenRay above min_angle."""
+    cams = np.asarray(cams, np.float64).reshape(-1, 18)
+    n = len(x1)
+    P = []
+    for c in cams[:2]:
+        K = np.array([[c[12], 0, c[13]], [0, c[12], c[14]], [0, 0, 1.0]])
+        P.append(K @ np.concatenate([c[:9].reshape(3, 3), c[9:12, None]], 1))
+    _, X = tri_dlt2(P[0].ravel(), P[1].ravel(), x1, x2, shared=True)
+
+    def pin(Pm, x):
+        h = X @ Pm[:, :3].T + Pm[:, 3]
+        return np.linalg.norm(x - h[:, :2] / h[:, 2:3], axis=1)
+    residual = (pin(P[0], x1) + pin(P[1], x2)) / 2.0
+    u1, d1 = _brown(np.repeat(cams[:1], n, 0), X)
+    u2, d2 = _brown(np.repeat(cams[1:2], n, 0), X)
+    r1, r2 = np.linalg.norm(x1 - u1, axis=1), np.linalg.norm(x2 - u2, axis=1)
+
+    def ray(c, x):
+        k = np.stack([(x[:, 0] - c[13]) / c[12], (x[:, 1] - c[14]) / c[12], np.ones(len(x))], 1)
+        r = k @ c[:9].reshape(3, 3)
+        return r / np.linalg.norm(r, axis=1, keepdims=True)
+    a, b = ray(cams[0], x1), ray(cams[1], x2)
+    mag = np.sqrt((a * a).sum(1) * (b * b).sum(1))
+    keep = (np.asarray(inlier) != 0) & (r1 < th1) & (r2 < th2) & (d1 > 0) & (d2 > 0) & \
+        (_angle_deg((a * b).sum(1) / mag) > min_angle)
+    return X, residual, keep.astype(np.uint8)
+
+
+def _track_ids(offsets):
+    off = np.asarray(offsets, np.int64)
+    return np.repeat(np.arange(len(off) - 1), np.diff(off)), off
+
+
+def sfm_reject_tracks(cams, points, offsets, cam, xy, precision, min_angle=3.0):
+    """badTrackRejector (sfm_incremental_engine.cpp:1047-1140), restated."""
+    cams = np.asarray(cams, np.float64).reshape(-1, 18)
+    tr, off = _track_ids(offsets)
+    cam = np.asarray(cam, np.int64)
+    X = np.asarray(points, np.float64)[tr]
+    u, _ = _brown(cams[cam], X)
+    bad = np.linalg.norm(np.asarray(xy) - u, axis=1) > precision
+    R = cams[cam, :9].reshape(-1, 3, 3)
+    C = -np.einsum("nji,nj->ni", R, cams[cam, 9:12])
+    d = X - C
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    nt = len(off) - 1
+    first = np.full(nt, -1, np.int64)
+    order = np.lexsort((cam, tr))  # per track, lowest camera first
+    starts = off[:-1][np.diff(off) > 0]
+    first[np.diff(off) > 0] = order[starts]
+    ang = _angle_deg((d * d[first[tr]]).sum(1))
+    ang[np.arange(len(tr)) == first[tr]] = 0.0
+    max_angle = np.zeros(nt)
+    np.maximum.at(max_angle, tr, ang)
+    narrow = max_angle < min_angle
+    erase = bad | narrow[tr]
+    erased = np.bincount(tr, weights=erase, minlength=nt).astype(np.int64)
+    remaining = np.diff(off) - erased
+    gone = (erased > 0) & (remaining < 2)
+    return (~erase).astype(np.uint8), (~gone).astype(np.uint8), int(erased.sum()), int(gone.sum())
+
+
+def sfm_residual_histogram(cams, points, offsets, cam, xy):
+    """ComputeResidualsHistogram (sfm_incremental_engine.cpp:1550-1616),
+    restated: float residuals, MinMaxMeanMedian<float>, Histogram<double>(min, max, 10)."""
+    cams = np.asarray(cams, np.float64).reshape(-1, 18)
+    tr, off = _track_ids(offsets)
+    u, _ = _brown(cams[np.asarray(cam, np.int64)], np.asarray(points, np.float64)[tr])
+    res = np.linalg.norm(np.asarray(xy) - u, axis=1).astype(np.float32)
+    out = {"count": len(res)}
+    if len(res) > 1:
+        v = np.sort(res)
+        mn, mx = float(v[0]), float(v[-1])
+        out.update(min=mn, max=mx, mean=float(np.float32(v.astype(np.float64).sum() / len(v))),
+                   median=float(v[len(v) // 2]))
+        x = v.astype(np.float64)
+        per = 10 / (mx - mn)
+        under = x < mn
+        b = ((x - mn) * per).astype(np.int64)
+        hist = np.bincount(b[(~under) & (b < 10)], minlength=10)[:10]
+        out.update(hist=hist, underflow=int(under.sum()), overflow=int(((~under) & (b >= 10)).sum()))
+    return out

@@ -16,6 +16,18 @@
 //       the call-site options of libs/sfm/src/sfm_incremental_engine.cpp:1395-1473.
 //   ref_harness eval <in> <out>    ceres::Problem::Evaluate (cost, residuals,
 //       gradient, dense Jacobian) at the given parameters.
+//   ref_harness two-view <in> <out>   triangulate2View_Vector's per-match DLT
+//       and residual (libs/sfm/include/mvg/sfm/sfm_robust.h:152-195) and the
+//       keep decision of its callers (sfm_incremental_engine.cpp:977-1029 with
+//       residual thresholds, :492-533 without), on the reference's
+//       BrownPinholeCamera / PinholeCamera functions.
+//   ref_harness reject <in> <out>  badTrackRejector's decisions
+//       (sfm_incremental_engine.cpp:1047-1140) per measurement and track.
+//   ref_harness histogram <in> <out>  ComputeResidualsHistogram
+//       (sfm_incremental_engine.cpp:1550-1616): float residuals, MinMaxMeanMedian
+//       and Histogram<double>(min, max, 10).
+// The last three restate the engines' loops (whose classes need the whole
+// engine) around the reference's own camera, triangulation and histogram code.
 //
 // File format ("kv text"): a sequence of records `name count` followed by
 // `count` whitespace-separated numbers (%.17g).
@@ -32,7 +44,10 @@
 
 #include "ceres/ceres.h"
 #include "ceres/rotation.h"
+#include "mvg/camera/brown_pinhole_camera.h"
+#include "mvg/camera/pinhole_camera.h"
 #include "mvg/camera/projection.h"
+#include "mvg/utils/histogram.h"
 #include "mvg/multiview/nview_data_sets.h"
 #include "mvg/multiview/triangulation.h"
 #include "mvg/multiview/triangulation_nview.h"
@@ -376,6 +391,131 @@ static int RunTri(const KV& kv, const char* out) {
   return 0;
 }
 
+// Cameras as [R (row-major 9), t (3), f, ppx, ppy, k1, k2, k3] per camera.
+static std::vector<BrownPinholeCamera> LoadCameras(const std::vector<double>& v) {
+  std::vector<BrownPinholeCamera> cams;
+  for (size_t c = 0; c + 18 <= v.size(); c += 18) {
+    Mat3 R;
+    for (int r = 0; r < 3; ++r) for (int k = 0; k < 3; ++k) R(r, k) = v[c + 3 * r + k];
+    const Vec3 t(v[c + 9], v[c + 10], v[c + 11]);
+    cams.push_back(BrownPinholeCamera(v[c + 12], v[c + 13], v[c + 14], R, t, v[c + 15], v[c + 16], v[c + 17]));
+  }
+  return cams;
+}
+
+static int RunTwoView(const KV& kv, const char* out) {
+  const std::vector<BrownPinholeCamera> cams = LoadCameras(Get(kv, "cameras"));
+  const BrownPinholeCamera& cam1 = cams[0];
+  const BrownPinholeCamera& cam2 = cams[1];
+  const std::vector<double>& x1 = Get(kv, "x1");
+  const std::vector<double>& x2 = Get(kv, "x2");
+  const std::vector<double>& inlier = Get(kv, "inlier");
+  const double th1 = Get1(kv, "max_residual1", 1e300), th2 = Get1(kv, "max_residual2", 1e300);
+  const double min_angle = Get1(kv, "min_angle", 2.0);
+  const size_t n = x1.size() / 2;
+  std::vector<double> X, res, keep;
+  for (size_t i = 0; i < n; ++i) {
+    const Vec2 a(x1[2 * i], x1[2 * i + 1]), b(x2[2 * i], x2[2 * i + 1]);
+    Vec3 Xe = Vec3::Zero();
+    TriangulateDLT(cam1.projection_matrix_, a, cam2.projection_matrix_, b, &Xe);
+    const double r = (PinholeCamera::Residual(cam1.projection_matrix_, Xe, a) +
+                      PinholeCamera::Residual(cam2.projection_matrix_, Xe, b)) / 2.0;
+    bool k = inlier[i] != 0;
+    k = k && cam1.Residual(Xe, a) < th1 && cam2.Residual(Xe, b) < th2;
+    k = k && cam1.Depth(Xe) > 0 && cam2.Depth(Xe) > 0;
+    k = k && BrownPinholeCamera::AngleBetweenRay(cam1, cam2, a, b) > min_angle;
+    for (int j = 0; j < 3; ++j) X.push_back(Xe(j));
+    res.push_back(r);
+    keep.push_back(k ? 1 : 0);
+  }
+  KVWriter w(out);
+  w.put("X", X);
+  w.put("residual", res);
+  w.put("keep", keep);
+  return 0;
+}
+
+// Tracks as CSR (track_offsets, camera_index, xy) over the cameras, with one
+// 3D point per track; observations of a track in increasing camera order (the
+// order of the reference's SubmapTrack map).
+static int RunReject(const KV& kv, const char* out) {
+  const std::vector<BrownPinholeCamera> cams = LoadCameras(Get(kv, "cameras"));
+  const std::vector<double>& pts = Get(kv, "points");
+  const std::vector<double>& offs = Get(kv, "track_offsets");
+  const std::vector<double>& cam = Get(kv, "camera_index");
+  const std::vector<double>& xy = Get(kv, "xy");
+  const double precision = Get1(kv, "precision", 4.0);
+  const size_t nt = offs.size() - 1;
+  std::vector<double> obs_keep(cam.size(), 1.0), track_keep(nt, 1.0);
+  double rejected_tracks = 0, rejected_measurements = 0;
+  for (size_t t = 0; t < nt; ++t) {
+    const Vec3 X(pts[3 * t], pts[3 * t + 1], pts[3 * t + 2]);
+    double maxAngle = 0.0;
+    Vec3 originRay;
+    std::vector<size_t> erase;
+    for (size_t o = (size_t)offs[t]; o < (size_t)offs[t + 1]; ++o) {
+      const BrownPinholeCamera& c = cams[(size_t)cam[o]];
+      const double r = c.Residual(X, Vec2(xy[2 * o], xy[2 * o + 1]));
+      const Vec3 dir = (X - c.camera_center_).normalized();
+      if (o == (size_t)offs[t]) {
+        originRay = dir;
+      } else {
+        const double angle = R2D(acos(clamp(originRay.dot(dir), -1.0 + 1.e-8, 1.0 - 1.e-8)));
+        maxAngle = std::max(angle, maxAngle);
+      }
+      if (r > precision) erase.push_back(o);
+    }
+    if (maxAngle < 3) {
+      erase.clear();
+      for (size_t o = (size_t)offs[t]; o < (size_t)offs[t + 1]; ++o) erase.push_back(o);
+    }
+    for (size_t e = 0; e < erase.size(); ++e) obs_keep[erase[e]] = 0.0;
+    rejected_measurements += (double)erase.size();
+    const size_t remaining = (size_t)(offs[t + 1] - offs[t]) - erase.size();
+    if (!erase.empty() && remaining < 2) {
+      track_keep[t] = 0.0;
+      rejected_tracks += 1;
+    }
+  }
+  KVWriter w(out);
+  w.put("obs_keep", obs_keep);
+  w.put("track_keep", track_keep);
+  w.put1("rejected_measurements", rejected_measurements);
+  w.put1("rejected_tracks", rejected_tracks);
+  return 0;
+}
+
+static int RunHistogram(const KV& kv, const char* out) {
+  const std::vector<BrownPinholeCamera> cams = LoadCameras(Get(kv, "cameras"));
+  const std::vector<double>& pts = Get(kv, "points");
+  const std::vector<double>& offs = Get(kv, "track_offsets");
+  const std::vector<double>& cam = Get(kv, "camera_index");
+  const std::vector<double>& xy = Get(kv, "xy");
+  std::vector<float> vec_residuals;
+  for (size_t t = 0; t + 1 < offs.size(); ++t) {
+    const Vec3 X(pts[3 * t], pts[3 * t + 1], pts[3 * t + 2]);
+    for (size_t o = (size_t)offs[t]; o < (size_t)offs[t + 1]; ++o)
+      vec_residuals.push_back(cams[(size_t)cam[o]].Residual(X, Vec2(xy[2 * o], xy[2 * o + 1])));
+  }
+  KVWriter w(out);
+  if (vec_residuals.size() > 1) {
+    float mn, mx, mean, median;
+    MinMaxMeanMedian<float>(vec_residuals.begin(), vec_residuals.end(), mn, mx, mean, median);
+    mvg::utils::Histogram<double> histo(mn, mx, 10);
+    histo.Add(vec_residuals.begin(), vec_residuals.end());
+    std::vector<double> freq(histo.GetHist().begin(), histo.GetHist().end());
+    w.put1("min", mn);
+    w.put1("max", mx);
+    w.put1("mean", mean);
+    w.put1("median", median);
+    w.put("hist", freq);
+    w.put1("underflow", (double)histo.GetUnderflow());
+    w.put1("overflow", (double)histo.GetOverflow());
+  }
+  w.put1("count", (double)vec_residuals.size());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) { fprintf(stderr, "usage: ref_harness <mode> ...\n"); return 2; }
   const std::string mode = argv[1];
@@ -383,6 +523,9 @@ int main(int argc, char** argv) {
   if (mode == "tri" && argc == 4) return RunTri(ReadKV(argv[2]), argv[3]);
   if (mode == "ba" && argc == 4) return RunBA(ReadKV(argv[2]), argv[3]);
   if (mode == "eval" && argc == 4) return RunEval(ReadKV(argv[2]), argv[3]);
+  if (mode == "two-view" && argc == 4) return RunTwoView(ReadKV(argv[2]), argv[3]);
+  if (mode == "reject" && argc == 4) return RunReject(ReadKV(argv[2]), argv[3]);
+  if (mode == "histogram" && argc == 4) return RunHistogram(ReadKV(argv[2]), argv[3]);
   fprintf(stderr, "bad arguments\n");
   return 2;
 }

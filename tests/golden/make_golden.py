@@ -142,7 +142,27 @@ def ba_windows(tmp):
         ba_case(tmp, f"window_{cams}", sc, max_num_iterations=100)
 
 
+def sfm_scans(tmp):
+    """The engine-side scans: pair triangulation with the Resection filter
+    (residual thresholds 4 px) and the MakeInitialPair3D filter (no residual
+    test), the bad-track rejection (precision 4 px) and the residual
+    histogram, from the reference's own camera, DLT and histogram code."""
+    pr = scenes.engine_pair()
+    for name, th in (("resection", 4.0), ("initial", 1e300)):
+        r = oracle.ref_run("two-view", {"cameras": pr["cameras"], "x1": pr["x1"], "x2": pr["x2"],
+                                        "inlier": pr["inlier"], "max_residual1": th, "max_residual2": th,
+                                        "min_angle": 2.0}, tmp)
+        save(f"sfm_pair_{name}.npz", max_residual=th, min_angle=2.0, **pr, **{"ref_" + k: v for k, v in r.items()})
+    tr = scenes.engine_tracks()
+    kv = {k: tr[k] for k in ("cameras", "points", "track_offsets", "camera_index", "xy")}
+    r = oracle.ref_run("reject", dict(kv, precision=4.0), tmp)
+    h = oracle.ref_run("histogram", kv, tmp)
+    save("sfm_tracks.npz", precision=4.0, **tr, **{"ref_" + k: v for k, v in r.items()},
+         **{"ref_hist_" + k: v for k, v in h.items()})
+
+
 GENERATORS = {
+    "sfm_scans": sfm_scans,
     "tri_ring": lambda tmp: (tri_ring(tmp, 2, 12), tri_ring(tmp, 5, 6)),
     "tri_noisy": tri_noisy,
     "tri_tracks_f32": tri_tracks_f32,
@@ -205,6 +225,7 @@ def main():
     tri_long(tmp)
     ba_iterative(tmp)
     ba_windows(tmp)
+    sfm_scans(tmp)
 
 
 if __name__ == "__main__":

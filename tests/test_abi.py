@@ -10,7 +10,7 @@ import pytest
 
 from conftest import ROOT
 
-HEADERS = [os.path.join(ROOT, "include", h) for h in ("gbba.h", "gbtri.h")]
+HEADERS = [os.path.join(ROOT, "include", h) for h in ("gbba.h", "gbtri.h", "gbsfm.h")]
 
 
 def declared_functions():
@@ -43,8 +43,9 @@ def test_no_device_is_reported_not_faked(gb, abi):
 
 def test_struct_layout_matches_c(abi):
     fields = {"gbba_problem": abi.GbbaProblem, "gbba_options": abi.GbbaOptions, "gbba_summary": abi.GbbaSummary,
-              "gbba_tuning": abi.GbbaTuning}
-    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbba.h"', "int main(void){"]
+              "gbba_tuning": abi.GbbaTuning, "gbsfm_camera": abi.GbsfmCamera,
+              "gbsfm_residual_stats": abi.GbsfmResidualStats}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gbba.h"', '#include "gbsfm.h"', "int main(void){"]
     for cname, cls in fields.items():
         lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
         for f, _ in cls._fields_:
