@@ -30,6 +30,7 @@ Metric: observations x LM iterations per second (higher is better).
   triangulation  the batched FP32 triangulation (1,000,000 tracks): the
              whole call, and the main kernel's compulsory bytes over its
              device time (gbba_last_kernel_time) as a roofline fraction.
+  large      the large workload on the PCG path: FP64 and mixed time to cost.
   batched    gbba_solve_batched on the 4,096 local-BA windows.
   cpu_baseline  the CPU oracle (restatement of ceres LM + dense Schur,
              OpenMP over the host cores) on a bounded sample: 1 LM iteration.
@@ -370,6 +371,58 @@ def time_to_cost(h, abi, scene, dp, pristine, st, sptr, max_iters):
     return out
 
 
+def measure_large(h, abi, max_iters=40):
+    """The large workload (5,000 cameras with per-camera K3, 2,000,000 points,
+    ~20M observations with geometric(10) views, 2% outliers, Huber) on the
+    iterative path: block-Jacobi PCG on the implicit Schur complement.  The
+    plain FP64 run with ceres's stopping rule gives C*; the mixed run (FP32
+    Jacobians and Schur blocks, FP64 PCG vectors and cost) is traced and its
+    time to (1 + 1e-6) C* is the first traced iteration at or below it.
+    Device-resident inputs; wall times of whole gbba_solve calls, setup
+    included."""
+    import torch
+    scenes = importlib.import_module("3dreconstruction_gb300.scenes")
+    t0 = time.perf_counter()
+    sc = scenes.large_scene(seed=5, hold=(0, 1))
+    gen_s = time.perf_counter() - t0
+    no = len(sc["observations"])
+    dp = abi.DeviceProblem(sc, device="cuda")
+    st = dp.struct()
+    pristine = {f: getattr(dp, f).clone() for f in ("extrinsics", "intrinsics", "points")}
+    out = {"workload": f"large: {len(sc['extrinsics'])} cameras, {len(sc['points'])} points, {no} observations, "
+                       "per-camera K3, Huber(4), block-Jacobi PCG (ITERATIVE_SCHUR)",
+           "observations": no, "generation_s": gen_s}
+    traces = {}
+    for name, prec, ftol in (("fp64", abi.PRECISION_FP64, 1e-6), ("mixed", abi.PRECISION_MIXED, 1e-10)):
+        for f, v in pristine.items():
+            getattr(dp, f).copy_(v)
+        o = scenes.ba_options_for(sc, max_num_iterations=max_iters, precision=prec, function_tolerance=ftol,
+                                  linear_solver=abi.SOLVER_ITERATIVE_SCHUR, fp64_polish_iterations=0)
+        cap = max_iters + 2
+        tc, tt = np.zeros(cap), np.zeros(cap)
+        o.trace_cost, o.trace_time_s, o.trace_capacity = tc.ctypes.data, tt.ctypes.data, cap
+        summ = abi.GbbaSummary()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        h.check(h.lib.gbba_solve(h.h, ctypes.byref(st), ctypes.byref(o), ctypes.byref(summ)), f"large {name}")
+        torch.cuda.synchronize()
+        sec = time.perf_counter() - t0
+        out[name] = {"seconds": sec, "final_cost": summ.final_cost, "iterations": summ.num_iterations,
+                     "cg_iterations": summ.linear_solver_iterations, "termination": summ.termination_type,
+                     "obs_iter_per_s": no * summ.num_iterations / sec, "function_tolerance": ftol}
+        traces[name] = (tc, tt, min(cap, summ.num_iterations + 1))
+    target = out["fp64"]["final_cost"] * (1 + 1e-6)
+    for name in ("fp64", "mixed"):
+        tc, tt, n = traces[name]
+        out[name]["time_to_target_s"] = trace_time_to(tc, tt, n, target)
+    t64, tm = out["fp64"]["time_to_target_s"], out["mixed"]["time_to_target_s"]
+    out["c_star"] = out["fp64"]["final_cost"]
+    out["speedup"] = (t64 / tm) if (t64 and tm) else None
+    del dp
+    torch.cuda.empty_cache()
+    return out
+
+
 def make_scene(workload):
     scenes = importlib.import_module("3dreconstruction_gb300.scenes")
     if workload == "medium":
@@ -568,6 +621,8 @@ def run_ours(args):
         line["time_to_cost"] = time_to_cost(h, abi, scene, dp, pristine, st, sptr, args.ttc_iters)
     if rank == 0 and args.triangulation:
         line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup, peak)
+    if rank == 0 and args.large:
+        line["large"] = measure_large(h, abi)
     if rank == 0 and args.batched_windows > 0:
         line["batched"] = measure_batched(h, abi, args.batched_windows)
     if rank == 0 and args.cpu_baseline:
@@ -592,6 +647,8 @@ def main():
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")
+    ap.add_argument("--no-large", dest="large", action="store_false",
+                    help="skip the large PCG workload (5,000 cameras, 20M observations)")
     ap.add_argument("--batched-windows", type=int, default=4096,
                     help="windows of the batched local-BA measurement (0: skip)")
     args = ap.parse_args()
