@@ -371,7 +371,7 @@ def time_to_cost(h, abi, scene, dp, pristine, st, sptr, max_iters):
     return out
 
 
-def measure_large(h, abi, max_iters=40):
+def measure_large(h, abi, max_iters=100):
     """The large workload (5,000 cameras with per-camera K3, 2,000,000 points,
     ~20M observations with geometric(10) views, 2% outliers, Huber) on the
     iterative path: block-Jacobi PCG on the implicit Schur complement.  The
@@ -409,7 +409,11 @@ def measure_large(h, abi, max_iters=40):
         sec = time.perf_counter() - t0
         out[name] = {"seconds": sec, "final_cost": summ.final_cost, "iterations": summ.num_iterations,
                      "cg_iterations": summ.linear_solver_iterations, "termination": summ.termination_type,
-                     "obs_iter_per_s": no * summ.num_iterations / sec, "function_tolerance": ftol}
+                     "obs_iter_per_s": no * summ.num_iterations / sec, "function_tolerance": ftol,
+                     "phases_s": {"solver_total": summ.total_time_s, "schur": summ.jacobian_time_s,
+                                  "pcg_and_back_substitution": summ.linear_solver_time_s,
+                                  "candidate_cost": summ.residual_time_s,
+                                  "schur_kernels": summ.schur_kernel_time_s}}
         traces[name] = (tc, tt, min(cap, summ.num_iterations + 1))
     target = out["fp64"]["final_cost"] * (1 + 1e-6)
     for name in ("fp64", "mixed"):
