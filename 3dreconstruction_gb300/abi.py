@@ -160,6 +160,33 @@ class GbsfmResidualStats(C.Structure):
                 ("median", C.c_double), ("hist", C.c_int64 * 10), ("underflow", C.c_int64), ("overflow", C.c_int64)]
 
 
+LOCK_AS_REFERENCE, LOCK_FIRST_ADDED, LOCK_NONE = 0, 1, 2
+
+
+class GbsfmAcransacParams(C.Structure):
+    _fields_ = [("sample_size", C.c_int32), ("max_models", C.c_int32), ("logalpha0", C.c_double),
+                ("mult_error", C.c_double), ("max_threshold", C.c_double)]
+
+
+class GbsfmEngineState(C.Structure):
+    """gbsfm_engine_state: the incremental engine's maps as dense arrays."""
+    _fields_ = [("num_images", C.c_int64), ("cameras", C.c_void_p), ("reconstructed", C.c_void_p),
+                ("intrinsic_group", C.c_void_p), ("num_intrinsic_groups", C.c_int64),
+                ("group_intrinsics", C.c_void_p), ("num_features", C.c_int64), ("feature_offsets", C.c_void_p),
+                ("features", C.c_void_p), ("num_points", C.c_int64), ("points", C.c_void_p),
+                ("num_entries", C.c_int64), ("track_offsets", C.c_void_p), ("track_image", C.c_void_p),
+                ("track_feature", C.c_void_p)]
+
+
+class GbsfmBaArrays(C.Structure):
+    """gbsfm_ba_arrays: outputs of gbsfm_pack_ba."""
+    _fields_ = [("extrinsics", C.c_void_p), ("intrinsics", C.c_void_p), ("points", C.c_void_p),
+                ("observations", C.c_void_p), ("camera_index", C.c_void_p), ("intrinsic_index", C.c_void_p),
+                ("point_index", C.c_void_p), ("camera_constant", C.c_void_p), ("camera_image", C.c_void_p),
+                ("num_cameras", C.c_int64), ("num_observations", C.c_int64), ("measurements", C.c_int64),
+                ("locked_camera", C.c_int64)]
+
+
 def default_options(**kw):
     """ceres::Solver::Options defaults (include/ceres/solver.h:81-129)."""
     o = GbbaOptions()
@@ -289,6 +316,78 @@ class DeviceProblem:
                 "points": self.points.cpu().numpy()}
 
 
+class EnginePack:
+    """An engine state (the dict of scenes.engine_state()) and the output
+    arrays of gbsfm_pack_ba, on the host (numpy) or on a device (torch), with
+    the structs that point at them."""
+
+    STATE = {"cameras": np.float64, "reconstructed": np.uint8, "intrinsic_group": np.uint32,
+             "group_intrinsics": np.float64, "feature_offsets": np.int64, "features": np.float32,
+             "points": np.float64, "track_offsets": np.int64, "track_image": np.uint32, "track_feature": np.uint32}
+
+    def __init__(self, state, device=None):
+        self.device = device
+        self.ni = len(state["reconstructed"])
+        self.ng = len(np.asarray(state["group_intrinsics"]).reshape(-1, 6))
+        self.nf = len(np.asarray(state["features"]).reshape(-1, 2))
+        self.nt = len(state["track_offsets"]) - 1
+        self.ne = len(state["track_image"])
+        self.arrays = {k: self._put(np.ascontiguousarray(np.asarray(state[k], t))) for k, t in self.STATE.items()}
+        shapes = {"extrinsics": (6 * self.ni, np.float64), "intrinsics": (6 * self.ng, np.float64),
+                  "points": (3 * self.nt, np.float64), "observations": (2 * self.ne, np.float64),
+                  "camera_index": (self.ne, np.uint32), "intrinsic_index": (self.ne, np.uint32),
+                  "point_index": (self.ne, np.uint32), "camera_constant": (self.ni, np.uint8),
+                  "camera_image": (self.ni, np.uint32)}
+        self.out = {k: self._put(np.zeros(max(n, 1), t)) for k, (n, t) in shapes.items()}
+        self.memory = MEMORY_HOST if device is None else MEMORY_DEVICE
+
+    def _put(self, a):
+        if self.device is None:
+            return a
+        import torch
+        if a.dtype == np.uint32:
+            a = a.view(np.int32)
+        return torch.from_numpy(a.copy()).to(self.device)
+
+    def state_struct(self):
+        s = GbsfmEngineState()
+        a = self.arrays
+        s.num_images, s.num_intrinsic_groups, s.num_features = self.ni, self.ng, self.nf
+        s.num_points, s.num_entries = self.nt, self.ne
+        for k in ("cameras", "reconstructed", "intrinsic_group", "group_intrinsics", "feature_offsets", "features",
+                  "points", "track_offsets", "track_image", "track_feature"):
+            setattr(s, k, _ptr(a[k]))
+        return s
+
+    def out_struct(self):
+        o = GbsfmBaArrays()
+        for k, v in self.out.items():
+            setattr(o, k, _ptr(v))
+        return o
+
+    def pack(self, lib, h, first_added, lock=LOCK_AS_REFERENCE):
+        """Runs gbsfm_pack_ba; returns (status, GbsfmBaArrays)."""
+        s, o = self.state_struct(), self.out_struct()
+        st = lib.gbsfm_pack_ba(h, C.byref(s), int(first_added), int(lock), C.byref(o), self.memory)
+        return st, o
+
+    def result(self, o):
+        """The packed problem as numpy arrays, cut to the counts of `o`."""
+        nc, no = o.num_cameras, o.num_observations
+        get = {}
+        for k, v in self.out.items():
+            a = v if self.device is None else v.cpu().numpy()
+            if k in ("camera_index", "intrinsic_index", "point_index", "camera_image"):
+                a = a.view(np.uint32)
+            get[k] = a
+        return {"extrinsics": get["extrinsics"][:6 * nc].reshape(-1, 6), "intrinsics": get["intrinsics"][:6 * self.ng],
+                "points": get["points"][:3 * self.nt], "observations": get["observations"][:2 * no].reshape(-1, 2),
+                "camera_index": get["camera_index"][:no], "intrinsic_index": get["intrinsic_index"][:no],
+                "point_index": get["point_index"][:no], "camera_constant": get["camera_constant"][:nc],
+                "camera_image": get["camera_image"][:nc], "num_cameras": nc, "num_observations": no,
+                "measurements": o.measurements, "locked_camera": o.locked_camera}
+
+
 def declare_gbba(lib):
     """Attach argument / return types to the C-ABI symbols of libgbba."""
     P = C.POINTER
@@ -328,6 +427,13 @@ def declare_gbba(lib):
     lib.gbsfm_residual_histogram.argtypes = [vp, vp, C.c_int64, vp, C.c_int64, vp, vp, vp, P(GbsfmResidualStats),
                                              C.c_int32]
     lib.gbsfm_residual_histogram.restype = C.c_int
+    lib.gbsfm_pack_ba.argtypes = [vp, P(GbsfmEngineState), C.c_int64, C.c_int32, P(GbsfmBaArrays), C.c_int32]
+    lib.gbsfm_pack_ba.restype = C.c_int
+    lib.gbsfm_unpack_ba.argtypes = [vp, C.c_int64, vp, vp, vp, C.c_int64, vp, C.c_int64, vp, C.c_int32]
+    lib.gbsfm_unpack_ba.restype = C.c_int
+    lib.gbsfm_acransac_score.argtypes = [vp, P(GbsfmAcransacParams), C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp,
+                                         vp, C.c_int32]
+    lib.gbsfm_acransac_score.restype = C.c_int
     lib.gbba_last_kernel_time.argtypes = [vp, vp]
     lib.gbba_last_kernel_time.restype = C.c_int
     lib.gbtri_dlt2_batched.argtypes = [vp, C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp, C.c_int32]
@@ -348,5 +454,6 @@ EXPORTED_SYMBOLS = (
     "gbba_abi_version", "gbba_launch_count", "gbba_last_kernel_time", "gbba_solve", "gbba_solve_batched", "gbba_autotune",
     "gbba_project_forward", "gbba_project_backward", "gbba_project_backward_mixed", "gbba_project_forward_noalloc",
     "gbtri_dlt2_batched", "gbtri_nview_batched", "gbtri_nview_batched_f32", "gbtri_refine_gn",
-    "gbsfm_triangulate_pair", "gbsfm_reject_tracks", "gbsfm_residual_histogram",
+    "gbsfm_triangulate_pair", "gbsfm_reject_tracks", "gbsfm_residual_histogram", "gbsfm_pack_ba",
+    "gbsfm_unpack_ba", "gbsfm_acransac_score",
 )

@@ -5,7 +5,9 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -119,7 +121,7 @@ struct gbba_handle {
   int prio_hi = 0;
   // observation pairs per work item of the camera-pair products (gbba_autotune)
   int pair_chunk = 128;
-  // device time of the main kernel of the last triangulation call
+  // device time of the main kernel(s) of the last triangulation or engine-scan call
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
   bool kernel_timed = false;
 };
@@ -134,6 +136,39 @@ inline void check_launch(gbba_handle* h) {
 }
 
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// Runs the body of an engine-side entry point (gbsfm_*) on the handle's
+// device and stream, turning an internal error into its status.
+template <typename F>
+gbba_status sfm_guard(gbba_handle* h, F&& f) {
+  if (!h) return GBBA_ERROR_INVALID_ARGUMENT;
+  try {
+    GBBA_CUDA(cudaSetDevice(h->device));
+    h->active = h->stream;
+    return f();
+  } catch (const Error& e) {
+    if (std::getenv("GBBA_VERBOSE")) fprintf(stderr, "gbsfm: %s\n", e.what.c_str());
+    cudaGetLastError();
+    return e.status;
+  }
+}
+
+// Grid of a grid-stride loop over n items: enough blocks to cover them, at
+// most 16 per SM.
+inline unsigned grid_for(gbba_handle* h, int64_t n, int threads) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), (int64_t)h->sm_count * 16));
+}
+
+// Brackets the main kernel(s) of a call with the handle's events; the span is
+// read back by gbba_last_kernel_time.
+struct KernelTimer {
+  gbba_handle* h;
+  explicit KernelTimer(gbba_handle* hh) : h(hh) { GBBA_CUDA(cudaEventRecord(h->ev_k0, h->active)); }
+  void stop() {
+    GBBA_CUDA(cudaEventRecord(h->ev_k1, h->active));
+    h->kernel_timed = true;
+  }
+};
 
 // Device view of an input array: the caller's pointer (device memory) or a
 // staged copy (host memory).

@@ -258,19 +258,341 @@ __global__ void __launch_bounds__(256) k_residual_stats(const float* __restrict_
   if (threadIdx.x < 12 && sh_hist[threadIdx.x]) atomicAdd(&hist[threadIdx.x], (unsigned long long)sh_hist[threadIdx.x]);
 }
 
-template <typename F>
-gbba_status sfm_guard(gbba_handle* h, F&& f) {
-  if (!h) return GBBA_ERROR_INVALID_ARGUMENT;
-  try {
-    GBBA_CUDA(cudaSetDevice(h->device));
-    h->active = h->stream;
-    return f();
-  } catch (const Error& e) {
-    if (std::getenv("GBBA_VERBOSE")) fprintf(stderr, "gbsfm: %s\n", e.what.c_str());
-    cudaGetLastError();
-    return e.status;
+// ---- Problem assembly ------------------------------------------------------
+
+// ceres::RotationMatrixToQuaternion (Shoemake's branch on the trace, then on
+// the largest diagonal entry; include/ceres/rotation.h:312-350) followed by
+// QuaternionToAngleAxis (:266-306), which maps a rotation of more than pi
+// back below pi through atan2 of the negated pair.  R is row-major:
+// R(i, j) = R[3 i + j].
+__device__ void rotation_to_angle_axis(const double* R, double aa[3]) {
+  double q[4];
+  const double trace = R[0] + R[4] + R[8];
+  if (trace >= 0.0) {
+    double s = sqrt(trace + 1.0);
+    q[0] = 0.5 * s;
+    s = 0.5 / s;
+    q[1] = (R[7] - R[5]) * s;
+    q[2] = (R[2] - R[6]) * s;
+    q[3] = (R[3] - R[1]) * s;
+  } else {
+    int i = R[4] > R[0] ? 1 : 0;
+    if (R[8] > R[4 * i]) i = 2;
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    double s = sqrt(R[4 * i] - R[4 * j] - R[4 * k] + 1.0);
+    q[i + 1] = 0.5 * s;
+    s = 0.5 / s;
+    q[0] = (R[3 * k + j] - R[3 * j + k]) * s;
+    q[j + 1] = (R[3 * j + i] + R[3 * i + j]) * s;
+    q[k + 1] = (R[3 * k + i] + R[3 * i + k]) * s;
+  }
+  const double sin2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  double scale = 2.0;  // zero rotation: the first term of the series
+  if (sin2 > 0.0) {
+    const double sn = sqrt(sin2), cs = q[0];
+    scale = 2.0 * (cs < 0.0 ? atan2(-sn, -cs) : atan2(sn, cs)) / sn;
+  }
+  aa[0] = q[1] * scale;
+  aa[1] = q[2] * scale;
+  aa[2] = q[3] * scale;
+}
+
+// ceres::AngleAxisToRotationMatrix (include/ceres/rotation.h:377-414), row-major
+// output: Rodrigues' formula with the unit axis, or its first-order form when
+// theta^2 is not above the double epsilon.
+__device__ void angle_axis_to_rotation(const double aa[3], double R[9]) {
+  const double th2 = aa[0] * aa[0] + aa[1] * aa[1] + aa[2] * aa[2];
+  if (th2 > 2.220446049250313e-16) {
+    const double th = sqrt(th2);
+    const double wx = aa[0] / th, wy = aa[1] / th, wz = aa[2] / th;
+    double sn, cs;
+    sincos(th, &sn, &cs);
+    const double oc = 1.0 - cs;
+    R[0] = cs + wx * wx * oc;
+    R[1] = wx * wy * oc - wz * sn;
+    R[2] = wy * sn + wx * wz * oc;
+    R[3] = wz * sn + wx * wy * oc;
+    R[4] = cs + wy * wy * oc;
+    R[5] = -wx * sn + wy * wz * oc;
+    R[6] = -wy * sn + wx * wz * oc;
+    R[7] = wx * sn + wy * wz * oc;
+    R[8] = cs + wz * wz * oc;
+  } else {
+    R[0] = 1.0;
+    R[1] = -aa[2];
+    R[2] = aa[1];
+    R[3] = aa[2];
+    R[4] = 1.0;
+    R[5] = -aa[0];
+    R[6] = -aa[1];
+    R[7] = aa[0];
+    R[8] = 1.0;
   }
 }
+
+constexpr uint32_t kNoCamera = 0xffffffffu;
+constexpr int kPackThreads = 256;
+constexpr int kPackPer = 8;  // entries per thread and tile: a tile is 2048 entries
+constexpr int64_t kPackTile = (int64_t)kPackThreads * kPackPer;
+
+// Error bits of the pack and the write-back.
+enum : unsigned long long {
+  kBadImage = 1,       // an entry names an image outside the state
+  kBadFeature = 2,     // an entry names a feature outside its image
+  kBadOffsets = 4,     // track_offsets is not a CSR of num_entries entries
+  kBadGroup = 8,       // an intrinsic group outside the groups
+  kLockPastEnd = 16,   // the reference's lock reads past its observations
+  kBadCameraImage = 32 // a write-back ordinal names an image outside the state
+};
+
+// Exclusive block-wide count of `flag` over blockDim.x <= 1024 threads;
+// returns the thread's offset and leaves the block total in *total.
+__device__ __forceinline__ uint32_t block_exclusive_count(bool flag, uint32_t* sh_warp, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const unsigned mask = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) sh_warp[warp] = __popc(mask);
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+  for (int w = 0; w < nw; ++w) {
+    const uint32_t c = sh_warp[w];
+    before += w < warp ? c : 0u;
+    all += c;
+  }
+  __syncthreads();  // sh_warp is reused by the next call
+  *total = all;
+  return before + __popc(mask & ((1u << lane) - 1u));
+}
+
+// One block over the images: camera ordinals (ascending image id among the
+// reconstructed, the key order of map_Camera), the extrinsic blocks
+// [angle-axis, t] and the ordinal -> image table.
+__global__ void __launch_bounds__(1024) k_pack_images(int64_t ni, const uint8_t* __restrict__ rec,
+                                                      const gbsfm_camera* __restrict__ cams,
+                                                      const uint32_t* __restrict__ group, int64_t num_groups,
+                                                      uint32_t* __restrict__ ordinal, double* __restrict__ ext,
+                                                      uint32_t* __restrict__ camera_image,
+                                                      unsigned long long* __restrict__ counters) {
+  __shared__ uint32_t sh_warp[32];
+  uint32_t base = 0;
+  unsigned long long err = 0;
+  for (int64_t c0 = 0; c0 < ni; c0 += blockDim.x) {
+    const int64_t i = c0 + threadIdx.x;
+    const bool flag = i < ni && rec[i] != 0;
+    uint32_t total;
+    const uint32_t pos = base + block_exclusive_count(flag, sh_warp, &total);
+    if (i < ni) ordinal[i] = flag ? pos : kNoCamera;
+    if (flag) {
+      const gbsfm_camera& c = cams[i];
+      double aa[3];
+      rotation_to_angle_axis(c.R, aa);
+      double* e = ext + 6 * (int64_t)pos;
+      e[0] = aa[0];
+      e[1] = aa[1];
+      e[2] = aa[2];
+      e[3] = c.t[0];
+      e[4] = c.t[1];
+      e[5] = c.t[2];
+      if (camera_image) camera_image[pos] = (uint32_t)i;
+      if (group[i] >= (uint64_t)num_groups) err |= kBadGroup;
+    }
+    base += total;
+  }
+  if (err) atomicOr(&counters[2], err);
+  if (threadIdx.x == 0) counters[0] = base;
+}
+
+__device__ __forceinline__ bool entry_kept(int64_t e, int64_t ne, int64_t ni, const uint32_t* __restrict__ img,
+                                           const uint32_t* __restrict__ ordinal, uint32_t* im) {
+  if (e >= ne) return false;
+  *im = img[e];
+  return *im < (uint64_t)ni && ordinal[*im] != kNoCamera;
+}
+
+// Pass 1 over the entries: kept entries per tile of 2048, and the checks of
+// the image ids and of the track offsets.
+__global__ void __launch_bounds__(kPackThreads) k_pack_count(int64_t ne, int64_t ni, int64_t nt,
+                                                             const int64_t* __restrict__ offs,
+                                                             const uint32_t* __restrict__ img,
+                                                             const uint32_t* __restrict__ ordinal,
+                                                             uint32_t* __restrict__ tile_count,
+                                                             unsigned long long* __restrict__ counters) {
+  __shared__ uint32_t sh_warp[32];
+  unsigned long long err = 0;
+  uint32_t kept = 0;
+  const int64_t tile = blockIdx.x * kPackTile;
+#pragma unroll
+  for (int j = 0; j < kPackPer; ++j) {
+    const int64_t e = tile + j * kPackThreads + threadIdx.x;
+    uint32_t im = 0;
+    kept += entry_kept(e, ne, ni, img, ordinal, &im) ? 1u : 0u;
+    if (e < ne && im >= (uint64_t)ni) err |= kBadImage;
+  }
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t <= nt; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t o = offs[t];
+    const bool bad = (t == 0 && o != 0) || (t == nt && o != ne) || (t < nt && offs[t + 1] < o);
+    if (bad) err |= kBadOffsets;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+  if ((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = kept;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t s = 0;
+    for (int w = 0; w < kPackThreads / 32; ++w) s += sh_warp[w];
+    tile_count[blockIdx.x] = s;
+  }
+  if (err) atomicOr(&counters[2], err);
+}
+
+// Exclusive scan of the tile counts in place (one block); the total is the
+// observation count.
+__global__ void __launch_bounds__(1024) k_pack_scan(uint32_t* __restrict__ tile_count, int64_t nb,
+                                                    unsigned long long* __restrict__ counters) {
+  __shared__ uint32_t sh[1024];
+  __shared__ unsigned long long sh_base;
+  if (threadIdx.x == 0) sh_base = 0;
+  __syncthreads();
+  for (int64_t c0 = 0; c0 < nb; c0 += 1024) {
+    const int64_t i = c0 + threadIdx.x;
+    const uint32_t v = i < nb ? tile_count[i] : 0u;
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int d = 1; d < 1024; d <<= 1) {  // Hillis-Steele inclusive scan
+      const uint32_t add = threadIdx.x >= d ? sh[threadIdx.x - d] : 0u;
+      __syncthreads();
+      sh[threadIdx.x] += add;
+      __syncthreads();
+    }
+    const unsigned long long base = sh_base;
+    if (i < nb) tile_count[i] = (uint32_t)(base + sh[threadIdx.x] - v);
+    __syncthreads();
+    if (threadIdx.x == 1023) sh_base = base + sh[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) counters[1] = sh_base;
+}
+
+// Pass 2: the same tiles in entry order; each kept entry gets its place from
+// the tile base and the block-wide count, and gathers its feature (float ->
+// double), camera ordinal, intrinsic group and track (binary search of the
+// offsets: the last track that starts at or before the entry).
+__global__ void __launch_bounds__(kPackThreads) k_pack_gather(
+    int64_t ne, int64_t ni, int64_t nt, int64_t nf, const int64_t* __restrict__ offs,
+    const uint32_t* __restrict__ img, const uint32_t* __restrict__ feat, const uint32_t* __restrict__ ordinal,
+    const uint32_t* __restrict__ group, const int64_t* __restrict__ feature_offsets,
+    const float* __restrict__ features, const uint32_t* __restrict__ tile_base, double* __restrict__ obs,
+    uint32_t* __restrict__ camera_index, uint32_t* __restrict__ intrinsic_index, uint32_t* __restrict__ point_index,
+    unsigned long long* __restrict__ counters) {
+  __shared__ uint32_t sh_warp[32];
+  unsigned long long err = 0;
+  uint32_t running = tile_base[blockIdx.x];
+  const int64_t tile = blockIdx.x * kPackTile;
+  for (int j = 0; j < kPackPer; ++j) {
+    const int64_t e = tile + j * kPackThreads + threadIdx.x;
+    uint32_t im = 0, total;
+    const bool flag = entry_kept(e, ne, ni, img, ordinal, &im);
+    const uint32_t pos = running + block_exclusive_count(flag, sh_warp, &total);
+    if (flag) {
+      const uint32_t f = feat[e];
+      const int64_t a = feature_offsets[im], b = feature_offsets[im + 1];
+      const bool ok = a >= 0 && b <= nf && (int64_t)f < b - a;
+      float x = 0.0f, y = 0.0f;
+      if (ok) {
+        x = features[2 * (a + f)];
+        y = features[2 * (a + f) + 1];
+      } else {
+        err |= kBadFeature;
+      }
+      int64_t lo = 0, hi = nt;  // offs[lo] <= e < offs[hi] on a valid CSR
+      while (hi - lo > 1) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (offs[mid] <= e) lo = mid; else hi = mid;
+      }
+      obs[2 * (int64_t)pos] = (double)x;
+      obs[2 * (int64_t)pos + 1] = (double)y;
+      camera_index[pos] = ordinal[im];
+      intrinsic_index[pos] = group[im];
+      point_index[pos] = (uint32_t)lo;
+    }
+    running += total;
+  }
+  if (err) atomicOr(&counters[2], err);
+}
+
+// The locked block: the reference's mutable_camera_extrinsic_for_observation
+// (ordinal of the first-added image) is the block of observation number
+// `ordinal`; std::map::operator[] gives ordinal 0 to an image without a camera.
+__global__ void k_pack_lock(int32_t lock, int64_t first, const uint32_t* __restrict__ ordinal,
+                            const uint32_t* __restrict__ camera_index, uint8_t* __restrict__ camera_constant,
+                            unsigned long long* __restrict__ counters) {
+  const unsigned long long nc = counters[0], nobs = counters[1];
+  long long locked = -1;
+  if (lock != GBSFM_LOCK_NONE && first >= 0 && nc > 0) {
+    const uint32_t o = ordinal[first];
+    if (lock == GBSFM_LOCK_FIRST_ADDED) {
+      locked = o == kNoCamera ? -1 : (long long)o;
+    } else {
+      const unsigned long long k = o == kNoCamera ? 0ull : o;
+      if (k < nobs) locked = camera_index[k];
+      else atomicOr(&counters[2], kLockPastEnd);
+    }
+  }
+  if (locked >= 0 && camera_constant) camera_constant[locked] = 1;
+  counters[3] = (unsigned long long)(locked + 1);
+}
+
+// Write-back checks: every ordinal's image inside the state, every such
+// image's group inside the groups.
+__global__ void __launch_bounds__(128) k_unpack_check(int64_t nc, const uint32_t* __restrict__ camera_image,
+                                                      int64_t ni, const uint32_t* __restrict__ group, int64_t ng,
+                                                      unsigned long long* __restrict__ err) {
+  unsigned long long e = 0;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t im = camera_image[c];
+    if (im >= (uint64_t)ni) e |= kBadCameraImage;
+    else if (group[im] >= (uint64_t)ng) e |= kBadGroup;
+  }
+  if (e) atomicOr(err, e);
+}
+
+// Write-back: camera_image[c] becomes the BrownPinholeCamera of the refined
+// block c and its group's intrinsics.  Runs only after k_unpack_check found
+// nothing, so nothing is written for a bad call.
+__global__ void __launch_bounds__(128) k_unpack(int64_t nc, const double* __restrict__ ext,
+                                                const uint32_t* __restrict__ camera_image,
+                                                const double* __restrict__ intr, const uint32_t* __restrict__ group,
+                                                const unsigned long long* __restrict__ err,
+                                                gbsfm_camera* __restrict__ cams) {
+  if (*err) return;
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nc; c += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t im = camera_image[c];
+    const double* e = ext + 6 * c;
+    const double* k = intr + 6 * (int64_t)group[im];
+    gbsfm_camera out;
+    const double aa[3] = {e[0], e[1], e[2]};
+    angle_axis_to_rotation(aa, out.R);
+    out.t[0] = e[3];
+    out.t[1] = e[4];
+    out.t[2] = e[5];
+    out.f = k[0];
+    out.ppx = k[1];
+    out.ppy = k[2];
+    out.k1 = k[3];
+    out.k2 = k[4];
+    out.k3 = k[5];
+    cams[im] = out;
+  }
+}
+
+const char* pack_error(unsigned long long bits) {
+  if (bits & kBadOffsets) return "track_offsets is not a CSR of num_entries entries";
+  if (bits & kBadImage) return "a track entry names an image outside the state";
+  if (bits & kBadFeature) return "a track entry names a feature outside its image";
+  if (bits & kBadGroup) return "an intrinsic group out of range";
+  if (bits & kLockPastEnd) return "the first-added camera's ordinal is past the observations";
+  return "a camera ordinal names an image outside the state";
+}
+
 
 // Device views of a batch of tracks.  Offsets and camera indices are checked
 // on the host first, so a bad batch is never indexed.
@@ -331,9 +653,6 @@ TrackBatch stage_tracks(gbba_handle* h, const gbsfm_camera* cameras, int64_t nc,
   return tb;
 }
 
-unsigned grid_for(gbba_handle* h, int64_t n, int threads) {
-  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, threads), (int64_t)h->sm_count * 16));
-}
 
 }  // namespace
 }  // namespace gbba
@@ -460,6 +779,131 @@ gbba_status gbsfm_residual_histogram(gbba_handle* h, const gbsfm_camera* cameras
     for (int i = 0; i < 10; ++i) stats->hist[i] = (int64_t)hh[i];
     stats->underflow = (int64_t)hh[10];
     stats->overflow = (int64_t)hh[11];
+    return GBBA_SUCCESS;
+  });
+}
+
+gbba_status gbsfm_pack_ba(gbba_handle* h, const gbsfm_engine_state* st, int64_t first_added_image, int32_t lock,
+                          gbsfm_ba_arrays* out, int32_t memory) {
+  if (!st || !out || lock < GBSFM_LOCK_AS_REFERENCE || lock > GBSFM_LOCK_NONE) return GBBA_ERROR_INVALID_ARGUMENT;
+  const int64_t ni = st->num_images, ng = st->num_intrinsic_groups, nf = st->num_features, nt = st->num_points,
+                ne = st->num_entries;
+  if (ni < 0 || ng < 0 || nf < 0 || nt < 0 || ne < 0 || first_added_image >= ni || first_added_image < -1)
+    return GBBA_ERROR_INVALID_ARGUMENT;
+  if ((ni > 0 && (!st->cameras || !st->reconstructed || !st->intrinsic_group || !out->extrinsics)) ||
+      !st->feature_offsets || (nf > 0 && !st->features) || !st->track_offsets ||
+      (ne > 0 && (!st->track_image || !st->track_feature || !out->observations || !out->camera_index ||
+                  !out->intrinsic_index || !out->point_index)) ||
+      (ng > 0 && (!st->group_intrinsics || !out->intrinsics)) || (nt > 0 && (!st->points || !out->points)))
+    return GBBA_ERROR_INVALID_ARGUMENT;
+  if (ni > 0xfffffffeLL || ne > 0xffffffffLL || nt > 0xffffffffLL) return GBBA_ERROR_TOO_LARGE;
+  return sfm_guard(h, [&]() {
+    out->num_cameras = out->num_observations = 0;
+    out->measurements = ne;
+    out->locked_camera = -1;
+    const int64_t nb = std::max<int64_t>(1, ceil_div(ne, kPackTile));
+    h->arena.reset();
+    h->arena.reserve(sizeof(gbsfm_camera) * ni + 16 * ni + sizeof(int64_t) * (ni + nt + 2) + sizeof(float) * 2 * nf +
+                     sizeof(uint32_t) * 2 * ne + sizeof(double) * 6 * ni + sizeof(double) * 2 * ne +
+                     sizeof(uint32_t) * 3 * ne + 4 * nb + 256 * 24);
+    const gbsfm_camera* dcam = in_view(h, st->cameras, ni, memory);
+    const uint8_t* drec = in_view(h, st->reconstructed, ni, memory);
+    const uint32_t* dgrp = in_view(h, st->intrinsic_group, ni, memory);
+    const int64_t* dfo = in_view(h, st->feature_offsets, ni + 1, memory);
+    const float* dft = in_view(h, st->features, 2 * nf, memory);
+    const int64_t* doff = in_view(h, st->track_offsets, nt + 1, memory);
+    const uint32_t* dimg = in_view(h, st->track_image, ne, memory);
+    const uint32_t* dfeat = in_view(h, st->track_feature, ne, memory);
+    double* dext = out_view(h, out->extrinsics, 6 * ni, memory);
+    double* dobs = out_view(h, out->observations, 2 * ne, memory);
+    uint32_t* dci = out_view(h, out->camera_index, ne, memory);
+    uint32_t* dii = out_view(h, out->intrinsic_index, ne, memory);
+    uint32_t* dpi = out_view(h, out->point_index, ne, memory);
+    uint8_t* dcc = out_view(h, out->camera_constant, ni, memory);
+    uint32_t* dcimg = out_view(h, out->camera_image, ni, memory);
+    uint32_t* ordinal = h->arena.take<uint32_t>(std::max<int64_t>(1, ni));
+    uint32_t* tiles = h->arena.take<uint32_t>(nb);
+    unsigned long long* counters = h->arena.take<unsigned long long>(4);
+    // intrinsic groups and points enter the problem as they are
+    if (ng > 0 && out->intrinsics != st->group_intrinsics)
+      GBBA_CUDA(cudaMemcpyAsync(out->intrinsics, st->group_intrinsics, sizeof(double) * 6 * ng, cudaMemcpyDefault,
+                                h->active));
+    if (nt > 0 && out->points != st->points)
+      GBBA_CUDA(cudaMemcpyAsync(out->points, st->points, sizeof(double) * 3 * nt, cudaMemcpyDefault, h->active));
+    GBBA_CUDA(cudaMemsetAsync(counters, 0, 4 * sizeof(unsigned long long), h->active));
+    if (dcc && ni > 0) GBBA_CUDA(cudaMemsetAsync(dcc, 0, ni, h->active));
+    KernelTimer timer(h);
+    if (ni > 0) {
+      k_pack_images<<<1, 1024, 0, h->active>>>(ni, drec, dcam, dgrp, ng, ordinal, dext, dcimg, counters);
+      check_launch(h);
+    }
+    k_pack_count<<<(unsigned)nb, kPackThreads, 0, h->active>>>(ne, ni, nt, doff, dimg, ordinal, tiles, counters);
+    check_launch(h);
+    k_pack_scan<<<1, 1024, 0, h->active>>>(tiles, nb, counters);
+    check_launch(h);
+    if (ne > 0) {
+      k_pack_gather<<<(unsigned)nb, kPackThreads, 0, h->active>>>(ne, ni, nt, nf, doff, dimg, dfeat, ordinal, dgrp,
+                                                                  dfo, dft, tiles, dobs, dci, dii, dpi, counters);
+      check_launch(h);
+    }
+    if (ni > 0) {
+      k_pack_lock<<<1, 1, 0, h->active>>>(lock, first_added_image, ordinal, dci, dcc, counters);
+      check_launch(h);
+    }
+    timer.stop();
+    unsigned long long* hc = reinterpret_cast<unsigned long long*>(h->pinned + 176);
+    GBBA_CUDA(cudaMemcpyAsync(hc, counters, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->active));
+    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    const unsigned long long nc = hc[0], nobs = hc[1], err = hc[2], locked = hc[3];
+    GBBA_REQUIRE(err == 0, GBBA_ERROR_INVALID_ARGUMENT, pack_error(err));
+    out_back(h, out->extrinsics, dext, 6 * nc, memory);
+    out_back(h, out->observations, dobs, 2 * nobs, memory);
+    out_back(h, out->camera_index, dci, nobs, memory);
+    out_back(h, out->intrinsic_index, dii, nobs, memory);
+    out_back(h, out->point_index, dpi, nobs, memory);
+    out_back(h, out->camera_constant, dcc, nc, memory);
+    out_back(h, out->camera_image, dcimg, nc, memory);
+    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    out->num_cameras = (int64_t)nc;
+    out->num_observations = (int64_t)nobs;
+    out->locked_camera = (int64_t)locked - 1;
+    return GBBA_SUCCESS;
+  });
+}
+
+gbba_status gbsfm_unpack_ba(gbba_handle* h, int64_t num_cameras, const double* extrinsics,
+                            const uint32_t* camera_image, const double* intrinsics, int64_t num_intrinsic_groups,
+                            const uint32_t* intrinsic_group, int64_t num_images, gbsfm_camera* cameras,
+                            int32_t memory) {
+  if (num_cameras < 0 || num_images < 0 || num_intrinsic_groups < 0 || num_cameras > num_images)
+    return GBBA_ERROR_INVALID_ARGUMENT;
+  if (num_cameras > 0 && (!extrinsics || !camera_image || !intrinsics || !intrinsic_group || !cameras))
+    return GBBA_ERROR_INVALID_ARGUMENT;
+  return sfm_guard(h, [&]() {
+    if (num_cameras == 0) return GBBA_SUCCESS;
+    h->arena.reset();
+    h->arena.reserve(sizeof(double) * 6 * (num_cameras + num_intrinsic_groups) +
+                     sizeof(uint32_t) * (num_cameras + num_images) + sizeof(gbsfm_camera) * num_images + 256 * 8);
+    const double* dext = in_view(h, extrinsics, 6 * num_cameras, memory);
+    const uint32_t* dcimg = in_view(h, camera_image, num_cameras, memory);
+    const double* dintr = in_view(h, intrinsics, 6 * num_intrinsic_groups, memory);
+    const uint32_t* dgrp = in_view(h, intrinsic_group, num_images, memory);
+    gbsfm_camera* dcam = const_cast<gbsfm_camera*>(in_view(h, (const gbsfm_camera*)cameras, num_images, memory));
+    unsigned long long* err = h->arena.take<unsigned long long>(1);
+    GBBA_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned long long), h->active));
+    const unsigned grid = grid_for(h, num_cameras, 128);
+    KernelTimer timer(h);
+    k_unpack_check<<<grid, 128, 0, h->active>>>(num_cameras, dcimg, num_images, dgrp, num_intrinsic_groups, err);
+    check_launch(h);
+    k_unpack<<<grid, 128, 0, h->active>>>(num_cameras, dext, dcimg, dintr, dgrp, err, dcam);
+    check_launch(h);
+    timer.stop();
+    unsigned long long* he = reinterpret_cast<unsigned long long*>(h->pinned + 176);
+    GBBA_CUDA(cudaMemcpyAsync(he, err, sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->active));
+    GBBA_CUDA(cudaStreamSynchronize(h->active));
+    GBBA_REQUIRE(*he == 0, GBBA_ERROR_INVALID_ARGUMENT, pack_error(*he));
+    out_back(h, cameras, (const gbsfm_camera*)dcam, num_images, memory);
+    GBBA_CUDA(cudaStreamSynchronize(h->active));
     return GBBA_SUCCESS;
   });
 }

@@ -359,15 +359,6 @@ void finish_check(gbba_handle* h, const unsigned int* err) {
 }
 
 // Device time of the call's main kernel, kept in the handle (gbba_last_kernel_time).
-struct KernelTimer {
-  gbba_handle* h;
-  explicit KernelTimer(gbba_handle* hh) : h(hh) { GBBA_CUDA(cudaEventRecord(h->ev_k0, h->active)); }
-  void stop() {
-    GBBA_CUDA(cudaEventRecord(h->ev_k1, h->active));
-    h->kernel_timed = true;
-  }
-};
-
 }  // namespace
 
 extern "C" {

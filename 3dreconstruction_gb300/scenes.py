@@ -414,3 +414,122 @@ def engine_tracks(num_cameras=30, num_tracks=3000, seed=8, sigma=0.5, outlier_fr
     off = np.zeros(num_tracks + 1, np.int64)
     off[1:] = np.cumsum(L)
     return {"cameras": cams, "points": X, "track_offsets": off, "camera_index": cam, "xy": xy}
+
+
+def _axis_rotation(axis, angle):
+    """Rotation matrix of `angle` about the unit `axis` (Rodrigues)."""
+    k = np.asarray(axis, float) / np.linalg.norm(axis)
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + math.sin(angle) * K + (1 - math.cos(angle)) * (K @ K)
+
+
+def engine_state(num_images=40, num_points=2000, seed=9, reconstructed_frac=0.8, num_groups=3, max_len=8):
+    """The incremental engine's state before a bundle adjustment, as dense
+    arrays in the key order of its maps: cameras per image (some images not
+    reconstructed), intrinsic groups with non-dense keys, features per image
+    (float pixels), 3D points with non-dense track ids, and tracks whose
+    entries (image, feature) ascend by image and may name images without a
+    camera.  A few rotations take the special branches of the matrix to
+    angle-axis conversion: the identity, half turns about each axis, a turn
+    just short of half, and a small angle.  Also a refined parameter set for
+    the write-back: angle-axis vectors of zero, sub-epsilon, near-pi and
+    generic length."""
+    rng = np.random.default_rng(seed)
+    centers = 12.0 * sphere_directions(num_images, rng)
+    cams = brown_cameras(centers, rng)
+    special = [np.eye(3), _axis_rotation([1, 0, 0], math.pi), _axis_rotation([0, 1, 0], math.pi),
+               _axis_rotation([0, 0, 1], math.pi), _axis_rotation([1, 2, -1], math.pi - 1e-3),
+               _axis_rotation([0.3, -1, 0.2], 1e-6), _axis_rotation([-2, 1, 3], 2.5)]
+    slots = [3 + 2 * i for i in range(len(special)) if 3 + 2 * i < num_images]
+    for i, R in zip(slots, special):
+        cams[i, :9] = R.ravel()
+    rec = (rng.random(num_images) < reconstructed_frac).astype(np.uint8)
+    rec[slots] = 1
+    group_keys = np.sort(rng.choice(np.arange(2, 40), num_groups, replace=False))
+    image_group = rng.integers(0, num_groups, num_images).astype(np.uint32)
+    group_intr = np.column_stack([rng.uniform(900, 1100, num_groups), np.full(num_groups, PP[0]),
+                                  np.full(num_groups, PP[1]), rng.normal(0, 0.05, num_groups),
+                                  rng.normal(0, 0.01, num_groups), rng.normal(0, 0.01, num_groups)])
+    nfeat = rng.integers(20, 400, num_images)
+    nfeat[0] = 0  # an image without features, named by no track
+    feature_offsets = np.zeros(num_images + 1, np.int64)
+    feature_offsets[1:] = np.cumsum(nfeat)
+    features = rng.uniform(0, 2000, (int(feature_offsets[-1]), 2)).astype(np.float32)
+    track_keys = np.sort(rng.choice(np.arange(10 * num_points), num_points, replace=False)).astype(np.int64)
+    X = rng.uniform(-2, 2, (num_points, 3))
+    L = rng.integers(2, max_len + 1, num_points)
+    L[5] = 1
+    imgs, fts = [], []
+    for t in range(num_points):
+        im = np.sort(rng.choice(np.arange(1, num_images), L[t], replace=False))
+        imgs.append(im)
+        fts.append(rng.integers(0, nfeat[im]))
+    track_offsets = np.zeros(num_points + 1, np.int64)
+    track_offsets[1:] = np.cumsum(L)
+    nc = int(rec.sum())
+    aa = rng.normal(0, 0.6, (nc, 3))
+    aa[:3][:nc] = [[0.0, 0.0, 0.0], [1e-9, -2e-9, 5e-10], [0.6 * (math.pi - 1e-7), -0.8 * (math.pi - 1e-7), 0.0]][:nc]
+    refined_ext = np.column_stack([aa, rng.normal(0, 3, (nc, 3))])
+    refined_intr = group_intr * (1 + rng.normal(0, 0.01, group_intr.shape))
+    return {"cameras": cams, "reconstructed": rec, "intrinsic_group": image_group, "group_keys": group_keys,
+            "group_intrinsics": group_intr, "feature_offsets": feature_offsets, "features": features,
+            "track_keys": track_keys, "points": X, "track_offsets": track_offsets,
+            "track_image": np.concatenate(imgs).astype(np.uint32),
+            "track_feature": np.concatenate(fts).astype(np.uint32), "first_added": min(7, num_images - 1),
+            "refined_extrinsics": refined_ext, "refined_intrinsics": refined_intr}
+
+
+def engine_state_large(num_images=5000, num_points=2_000_000, seed=12, reconstructed_frac=0.8):
+    """A full-size engine state (the large workload's 5,000 cameras and 2M
+    points, track lengths 2..8, ~10M entries), built with numpy only: entries
+    ascend by image inside a track, features are drawn per image."""
+    rng = np.random.default_rng(seed)
+    base = engine_state(num_images=num_images, num_points=8, seed=seed, reconstructed_frac=reconstructed_frac)
+    L = rng.integers(2, 9, num_points)
+    off = np.zeros(num_points + 1, np.int64)
+    off[1:] = np.cumsum(L)
+    ne = int(off[-1])
+    start = rng.integers(1, num_images - 40, num_points)
+    step = rng.integers(1, 5, ne)
+    tr = np.repeat(np.arange(num_points), L)
+    first_of = off[:-1][tr]
+    step[np.arange(ne) == first_of] = 0
+    cs = np.cumsum(step)
+    img = start[tr] + cs - cs[first_of]
+    nfeat = np.diff(base["feature_offsets"])
+    nfeat[nfeat == 0] = 1
+    fo = np.zeros(num_images + 1, np.int64)
+    fo[1:] = np.cumsum(nfeat)
+    st = dict(base)
+    st.update(feature_offsets=fo, features=rng.uniform(0, 2000, (int(fo[-1]), 2)).astype(np.float32),
+              points=rng.uniform(-2, 2, (num_points, 3)), track_offsets=off, track_image=img.astype(np.uint32),
+              track_feature=(rng.random(ne) * nfeat[img]).astype(np.uint32), track_keys=np.arange(num_points))
+    return st
+
+
+def engine_state_sample(st, num_points):
+    """The first `num_points` tracks of an engine state (same images,
+    cameras and features)."""
+    off = st["track_offsets"][:num_points + 1]
+    out = dict(st)
+    out.update(points=st["points"][:num_points], track_offsets=off, track_image=st["track_image"][:off[-1]],
+               track_feature=st["track_feature"][:off[-1]], track_keys=st["track_keys"][:num_points])
+    return out
+
+
+def resection_scene(num_points=600, seed=13, outlier_frac=0.3, sigma=0.5, width=1920, height=1080):
+    """2D-3D correspondences for a robust resection: one pinhole camera
+    (f = 1000, principal point at the image centre) 8 units from a cloud of
+    points, pixel noise, and a share of the 2D points replaced by uniform
+    positions in the image (outliers)."""
+    rng = np.random.default_rng(seed)
+    center = np.array([[0.5, -0.3, -8.0]])
+    R, t = _cameras_facing_origin(center)
+    K = np.array([[1000.0, 0.0, width / 2], [0.0, 1000.0, height / 2], [0.0, 0.0, 1.0]])
+    X = rng.uniform(-2.5, 2.5, (num_points, 3))
+    p = X @ R[0].T + t[0]
+    x = (p[:, :2] / p[:, 2:]) @ K[:2, :2].T + K[:2, 2]
+    x += rng.normal(scale=sigma, size=x.shape)
+    out = rng.random(num_points) < outlier_frac
+    x[out] = rng.uniform([0, 0], [width, height], (out.sum(), 2))
+    return {"x2d": x, "x3d": X, "K": K, "width": width, "height": height, "outlier": out.astype(np.uint8)}

@@ -30,6 +30,10 @@ Metric: observations x LM iterations per second (higher is better).
   triangulation  the batched FP32 triangulation (1,000,000 tracks): the
              whole call, and the main kernel's compulsory bytes over its
              device time (gbba_last_kernel_time) as a roofline fraction.
+  pack       the engine's BA assembly (gbsfm_pack_ba) on a 5,000-image,
+             2M-track state: device call, host call, std::map loop on the CPU.
+  acransac   AC-RANSAC hypothesis scoring: 4,096 resection models x 2,000
+             correspondences in one call, against the per-model CPU loop.
   large      the large workload on the PCG path: FP64 and mixed time to cost.
   batched    gbba_solve_batched on the 4,096 local-BA windows.
   cpu_baseline  the CPU oracle (restatement of ceres LM + dense Schur,
@@ -256,6 +260,139 @@ def measure_triangulation(h, torch, steps, warmup, peak):
             "roofline": {"kernel": "k_tri_f32", "bound": "hbm", "achieved": alg / kt / 1e9, "peak": peak,
                          "unit": "GB/s", "frac": alg / kt / 1e9 / peak, "kernel_ms": kt * 1e3,
                          "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)"}}
+
+
+def pack_algorithmic_bytes(ni, nc, ne, nobs, nt):
+    """Compulsory DRAM bytes of one gbsfm_pack_ba over a device-resident
+    state: per entry its image and feature ids (8 B) read once; per kept
+    observation its feature (8 B) read and the observation (16 B) and three
+    indices (12 B) written; per track its offset (8 B) and the point copy
+    (24 B read, 24 B written); per image its flag, group and ordinal (9 B) and,
+    when reconstructed, its camera (144 B) read and extrinsic block (48 B) and
+    ordinal -> image entry (4 B) written."""
+    return 8 * ne + 36 * nobs + 56 * nt + 9 * ni + 196 * nc
+
+
+def measure_pack(h, torch, steps, warmup, peak):
+    """The engine's BA assembly (gbsfm_pack_ba) on the large workload's
+    state: 5,000 images (~4,000 with a camera), 2M tracks, ~10M entries.
+    Device-resident call timed with CUDA events (L2 flushed between calls),
+    the same call from host buffers (copies inside), and the reference's
+    std::map assembly loop restated in C++ (liboracle, one thread) on the
+    first 200,000 tracks, scaled per entry."""
+    scenes = importlib.import_module("3dreconstruction_gb300.scenes")
+    abi = importlib.import_module("3dreconstruction_gb300.abi")
+    st = scenes.engine_state_large()
+    dev_pack = abi.EnginePack(st, "cuda:0")
+    host_pack = abi.EnginePack(st)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    first = int(st["first_added"])
+    for _ in range(warmup):
+        h.check(dev_pack.pack(h.lib, h.h, first)[0], "gbsfm_pack_ba")
+    times, ktimes, e2e = [], [], []
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.current_stream())
+        rc, o = dev_pack.pack(h.lib, h.h, first)
+        e1.record(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        h.check(rc, "gbsfm_pack_ba")
+        times.append(e0.elapsed_time(e1) / 1e3)
+        kt = ctypes.c_double()
+        h.check(h.lib.gbba_last_kernel_time(h.h, ctypes.byref(kt)), "gbba_last_kernel_time")
+        ktimes.append(kt.value)
+    for _ in range(max(1, steps)):
+        t0 = time.perf_counter()
+        rc, oh = host_pack.pack(h.lib, h.h, first)
+        e2e.append(time.perf_counter() - t0)
+        h.check(rc, "gbsfm_pack_ba")
+    ne, nt, ni = dev_pack.ne, dev_pack.nt, dev_pack.ni
+    nobs, nc = o.num_observations, o.num_cameras
+    same = oh.num_observations == nobs and oh.num_cameras == nc
+    out = {"workload": "engine state: 5,000 images, 2,000,000 tracks of 2-8 entries, 80% of images with a camera",
+           "entries": ne, "observations": nobs, "cameras": nc, "host_and_device_counts_agree": same,
+           "ms_per_call": float(np.median(times)) * 1e3, "e2e_ms_per_call": float(np.median(e2e)) * 1e3,
+           "e2e_note": "host arrays in and out, copies inside the call"}
+    kt = float(np.median(ktimes))
+    alg = pack_algorithmic_bytes(ni, nc, ne, nobs, nt)
+    out["roofline"] = {"kernel": "k_pack_images + k_pack_count + k_pack_scan + k_pack_gather + k_pack_lock",
+                       "bound": "hbm", "achieved": alg / kt / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": alg / kt / 1e9 / peak, "kernel_ms": kt * 1e3, "algorithmic_bytes": alg}
+    try:
+        import oracle
+        sample = scenes.engine_state_sample(st, 200_000)
+        _, sec = oracle.sfm_pack_maps(sample)
+        per_entry = sec / len(sample["track_image"])
+        out["cpu_std_map"] = {"ms_scaled_to_workload": per_entry * ne * 1e3, "sample_entries": len(sample["track_image"]),
+                              "sample_ms": sec * 1e3, "cores": 1, "kind": "port",
+                              "note": "BundleAdjustment's assembly loop over std::map containers (maps built untimed)"}
+    except Exception as e:  # the oracle is a baseline only
+        out["cpu_std_map"] = {"unavailable": str(e)[:200]}
+    return out
+
+
+def measure_acransac(h, torch, steps, warmup):
+    """AC-RANSAC hypothesis scoring (gbsfm_acransac_score): 4,096 candidate
+    six-point resection models against 2,000 correspondences (30% outliers),
+    one batched call on device-resident inputs, against the reference's loop
+    (residuals, std::sort, bestNFA model after model) restated in C++ on one
+    host core on the first 256 models, scaled per model."""
+    scenes = importlib.import_module("3dreconstruction_gb300.scenes")
+    abi = importlib.import_module("3dreconstruction_gb300.abi")
+    sc = scenes.resection_scene(num_points=2000, seed=21)
+    n, hm = 2000, 4096
+    xn = (sc["x2d"] - np.array([sc["width"], sc["height"]]) / 2) / max(sc["width"], sc["height"])
+    # candidate models: the true camera in normalised coordinates, perturbed
+    K = sc["K"].copy()
+    N = np.array([[1 / 1920, 0, -0.5], [0, 1 / 1920, -540 / 1920], [0, 0, 1]])
+    R, t = scenes._cameras_facing_origin(np.array([[0.5, -0.3, -8.0]]))
+    P = N @ K @ np.hstack([R[0], t[0][:, None]])
+    rng = np.random.default_rng(5)
+    models = np.repeat(P.reshape(1, 12), hm, 0) * (1 + 0.01 * rng.normal(size=(hm, 12)))
+    dev = "cuda"
+    x2 = torch.from_numpy(np.ascontiguousarray(xn)).to(dev)
+    x3 = torch.from_numpy(np.ascontiguousarray(sc["x3d"])).to(dev)
+    md = torch.from_numpy(np.ascontiguousarray(models)).to(dev)
+    nfa = torch.empty(hm, dtype=torch.float64, device=dev)
+    k = torch.empty(hm, dtype=torch.int32, device=dev)
+    em = torch.empty(hm, dtype=torch.float64, device=dev)
+    prm = abi.GbsfmAcransacParams(6, 1, float(np.log10(np.pi)), 1.0, float("inf"))
+
+    def run():
+        h.check(h.lib.gbsfm_acransac_score(h.h, ctypes.byref(prm), n, x2.data_ptr(), x3.data_ptr(), hm, md.data_ptr(),
+                                           nfa.data_ptr(), k.data_ptr(), em.data_ptr(), None, abi.MEMORY_DEVICE),
+                "gbsfm_acransac_score")
+
+    for _ in range(warmup):
+        run()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(torch.cuda.current_stream())
+        run()
+        e1.record(torch.cuda.current_stream())
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = float(np.median(times))
+    out = {"workload": "4,096 six-point resection models x 2,000 correspondences (30% outliers)",
+           "models_per_s": hm / t, "ms_per_call": t * 1e3,
+           "mean_inliers": float(k.float().mean().item()),
+           "note": "one call: logcombi tables, residuals, per-model sort and bestNFA; device-resident inputs"}
+    try:
+        import oracle
+        _, _, _, _, per_model = oracle.acransac_score_cpp(xn, sc["x3d"], models[:256], 6, 1, float(np.log10(np.pi)),
+                                                          with_order=False)
+        out["cpu_reference_loop"] = {"ms_scaled_to_workload": per_model * hm * 1e3, "sample_models": 256,
+                                     "cores": 1, "kind": "port",
+                                     "note": "ACRANSAC's per-model scoring as the reference runs it (std::sort)"}
+    except Exception as e:  # the oracle is a baseline only
+        out["cpu_reference_loop"] = {"unavailable": str(e)[:200]}
+    return out
 
 
 def _local_window(args):
@@ -625,6 +762,9 @@ def run_ours(args):
         line["time_to_cost"] = time_to_cost(h, abi, scene, dp, pristine, st, sptr, args.ttc_iters)
     if rank == 0 and args.triangulation:
         line["triangulation"] = measure_triangulation(h, torch, args.steps, args.warmup, peak)
+    if rank == 0 and args.pack:
+        line["pack"] = measure_pack(h, torch, args.steps, args.warmup, peak)
+        line["acransac"] = measure_acransac(h, torch, args.steps, args.warmup)
     if rank == 0 and args.large:
         line["large"] = measure_large(h, abi)
     if rank == 0 and args.batched_windows > 0:
@@ -651,6 +791,7 @@ def main():
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")
+    ap.add_argument("--no-pack", dest="pack", action="store_false", help="skip the engine assembly and AC-RANSAC legs")
     ap.add_argument("--no-large", dest="large", action="store_false",
                     help="skip the large PCG workload (5,000 cameras, 20M observations)")
     ap.add_argument("--batched-windows", type=int, default=4096,

@@ -201,9 +201,10 @@ const char* gbba_status_string(gbba_status status);
 int gbba_abi_version(void);
 /* Number of CUDA kernel launches issued through this handle so far. */
 int64_t gbba_launch_count(const gbba_handle* handle);
-/* Device time (CUDA events on the call's stream) of the main kernel of the
- * handle's last triangulation call (gbtri_*), without its input check and
- * copies; GBBA_ERROR_NOT_SUPPORTED before any such call.  No counterpart in
+/* Device time (CUDA events on the call's stream) of the main kernel(s) of the
+ * handle's last triangulation call (gbtri_*) or problem pack / write-back
+ * (gbsfm_pack_ba, gbsfm_unpack_ba), without input checks and host copies;
+ * GBBA_ERROR_NOT_SUPPORTED before any such call.  No counterpart in
  * the reference, which has no device kernels: it serves roofline accounting. */
 gbba_status gbba_last_kernel_time(gbba_handle* handle, double* seconds);
 

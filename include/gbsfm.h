@@ -1,8 +1,8 @@
 /*
- * gbsfm.h - C ABI of the engine-side scans around the bundle adjustment.
+ * gbsfm.h - C ABI of the engine-side work around the bundle adjustment.
  *
- * The incremental engine runs three per-element loops over state it already
- * holds between BA calls; here each is one batched call:
+ * The incremental engine runs per-element loops over state it already holds
+ * between BA calls; here each is one batched call:
  *   - gbsfm_triangulate_pair: triangulate2View_Vector
  *       (libs/sfm/include/mvg/sfm/sfm_robust.h:152-195), the per-match DLT
  *       and mean reprojection residual, with the keep decision its callers
@@ -13,7 +13,11 @@
  *   - gbsfm_reject_tracks: IncrementalReconstructionEngine::badTrackRejector
  *       (:1047-1140);
  *   - gbsfm_residual_histogram: IncrementalReconstructionEngine::
- *       ComputeResidualsHistogram (:1550-1616).
+ *       ComputeResidualsHistogram (:1550-1616);
+ *   - gbsfm_pack_ba / gbsfm_unpack_ba: BundleAdjustment's problem assembly
+ *       and write-back (:1250-1393, 1475-1546);
+ *   - gbsfm_acransac_score: the hypothesis scoring of robustResection's
+ *       AC-RANSAC (libs/sfm/include/mvg/sfm/sfm_robust.h:207-254).
  * Cameras are the engine's BrownPinholeCamera
  * (libs/camera/include/mvg/camera/brown_pinhole_camera.h:44-140): rotation,
  * translation, focal length, principal point and radial K3 distortion, with
@@ -83,6 +87,133 @@ gbba_status gbsfm_residual_histogram(gbba_handle* handle, const gbsfm_camera* ca
                                      const double* points, int64_t num_tracks, const int64_t* track_offsets,
                                      const uint32_t* camera_index, const double* xy, gbsfm_residual_stats* stats,
                                      int32_t memory);
+
+/* ---- Problem assembly ----------------------------------------------------
+ * IncrementalReconstructionEngine::BundleAdjustment packs its std::map state
+ * into a BA_Problem_data_camMotionAndIntrinsic<6,6>
+ * (libs/sfm/src/sfm_incremental_engine.cpp:1250-1393) and writes the refined
+ * parameters back after the solve (:1475-1546).  Here the engine state is a
+ * set of dense arrays, the pack is one pass over the track entries and the
+ * write-back one pass over the cameras, so the state can stay in device
+ * memory between BA calls.
+ *
+ * Engine state, every map in its key order:
+ *   map_Camera           -> cameras[image] where reconstructed[image] != 0
+ *   map_images_id_per_intrinsic_group_ -> intrinsic_group[image] (the
+ *                           ordinal of the image's group among the keys)
+ *   map_intrinsics_per_group_ -> group_intrinsics [G][6] f, ppx, ppy, k1, k2, k3
+ *   map_features_        -> CSR feature_offsets [num_images+1] over
+ *                           features [num_features][2] (ScalePointFeature x, y)
+ *   map_3d_points        -> points [num_points][3], ascending track id
+ *   map_reconstructed_   -> CSR track_offsets [num_points+1] over the entries
+ *                           (track_image, track_feature), image id ascending
+ *                           inside a track (SubmapTrack order). */
+typedef struct gbsfm_engine_state {
+  int64_t num_images;
+  const gbsfm_camera* cameras;       /* [num_images] */
+  const uint8_t* reconstructed;      /* [num_images] */
+  const uint32_t* intrinsic_group;   /* [num_images] */
+  int64_t num_intrinsic_groups;
+  const double* group_intrinsics;    /* [num_intrinsic_groups][6] */
+  int64_t num_features;
+  const int64_t* feature_offsets;    /* [num_images+1] */
+  const float* features;             /* [num_features][2] */
+  int64_t num_points;
+  const double* points;              /* [num_points][3] */
+  int64_t num_entries;               /* track_offsets[num_points] */
+  const int64_t* track_offsets;      /* [num_points+1] */
+  const uint32_t* track_image;       /* [num_entries] */
+  const uint32_t* track_feature;     /* [num_entries] */
+} gbsfm_engine_state;
+
+/* Which extrinsic block the pack holds constant.  The reference locks
+ * mutable_camera_extrinsic_for_observation(ordinal of vec_added_order_[0])
+ * (:1437-1443), an accessor that takes an observation index
+ * (libs/sfm/include/mvg/sfm/problem_data_container.h:93-95): the block of
+ * observation number `ordinal`.  GBSFM_LOCK_AS_REFERENCE reproduces that;
+ * GBSFM_LOCK_FIRST_ADDED locks the first-added camera itself. */
+typedef enum gbsfm_lock {
+  GBSFM_LOCK_AS_REFERENCE = 0,
+  GBSFM_LOCK_FIRST_ADDED = 1,
+  GBSFM_LOCK_NONE = 2
+} gbsfm_lock;
+
+/* Outputs of the pack, sized for the worst case by the caller: extrinsics
+ * [num_images][6], intrinsics [G][6], points [num_points][3], observations
+ * [num_entries][2], the three index arrays [num_entries], camera_constant
+ * and camera_image [num_images] (both may be NULL).  The layout is the
+ * reference's parameters_ split in three: extrinsics (angle-axis from
+ * ceres::RotationMatrixToAngleAxis, then t) in ascending image id,
+ * intrinsic groups in key order, points in track order; observations keep
+ * the track-major order, dropping entries of images without a camera.  It is
+ * a gbba_problem of camera model GBBA_MODEL_RADIAL_K3 as it stands. */
+typedef struct gbsfm_ba_arrays {
+  double* extrinsics;
+  double* intrinsics;
+  double* points;
+  double* observations;
+  uint32_t* camera_index;
+  uint32_t* intrinsic_index;
+  uint32_t* point_index;
+  uint8_t* camera_constant;   /* 1 on the locked block */
+  uint32_t* camera_image;     /* image id of each camera ordinal */
+  int64_t num_cameras;        /* out */
+  int64_t num_observations;   /* out: observations written */
+  int64_t measurements;       /* out: sum of the track sizes, the reference's num_observations_ */
+  int64_t locked_camera;      /* out: ordinal of the locked block, -1 for none */
+} gbsfm_ba_arrays;
+
+/* first_added_image: vec_added_order_[0], or -1 when the engine has added no
+ * image.  Arrays of `state` and `out` are in `memory`.  Entries that name an
+ * image or a feature outside the state, offsets that are not a CSR of
+ * num_entries entries and intrinsic groups out of range return
+ * GBBA_ERROR_INVALID_ARGUMENT (the reference indexes its maps unchecked). */
+gbba_status gbsfm_pack_ba(gbba_handle* handle, const gbsfm_engine_state* state, int64_t first_added_image,
+                          int32_t lock, gbsfm_ba_arrays* out, int32_t memory);
+
+/* Write-back: for camera ordinal c, cameras[camera_image[c]] becomes the
+ * BrownPinholeCamera of R = ceres::AngleAxisToRotationMatrix(extrinsics[c]),
+ * t = extrinsics[c][3..5] and the intrinsics of its group
+ * intrinsics[intrinsic_group[camera_image[c]]] (:1491-1516).  The points and
+ * the groups' intrinsics go back as they are (:1481-1489, 1519-1529): the
+ * packed arrays may be the engine's own. */
+gbba_status gbsfm_unpack_ba(gbba_handle* handle, int64_t num_cameras, const double* extrinsics,
+                            const uint32_t* camera_image, const double* intrinsics, int64_t num_intrinsic_groups,
+                            const uint32_t* intrinsic_group, int64_t num_images, gbsfm_camera* cameras,
+                            int32_t memory);
+
+/* ---- AC-RANSAC hypothesis scoring ------------------------------------------
+ * The per-model body of ACRANSAC's main loop
+ * (libs/feature/include/mvg/feature/estimator_acransac.h:170-200) as used by
+ * robustResection (libs/sfm/include/mvg/sfm/sfm_robust.h:207-254), for a
+ * batch of candidate models: the squared reprojection error of every
+ * correspondence (ResectionSquaredResidualError, sfm_robust.h:197-204:
+ * |Project(P, X) - x|^2, P in the kernel's normalised image frame), sorted
+ * ascending with ties in index order (std::sort of (error, index) pairs),
+ * and bestNFA (estimator_acransac.h:75-97) over the sorted errors with the
+ * float tables logcombi(k, n) and logcombi(sample_size, k) (:40-65).  Each
+ * model's NFA, inlier count k and threshold e[k-1] come back; a model none
+ * of whose errors passes max_threshold gets NFA +inf, k = sample_size and
+ * threshold +inf (the reference leaves such a model unused).  The sampling
+ * and the adaptive loop around it stay with the caller. */
+typedef struct gbsfm_acransac_params {
+  int32_t sample_size;   /* Kernel::MINIMUM_SAMPLES: 6 (six-point DLT) or 3 (P3P) */
+  int32_t max_models;    /* Kernel::MAX_MODELS: 1 or 4; loge0 = log10(max_models (n - sample_size)) */
+  double logalpha0;      /* log10(pi) for both resection kernels */
+  double mult_error;     /* 1.0: point-to-point error */
+  double max_threshold;  /* +inf, or precision * normalizer2(0,0)^2 */
+} gbsfm_acransac_params;
+
+/* x2d [num_points][2] (normalised, as the kernel adaptor holds them), x3d
+ * [num_points][3], models [num_models][12] (row-major 3x4).  Outputs nfa,
+ * num_inliers, error_max [num_models]; order [num_models][num_points] the
+ * sorted correspondence indices (the inliers of model h are
+ * order[h][0 .. num_inliers[h]-1]), or NULL.  num_points must exceed
+ * sample_size (ACRANSAC returns early otherwise). */
+gbba_status gbsfm_acransac_score(gbba_handle* handle, const gbsfm_acransac_params* params, int64_t num_points,
+                                 const double* x2d, const double* x3d, int64_t num_models, const double* models,
+                                 double* nfa, int32_t* num_inliers, double* error_max, uint32_t* order,
+                                 int32_t memory);
 
 #ifdef __cplusplus
 }

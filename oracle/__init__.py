@@ -5,6 +5,7 @@ bench.py's CPU baseline, never by the product package.
 """
 import ctypes as C
 import importlib
+import math
 import os
 import subprocess
 
@@ -53,6 +54,10 @@ def load():
         lib.oracle_tri_dlt2.argtypes = [C.c_int64, vp, vp, C.c_int64, vp, vp, vp, vp]
         lib.oracle_tri_nview.argtypes = [C.c_int, vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp]
         lib.oracle_tri_linear_gn.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int, vp, vp, vp]
+        lib.oracle_acransac_score.argtypes = [C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, C.c_int64, vp,
+                                              vp, C.c_int64, vp, vp, vp, vp, vp, vp]
+        lib.oracle_sfm_pack_maps.argtypes = [C.POINTER(abi.GbsfmEngineState), C.c_int64, vp, vp, vp, vp, vp, vp, vp,
+                                             vp, C.c_int, vp]
         _lib = lib
     return _lib
 
@@ -337,3 +342,220 @@ def sfm_residual_histogram(cams, points, offsets, cam, xy):
         hist = np.bincount(b[(~under) & (b < 10)], minlength=10)[:10]
         out.update(hist=hist, underflow=int(under.sum()), overflow=int(((~under) & (b >= 10)).sum()))
     return out
+
+
+def rotation_to_angle_axis(R):
+    """ceres::RotationMatrixToAngleAxis (include/ceres/rotation.h:357-370):
+    RotationMatrixToQuaternion (Shoemake's branches, :312-350) then
+    QuaternionToAngleAxis (:266-306), on one row-major 3x3 matrix."""
+    R = np.asarray(R, np.float64).reshape(3, 3)
+    q = np.zeros(4)
+    tr = R[0, 0] + R[1, 1] + R[2, 2]
+    if tr >= 0.0:
+        s = math.sqrt(tr + 1.0)
+        q[0] = 0.5 * s
+        s = 0.5 / s
+        q[1], q[2], q[3] = (R[2, 1] - R[1, 2]) * s, (R[0, 2] - R[2, 0]) * s, (R[1, 0] - R[0, 1]) * s
+    else:
+        i = 1 if R[1, 1] > R[0, 0] else 0
+        if R[2, 2] > R[i, i]:
+            i = 2
+        j, k = (i + 1) % 3, (i + 2) % 3
+        s = math.sqrt(R[i, i] - R[j, j] - R[k, k] + 1.0)
+        q[i + 1] = 0.5 * s
+        s = 0.5 / s
+        q[0] = (R[k, j] - R[j, k]) * s
+        q[j + 1] = (R[j, i] + R[i, j]) * s
+        q[k + 1] = (R[k, i] + R[i, k]) * s
+    s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3]
+    if s2 > 0.0:
+        st, ct = math.sqrt(s2), q[0]
+        two_theta = 2.0 * (math.atan2(-st, -ct) if ct < 0.0 else math.atan2(st, ct))
+        kk = two_theta / st
+    else:
+        kk = 2.0
+    return q[1:] * kk
+
+
+def angle_axis_to_rotation(aa):
+    """ceres::AngleAxisToRotationMatrix (include/ceres/rotation.h:372-414),
+    returned row-major: Rodrigues' formula, first order below theta^2 = eps."""
+    w = np.asarray(aa, np.float64)
+    th2 = float(w @ w)
+    if th2 > np.finfo(np.float64).eps:
+        th = math.sqrt(th2)
+        wx, wy, wz = w / th
+        c, s = math.cos(th), math.sin(th)
+        oc = 1.0 - c
+        return np.array([[c + wx * wx * oc, wx * wy * oc - wz * s, wy * s + wx * wz * oc],
+                         [wz * s + wx * wy * oc, c + wy * wy * oc, -wx * s + wy * wz * oc],
+                         [-wy * s + wx * wz * oc, wx * s + wy * wz * oc, c + wz * wz * oc]])
+    return np.array([[1.0, -w[2], w[1]], [w[2], 1.0, -w[0]], [-w[1], w[0], 1.0]])
+
+
+def sfm_pack(st, lock=0):
+    """IncrementalReconstructionEngine::BundleAdjustment's assembly
+    (sfm_incremental_engine.cpp:1250-1393) over the dense engine state of
+    gbsfm_pack_ba: cameras in ascending image id, observations of the
+    reconstructed images in track-major order, and the locked block
+    (:1437-1443: camera_index_extrinsic[ordinal of the first-added image])."""
+    rec = np.asarray(st["reconstructed"]) != 0
+    ordinal = np.cumsum(rec) - 1
+    cams = np.asarray(st["cameras"], np.float64).reshape(-1, 18)
+    ext = np.array([np.concatenate([rotation_to_angle_axis(cams[i, :9]), cams[i, 9:12]])
+                    for i in np.flatnonzero(rec)]).reshape(-1, 6)
+    off = np.asarray(st["track_offsets"], np.int64)
+    tr = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    img = np.asarray(st["track_image"], np.int64)
+    keep = rec[img]
+    fidx = np.asarray(st["feature_offsets"], np.int64)[img] + np.asarray(st["track_feature"], np.int64)
+    obs = np.asarray(st["features"], np.float32)[fidx].astype(np.float64)[keep]
+    out = {"extrinsics": ext, "observations": obs, "camera_index": ordinal[img][keep].astype(np.uint32),
+           "intrinsic_index": np.asarray(st["intrinsic_group"], np.uint32)[img][keep],
+           "point_index": tr[keep].astype(np.uint32), "camera_image": np.flatnonzero(rec).astype(np.uint32),
+           "num_cameras": int(rec.sum()), "measurements": len(img)}
+    fa = int(st["first_added"])
+    locked = -1
+    if fa >= 0 and rec.any() and lock != 2:
+        k = int(ordinal[fa]) if rec[fa] else (0 if lock == 0 else -1)
+        if lock == 1:
+            locked = k
+        elif k < len(out["camera_index"]):
+            locked = int(out["camera_index"][k])
+    out["locked_camera"] = locked
+    return out
+
+
+def sfm_unpack(extrinsics, camera_image, intrinsics, intrinsic_group, cameras):
+    """The write-back of BundleAdjustment (sfm_incremental_engine.cpp:
+    1491-1516): each camera rebuilt from its refined angle-axis, translation
+    and its group's intrinsics; rows of the engine camera layout."""
+    out = np.array(cameras, np.float64).reshape(-1, 18)
+    ext = np.asarray(extrinsics, np.float64).reshape(-1, 6)
+    intr = np.asarray(intrinsics, np.float64).reshape(-1, 6)
+    for c, i in enumerate(np.asarray(camera_image, np.int64)):
+        out[i, :9] = angle_axis_to_rotation(ext[c, :3]).ravel()
+        out[i, 9:12] = ext[c, 3:]
+        out[i, 12:18] = intr[int(intrinsic_group[i])]
+    return out
+
+
+def sfm_pack_maps(st, repeats=1):
+    """The same assembly run by C++ over std::map containers built from the
+    state, as the engine runs it (liboracle.so); returns (result dict, mean
+    seconds of the assembly loop)."""
+    abi = _abi()
+    lib = load()
+    ep = abi.EnginePack(st)
+    s = ep.state_struct()
+    ni, ne = ep.ni, ep.ne
+    ext = np.zeros((max(ni, 1), 6))
+    intr = np.zeros((max(ep.ng, 1), 6))
+    pts = np.zeros((max(ep.nt, 1), 3))
+    obs = np.zeros((max(ne, 1), 2))
+    idx = [np.zeros(max(ne, 1), np.uint32) for _ in range(3)]
+    counts = np.zeros(3, np.int64)
+    sec = np.zeros(1)
+    lib.oracle_sfm_pack_maps(C.byref(s), int(st["first_added"]), ext.ctypes.data, intr.ctypes.data, pts.ctypes.data,
+                             obs.ctypes.data, idx[0].ctypes.data, idx[1].ctypes.data, idx[2].ctypes.data,
+                             counts.ctypes.data, int(repeats), sec.ctypes.data)
+    nc, no = int(counts[0]), int(counts[1])
+    return ({"extrinsics": ext[:nc], "intrinsics": intr[:ep.ng], "points": pts[:ep.nt], "observations": obs[:no],
+             "camera_index": idx[0][:no], "intrinsic_index": idx[1][:no], "point_index": idx[2][:no],
+             "num_cameras": nc, "locked_camera": int(counts[2])}, float(sec[0]))
+
+
+def _logcombi(k, n):
+    """logcombi (estimator_acransac.h:40-49)."""
+    if k >= n or k <= 0:
+        return 0.0
+    if n - k < k:
+        k = n - k
+    r = 0.0
+    for i in range(1, k + 1):
+        r += math.log10(n - i + 1) - math.log10(i)
+    return r
+
+
+def acransac_tables(n, sample_size):
+    """makelogcombi_n / makelogcombi_k (estimator_acransac.h:52-65), float32."""
+    return (np.array([_logcombi(k, n) for k in range(n + 1)], np.float32),
+            np.array([_logcombi(sample_size, m) for m in range(n + 1)], np.float32))
+
+
+def acransac_score(x2d, x3d, models, sample_size, max_models, logalpha0, mult_error=1.0,
+                   max_threshold=math.inf, tables=None):
+    """The per-model scoring of ACRANSAC's main loop (estimator_acransac.h:
+    170-200) on normalised points: ResectionSquaredResidualError
+    (sfm_robust.h:197-204), std::sort of (error, index), bestNFA (:75-97).
+    Returns nfa, k, e[k-1] per model and the sorted index order."""
+    x2d = np.asarray(x2d, np.float64).reshape(-1, 2)
+    X = np.asarray(x3d, np.float64).reshape(-1, 3)
+    n = len(x2d)
+    logc_n, logc_k = tables if tables is not None else acransac_tables(n, sample_size)
+    loge0 = math.log10(max_models * (n - sample_size))
+    M = np.asarray(models, np.float64).reshape(-1, 3, 4)
+    nfa, kk, emax, order = [], [], [], []
+    fmin = float(np.finfo(np.float32).tiny)
+    for P in M:
+        h = X @ P[:, :3].T + P[:, 3]
+        d = h[:, :2] / h[:, 2:] - x2d
+        e = d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]
+        o = np.lexsort((np.arange(n), e))
+        es = e[o]
+        ks = np.arange(sample_size + 1, n + 1)
+        ok = np.cumprod(es[ks - 1] <= max_threshold).astype(bool)
+        ks = ks[ok]
+        v = loge0 + (logalpha0 + mult_error * np.log10(es[ks - 1] + fmin)) * (ks - sample_size) \
+            + logc_n[ks].astype(np.float64) + logc_k[ks].astype(np.float64)
+        if len(v) and np.min(v) < math.inf:
+            j = int(np.argmin(v))
+            nfa.append(float(v[j]))
+            kk.append(int(ks[j]))
+            emax.append(float(es[ks[j] - 1]))
+        else:
+            nfa.append(math.inf)
+            kk.append(sample_size)
+            emax.append(math.inf)
+        order.append(o)
+    return np.array(nfa), np.array(kk), np.array(emax), np.array(order)
+
+
+def acransac_replay(nfa, k, emax, order, models_per_fit, normalizer):
+    """ACRANSAC's model selection (estimator_acransac.h:172-244) over scored
+    models in the order they were drawn: a model strictly below the running
+    minimum NFA becomes the result; no result unless the minimum is below 0.
+    Returns (error_max unnormalised, min_nfa, inliers, model index)."""
+    min_nfa, best = math.inf, -1
+    m = 0
+    for cnt in np.asarray(models_per_fit, np.int64):
+        for _ in range(int(cnt)):
+            if nfa[m] < min_nfa:
+                min_nfa, best = nfa[m], m
+            m += 1
+    if best < 0:
+        return math.inf, min_nfa, np.zeros(0, np.int64), -1
+    inliers = np.asarray(order[best][:int(k[best])], np.int64)
+    if min_nfa >= 0:
+        inliers = inliers[:0]
+    err = math.sqrt(emax[best]) / normalizer if len(inliers) else emax[best]
+    return err, min_nfa, inliers, best
+
+
+def acransac_score_cpp(x2d, x3d, models, sample_size, max_models, logalpha0, mult_error=1.0,
+                       max_threshold=math.inf, with_order=True):
+    """The same scoring in C++ (liboracle), model after model with std::sort;
+    returns (nfa, k, e[k-1], order or None, mean seconds per model)."""
+    lib = load()
+    x2d = np.ascontiguousarray(x2d, np.float64)
+    x3d = np.ascontiguousarray(x3d, np.float64)
+    models = np.ascontiguousarray(models, np.float64)
+    n, h = len(x2d.reshape(-1, 2)), len(models.reshape(-1, 12))
+    nfa, emax = np.zeros(h), np.zeros(h)
+    k = np.zeros(h, np.int32)
+    order = np.zeros((h, n), np.uint32) if with_order else None
+    sec = np.zeros(1)
+    lib.oracle_acransac_score(sample_size, max_models, logalpha0, mult_error, max_threshold, n, x2d.ctypes.data,
+                              x3d.ctypes.data, h, models.ctypes.data, nfa.ctypes.data, k.ctypes.data,
+                              emax.ctypes.data, order.ctypes.data if with_order else None, sec.ctypes.data)
+    return nfa, k, emax, order, float(sec[0])

@@ -29,6 +29,11 @@
 //                                            libs/base/include/mvg/math/numeric.h:228-240
 //   - TriangulateNView(/Algebraic), Triangulation::compute/error
 //                                            libs/multiview/src/triangulation_nview.cpp:8-121
+//   - BundleAdjustment's problem assembly    libs/sfm/src/sfm_incremental_engine.cpp:1250-1393,
+//     over the engine's std::map state, with RotationMatrixToAngleAxis
+//                                            include/ceres/rotation.h:266-370
+//   - AC-RANSAC model scoring (residuals, sort, bestNFA)
+//                                            libs/feature/include/mvg/feature/estimator_acransac.h:40-200
 #include <algorithm>
 #include <chrono>
 #include <cfloat>
@@ -36,6 +41,9 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <map>
+#include <set>
+#include <utility>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -43,6 +51,7 @@
 
 #include "../include/gbba.h"
 #include "../include/gbtri.h"
+#include "../include/gbsfm.h"
 
 namespace {
 
@@ -906,6 +915,217 @@ int oracle_tri_linear_gn(const double* P, const int64_t* offs, const uint32_t* c
     if (status) status[t] = st;
     if (min_depth) min_depth[t] = n > 0 ? md : 0.0;
   }
+  return 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------- engine BA assembly
+
+// ceres::RotationMatrixToQuaternion (Shoemake, rotation.h:312-350) and
+// QuaternionToAngleAxis (:266-306) on a column-major matrix, as the engine
+// passes Eigen's Mat3::data().
+static void oracle_rotation_to_angle_axis(const double* Rc, double* aa) {
+  auto R = [&](int i, int j) { return Rc[3 * j + i]; };
+  double q[4];
+  const double trace = R(0, 0) + R(1, 1) + R(2, 2);
+  if (trace >= 0.0) {
+    double t = std::sqrt(trace + 1.0);
+    q[0] = 0.5 * t;
+    t = 0.5 / t;
+    q[1] = (R(2, 1) - R(1, 2)) * t;
+    q[2] = (R(0, 2) - R(2, 0)) * t;
+    q[3] = (R(1, 0) - R(0, 1)) * t;
+  } else {
+    int i = R(1, 1) > R(0, 0) ? 1 : 0;
+    if (R(2, 2) > R(i, i)) i = 2;
+    const int j = (i + 1) % 3, k = (j + 1) % 3;
+    double t = std::sqrt(R(i, i) - R(j, j) - R(k, k) + 1.0);
+    q[i + 1] = 0.5 * t;
+    t = 0.5 / t;
+    q[0] = (R(k, j) - R(j, k)) * t;
+    q[j + 1] = (R(j, i) + R(i, j)) * t;
+    q[k + 1] = (R(k, i) + R(i, k)) * t;
+  }
+  const double s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  double kk = 2.0;
+  if (s2 > 0.0) {
+    const double st = std::sqrt(s2), ct = q[0];
+    kk = 2.0 * (ct < 0.0 ? std::atan2(-st, -ct) : std::atan2(st, ct)) / st;
+  }
+  for (int a = 0; a < 3; ++a) aa[a] = q[a + 1] * kk;
+}
+
+struct OracleEngineCamera {
+  double R[9];  // column-major, as Eigen stores rotation_matrix_
+  double t[3];
+};
+
+extern "C" {
+
+// The engine's maps are built from the dense state (not timed); then the
+// assembly loop of BundleAdjustment runs `repeats` times over them and its
+// mean wall time goes to *seconds.  The last run's problem is written in the
+// gbsfm_ba_arrays layout; counts[0..2] = cameras, observations, locked block.
+int oracle_sfm_pack_maps(const gbsfm_engine_state* st, int64_t first_added, double* ext, double* intr, double* pts,
+                         double* obs, uint32_t* cam_idx, uint32_t* intr_idx, uint32_t* pt_idx, int64_t* counts,
+                         int repeats, double* seconds) {
+  std::map<size_t, OracleEngineCamera> map_Camera;
+  std::map<size_t, std::vector<std::pair<float, float> > > map_features;
+  std::map<size_t, std::vector<size_t> > map_images_id_per_intrinsic_group;
+  std::map<size_t, std::vector<double> > map_intrinsics_per_group;
+  std::map<size_t, std::vector<double> > map_3d_points;
+  std::map<size_t, std::map<size_t, size_t> > map_reconstructed;
+  for (int64_t g = 0; g < st->num_intrinsic_groups; ++g)
+    map_intrinsics_per_group[(size_t)g] = std::vector<double>(st->group_intrinsics + 6 * g,
+                                                               st->group_intrinsics + 6 * g + 6);
+  for (int64_t i = 0; i < st->num_images; ++i) {
+    map_images_id_per_intrinsic_group[st->intrinsic_group[i]].push_back((size_t)i);
+    std::vector<std::pair<float, float> >& f = map_features[(size_t)i];
+    for (int64_t k = st->feature_offsets[i]; k < st->feature_offsets[i + 1]; ++k)
+      f.push_back(std::make_pair(st->features[2 * k], st->features[2 * k + 1]));
+    if (!st->reconstructed[i]) continue;
+    const gbsfm_camera& c = st->cameras[i];
+    OracleEngineCamera e;
+    for (int r = 0; r < 3; ++r)
+      for (int k = 0; k < 3; ++k) e.R[3 * k + r] = c.R[3 * r + k];
+    for (int r = 0; r < 3; ++r) e.t[r] = c.t[r];
+    map_Camera[(size_t)i] = e;
+  }
+  for (int64_t t = 0; t < st->num_points; ++t) {
+    map_3d_points[(size_t)t] = std::vector<double>(st->points + 3 * t, st->points + 3 * t + 3);
+    std::map<size_t, size_t>& tr = map_reconstructed[(size_t)t];
+    for (int64_t e = st->track_offsets[t]; e < st->track_offsets[t + 1]; ++e)
+      tr[st->track_image[e]] = st->track_feature[e];
+  }
+
+  std::vector<double> parameters, observations;
+  std::vector<size_t> point_index, cam_ext, cam_intr;
+  size_t num_cameras = 0, num_intrinsic = 0;
+  int64_t locked = -1;
+  const auto t0 = std::chrono::steady_clock::now();
+  for (int rep = 0; rep < std::max(1, repeats); ++rep) {
+    parameters.clear();
+    observations.clear();
+    point_index.clear();
+    cam_ext.clear();
+    cam_intr.clear();
+    num_cameras = map_Camera.size();
+    num_intrinsic = map_images_id_per_intrinsic_group.size();
+    size_t measurements = 0;
+    for (auto it = map_3d_points.begin(); it != map_3d_points.end(); ++it)
+      measurements += map_reconstructed[it->first].size();
+    point_index.reserve(measurements);
+    cam_ext.reserve(measurements);
+    cam_intr.reserve(measurements);
+    observations.reserve(2 * measurements);
+    parameters.reserve(6 * num_cameras + 6 * num_intrinsic + 3 * map_3d_points.size());
+    std::set<size_t> set_camIndex;
+    std::map<size_t, size_t> ext_number, intr_number;
+    size_t cpt = 0;
+    for (auto it = map_Camera.begin(); it != map_Camera.end(); ++it, ++cpt) {
+      set_camIndex.insert(it->first);
+      ext_number.insert(std::make_pair(it->first, cpt));
+      double aa[3];
+      oracle_rotation_to_angle_axis(it->second.R, aa);
+      for (int a = 0; a < 3; ++a) parameters.push_back(aa[a]);
+      for (int a = 0; a < 3; ++a) parameters.push_back(it->second.t[a]);
+    }
+    for (auto it = map_intrinsics_per_group.begin(); it != map_intrinsics_per_group.end(); ++it)
+      for (int j = 0; j < 6; ++j) parameters.push_back(it->second[j]);
+    cpt = 0;
+    for (auto it = map_images_id_per_intrinsic_group.begin(); it != map_images_id_per_intrinsic_group.end();
+         ++it, ++cpt)
+      for (size_t k = 0; k < it->second.size(); ++k) intr_number.insert(std::make_pair(it->second[k], cpt));
+    for (auto it = map_3d_points.begin(); it != map_3d_points.end(); ++it)
+      for (int j = 0; j < 3; ++j) parameters.push_back(it->second[j]);
+    cpt = 0;
+    for (auto it = map_3d_points.begin(); it != map_3d_points.end(); ++it, ++cpt) {
+      const std::map<size_t, size_t>& tr = map_reconstructed[it->first];
+      for (auto e = tr.begin(); e != tr.end(); ++e) {
+        if (set_camIndex.find(e->first) == set_camIndex.end()) continue;
+        const std::pair<float, float>& f = map_features[e->first][e->second];
+        observations.push_back(f.first);
+        observations.push_back(f.second);
+        point_index.push_back(cpt);
+        cam_ext.push_back(ext_number[e->first]);
+        cam_intr.push_back(intr_number[e->first]);
+      }
+    }
+    locked = -1;
+    if (first_added >= 0 && !ext_number.empty()) {
+      const size_t k = ext_number[(size_t)first_added];
+      if (k < cam_ext.size()) locked = (int64_t)cam_ext[k];
+    }
+  }
+  *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() / std::max(1, repeats);
+  const size_t nc = num_cameras, ng = num_intrinsic;
+  if (ext) std::memcpy(ext, parameters.data(), sizeof(double) * 6 * nc);
+  if (intr) std::memcpy(intr, parameters.data() + 6 * nc, sizeof(double) * 6 * ng);
+  if (pts) std::memcpy(pts, parameters.data() + 6 * (nc + ng), sizeof(double) * 3 * st->num_points);
+  if (obs) std::memcpy(obs, observations.data(), sizeof(double) * observations.size());
+  for (size_t o = 0; o < point_index.size(); ++o) {
+    if (cam_idx) cam_idx[o] = (uint32_t)cam_ext[o];
+    if (intr_idx) intr_idx[o] = (uint32_t)cam_intr[o];
+    if (pt_idx) pt_idx[o] = (uint32_t)point_index[o];
+  }
+  counts[0] = (int64_t)nc;
+  counts[1] = (int64_t)point_index.size();
+  counts[2] = locked;
+  return 0;
+}
+
+
+// AC-RANSAC scoring of a batch of models as the reference's main loop does
+// it, model after model (estimator_acransac.h:170-200): residuals
+// (ResectionSquaredResidualError, sfm_robust.h:197-204), std::sort of
+// (error, index) pairs, bestNFA (:75-97) with the float logcombi tables
+// (:40-65).  Returns the mean seconds per model in *seconds.
+static double oracle_logcombi(size_t k, size_t n) {
+  if (k >= n || k <= 0) return 0.0;
+  if (n - k < k) k = n - k;
+  double r = 0.0;
+  for (size_t i = 1; i <= k; i++) r += std::log10((double)(n - i + 1)) - std::log10((double)i);
+  return r;
+}
+
+int oracle_acransac_score(int sample_size, int max_models, double logalpha0, double mult_error, double max_threshold,
+                          int64_t n, const double* x2d, const double* x3d, int64_t num_models, const double* models,
+                          double* nfa, int32_t* num_inliers, double* error_max, uint32_t* order, double* seconds) {
+  const auto t0 = std::chrono::steady_clock::now();
+  std::vector<float> logc_n(n + 1), logc_k(n + 1);
+  for (int64_t k = 0; k <= n; ++k) logc_n[k] = (float)oracle_logcombi((size_t)k, (size_t)n);
+  for (int64_t m = 0; m <= n; ++m) logc_k[m] = (float)oracle_logcombi((size_t)sample_size, (size_t)m);
+  const double loge0 = std::log10((double)max_models * (double)(n - sample_size));
+  std::vector<std::pair<double, size_t> > e((size_t)n);
+  for (int64_t h = 0; h < num_models; ++h) {
+    const double* P = models + 12 * h;
+    for (int64_t i = 0; i < n; ++i) {
+      const double* X = x3d + 3 * i;
+      double hx[3];
+      for (int r = 0; r < 3; ++r) hx[r] = P[4 * r] * X[0] + P[4 * r + 1] * X[1] + P[4 * r + 2] * X[2] + P[4 * r + 3];
+      const double dx = hx[0] / hx[2] - x2d[2 * i], dy = hx[1] / hx[2] - x2d[2 * i + 1];
+      e[(size_t)i] = std::make_pair(dx * dx + dy * dy, (size_t)i);
+    }
+    std::sort(e.begin(), e.end());
+    double best = std::numeric_limits<double>::infinity();
+    int64_t best_k = sample_size;
+    for (int64_t k = sample_size + 1; k <= n && e[k - 1].first <= max_threshold; ++k) {
+      const double logalpha = logalpha0 + mult_error * std::log10(e[k - 1].first + std::numeric_limits<float>::min());
+      const double v = loge0 + logalpha * (double)(k - sample_size) + logc_n[k] + logc_k[k];
+      if (v < best) {
+        best = v;
+        best_k = k;
+      }
+    }
+    nfa[h] = best;
+    num_inliers[h] = (int32_t)best_k;
+    error_max[h] = best_k > sample_size ? e[best_k - 1].first : std::numeric_limits<double>::infinity();
+    if (order)
+      for (int64_t i = 0; i < n; ++i) order[h * n + i] = (uint32_t)e[(size_t)i].second;
+  }
+  *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count() /
+             (double)std::max<int64_t>(1, num_models);
   return 0;
 }
 

@@ -26,7 +26,14 @@
 //   ref_harness histogram <in> <out>  ComputeResidualsHistogram
 //       (sfm_incremental_engine.cpp:1550-1616): float residuals, MinMaxMeanMedian
 //       and Histogram<double>(min, max, 10).
-// The last three restate the engines' loops (whose classes need the whole
+//   ref_harness pack <in> <out>    BundleAdjustment's assembly of its std::map
+//       state into the BA problem and its write-back of refined parameters
+//       (sfm_incremental_engine.cpp:1250-1393, 1475-1546) with ceres's
+//       RotationMatrixToAngleAxis / AngleAxisToRotationMatrix.
+//   ref_harness acransac <in> <out>  robustResection's ACRANSAC with the
+//       reference's resection kernels (six-point DLT, or P3P with K), every
+//       model it draws recorded and scored by the reference's bestNFA.
+// The pair, reject, histogram and pack modes restate the engines' loops (whose classes need the whole
 // engine) around the reference's own camera, triangulation and histogram code.
 //
 // File format ("kv text"): a sequence of records `name count` followed by
@@ -37,7 +44,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <iostream>
 #include <map>
+#include <set>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -55,6 +64,12 @@ using namespace mvg::camera;  // pinhole_brown_rt_ceres_functor.h expects it
 #include "mvg/sfm/pinhole_brown_rt_ceres_functor.h"
 #include "mvg/sfm/pinhole_ceres_functor.h"
 #include "mvg/sfm/sfm_bundle_adjustment_helper_tonly.h"
+// sfm_robust.h logs through MVG_INFO without including its definition; the
+// harness discards that log.
+#ifndef MVG_INFO
+#define MVG_INFO if (false) std::cerr
+#endif
+#include "mvg/sfm/sfm_robust.h"
 
 using namespace mvg::multiview;
 using namespace mvg::sfm;
@@ -516,6 +531,245 @@ static int RunHistogram(const KV& kv, const char* out) {
   return 0;
 }
 
+// The incremental engine's BA assembly and write-back
+// (libs/sfm/src/sfm_incremental_engine.cpp:1250-1393, 1475-1546) over the
+// engine's own std::map containers, built here from dense arrays; the
+// rotation conversions are ceres's (rotation.h).  Outputs the packed
+// parameters_ / observations_ / index vectors, the locked extrinsic block and
+// the cameras written back from a given refined parameter set.
+static int RunPack(const KV& kv, const char* out) {
+  const std::vector<double>& cams = Get(kv, "cameras");
+  const std::vector<double>& rec = Get(kv, "reconstructed");
+  const std::vector<double>& image_group_key = Get(kv, "image_group_key");
+  const std::vector<double>& group_keys = Get(kv, "group_keys");
+  const std::vector<double>& group_intr = Get(kv, "group_intrinsics");
+  const std::vector<double>& foff = Get(kv, "feature_offsets");
+  const std::vector<double>& feats = Get(kv, "features");
+  const std::vector<double>& track_keys = Get(kv, "track_keys");
+  const std::vector<double>& pts = Get(kv, "points");
+  const std::vector<double>& toff = Get(kv, "track_offsets");
+  const std::vector<double>& timg = Get(kv, "track_image");
+  const std::vector<double>& tfeat = Get(kv, "track_feature");
+  const double first_added = Get1(kv, "first_added", -1);
+  const size_t ni = rec.size();
+
+  // engine state as the reference holds it
+  std::map<size_t, BrownPinholeCamera> map_Camera;
+  std::map<size_t, std::vector<std::pair<float, float> > > map_features;
+  std::map<size_t, std::vector<size_t> > map_images_id_per_intrinsic_group;
+  std::map<size_t, Vec6> map_intrinsics_per_group;
+  std::map<size_t, Vec3> map_3d_points;
+  std::map<size_t, std::map<size_t, size_t> > map_reconstructed;
+  for (size_t g = 0; g < group_keys.size(); ++g) {
+    Vec6 v;
+    for (int j = 0; j < 6; ++j) v(j) = group_intr[6 * g + j];
+    map_intrinsics_per_group[(size_t)group_keys[g]] = v;
+  }
+  for (size_t i = 0; i < ni; ++i) {
+    map_images_id_per_intrinsic_group[(size_t)image_group_key[i]].push_back(i);
+    std::vector<std::pair<float, float> >& f = map_features[i];
+    for (size_t k = (size_t)foff[i]; k < (size_t)foff[i + 1]; ++k)
+      f.push_back(std::make_pair((float)feats[2 * k], (float)feats[2 * k + 1]));
+    if (rec[i] == 0) continue;
+    const double* c = &cams[18 * i];
+    Mat3 R;
+    for (int r = 0; r < 3; ++r) for (int k = 0; k < 3; ++k) R(r, k) = c[3 * r + k];
+    map_Camera[i] = BrownPinholeCamera(c[12], c[13], c[14], R, Vec3(c[9], c[10], c[11]), c[15], c[16], c[17]);
+  }
+  for (size_t t = 0; t < track_keys.size(); ++t) {
+    const size_t id = (size_t)track_keys[t];
+    map_3d_points[id] = Vec3(pts[3 * t], pts[3 * t + 1], pts[3 * t + 2]);
+    std::map<size_t, size_t>& tr = map_reconstructed[id];
+    for (size_t e = (size_t)toff[t]; e < (size_t)toff[t + 1]; ++e) tr[(size_t)timg[e]] = (size_t)tfeat[e];
+  }
+
+  // the pack (:1250-1393)
+  size_t measurements = 0;
+  for (std::map<size_t, Vec3>::const_iterator it = map_3d_points.begin(); it != map_3d_points.end(); ++it)
+    measurements += map_reconstructed[it->first].size();
+  std::vector<double> parameters, observations, point_index, cam_ext, cam_intr;
+  std::set<size_t> set_camIndex;
+  std::map<size_t, size_t> ext_number, intr_number;
+  size_t cpt = 0;
+  for (std::map<size_t, BrownPinholeCamera>::const_iterator it = map_Camera.begin(); it != map_Camera.end();
+       ++it, ++cpt) {
+    set_camIndex.insert(it->first);
+    ext_number.insert(std::make_pair(it->first, cpt));
+    const Mat3 R = it->second.rotation_matrix_;
+    double aa[3];
+    ceres::RotationMatrixToAngleAxis((const double*)R.data(), aa);
+    const Vec3 t = it->second.translation_vector_;
+    parameters.push_back(aa[0]);
+    parameters.push_back(aa[1]);
+    parameters.push_back(aa[2]);
+    parameters.push_back(t[0]);
+    parameters.push_back(t[1]);
+    parameters.push_back(t[2]);
+  }
+  for (std::map<size_t, Vec6>::const_iterator it = map_intrinsics_per_group.begin();
+       it != map_intrinsics_per_group.end(); ++it)
+    for (int j = 0; j < 6; ++j) parameters.push_back(it->second(j));
+  cpt = 0;
+  for (std::map<size_t, std::vector<size_t> >::const_iterator it = map_images_id_per_intrinsic_group.begin();
+       it != map_images_id_per_intrinsic_group.end(); ++it, ++cpt)
+    for (size_t k = 0; k < it->second.size(); ++k) intr_number.insert(std::make_pair(it->second[k], cpt));
+  for (std::map<size_t, Vec3>::const_iterator it = map_3d_points.begin(); it != map_3d_points.end(); ++it)
+    for (int j = 0; j < 3; ++j) parameters.push_back(it->second[j]);
+  cpt = 0;
+  for (std::map<size_t, Vec3>::const_iterator it = map_3d_points.begin(); it != map_3d_points.end(); ++it, ++cpt) {
+    const std::map<size_t, size_t>& tr = map_reconstructed[it->first];
+    for (std::map<size_t, size_t>::const_iterator e = tr.begin(); e != tr.end(); ++e) {
+      if (set_camIndex.find(e->first) == set_camIndex.end()) continue;
+      const std::pair<float, float>& f = map_features[e->first][e->second];
+      observations.push_back(f.first);
+      observations.push_back(f.second);
+      point_index.push_back((double)cpt);
+      cam_ext.push_back((double)ext_number[e->first]);
+      cam_intr.push_back((double)intr_number[e->first]);
+    }
+  }
+  // the locked block (:1437-1443): mutable_camera_extrinsic_for_observation
+  // indexes camera_index_extrinsic with the camera ordinal
+  double locked = -1;
+  if (first_added >= 0 && !ext_number.empty()) {
+    const size_t k = ext_number[(size_t)first_added];
+    locked = k < cam_ext.size() ? cam_ext[k] : -2;  // -2: the reference reads past its vector
+  }
+
+  // the write-back (:1491-1516) of a refined parameter set
+  const std::vector<double>& ref_ext = Get(kv, "refined_extrinsics");
+  const std::vector<double>& ref_intr = Get(kv, "refined_intrinsics");
+  std::vector<double> unpacked;
+  for (std::map<size_t, BrownPinholeCamera>::const_iterator it = map_Camera.begin(); it != map_Camera.end(); ++it) {
+    const size_t e = ext_number[it->first];
+    const double* camE = &ref_ext[6 * e];
+    Mat3 R;
+    ceres::AngleAxisToRotationMatrix(camE, R.data());
+    const double* ci = &ref_intr[6 * intr_number[it->first]];
+    const BrownPinholeCamera c(ci[0], ci[1], ci[2], R, Vec3(camE[3], camE[4], camE[5]), ci[3], ci[4], ci[5]);
+    for (int r = 0; r < 3; ++r) for (int k = 0; k < 3; ++k) unpacked.push_back(c.rotation_matrix_(r, k));
+    for (int r = 0; r < 3; ++r) unpacked.push_back(c.translation_vector_[r]);
+    unpacked.push_back(c._f);
+    unpacked.push_back(c._ppx);
+    unpacked.push_back(c._ppy);
+    unpacked.push_back(c._k1);
+    unpacked.push_back(c._k2);
+    unpacked.push_back(c._k3);
+  }
+  KVWriter w(out);
+  w.put("parameters", parameters);
+  w.put("observations", observations);
+  w.put("point_index", point_index);
+  w.put("camera_index_extrinsic", cam_ext);
+  w.put("camera_index_intrinsic", cam_intr);
+  w.put1("num_cameras", (double)map_Camera.size());
+  w.put1("measurements", (double)measurements);
+  w.put1("locked", locked);
+  w.put("unpacked", unpacked);
+  return 0;
+}
+
+// robustResection's AC-RANSAC (libs/sfm/include/mvg/sfm/sfm_robust.h:207-254)
+// with the reference's kernels, solvers and ACRANSAC, the kernel wrapped so
+// that every model its Fit returns is recorded.  Then, for each recorded
+// model, the reference's per-model scoring: ResectionSquaredResidualError
+// on the normalised points, std::sort of (error, index) and bestNFA with the
+// logcombi tables.  Outputs the normalised points, the models, their
+// (nfa, k, e[k-1]), the models per iteration, and ACRANSAC's own result.
+template <class Base>
+struct RecordingKernel : public Base {
+  RecordingKernel(const Mat& a, int w, int h, const Mat& b) : Base(a, w, h, b) {}
+  RecordingKernel(const Mat& a, const Mat& b, const Mat3& K) : Base(a, b, K) {}
+  mutable std::vector<Mat34> models;
+  mutable std::vector<double> per_fit;
+  void Fit(const std::vector<size_t>& samples, std::vector<Mat34>* m) const {
+    Base::Fit(samples, m);
+    models.insert(models.end(), m->begin(), m->end());
+    per_fit.push_back((double)m->size());
+  }
+};
+
+template <class Kernel>
+static void RecordAcransac(const Kernel& kernel, const Mat& xn, const Mat& x3d, size_t iters, KVWriter& w) {
+  std::vector<size_t> inliers;
+  Mat34 P;
+  const std::pair<double, double> res =
+      mvg::feature::ACRANSAC(kernel, inliers, iters, &P, std::numeric_limits<double>::infinity(), false);
+  const size_t n = (size_t)xn.cols(), s = Kernel::MINIMUM_SAMPLES;
+  std::vector<float> logc_n, logc_k;
+  mvg::feature::makelogcombi_n(n, logc_n);
+  mvg::feature::makelogcombi_k(s, n, logc_k);
+  const double loge0 = log10((double)Kernel::MAX_MODELS * (n - s));
+  std::vector<double> models, nfa, k, emax;
+  std::vector<mvg::feature::ErrorIndex> e(n);
+  for (size_t m = 0; m < kernel.models.size(); ++m) {
+    const Mat34& M = kernel.models[m];
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 4; ++c) models.push_back(M(r, c));
+    for (size_t i = 0; i < n; ++i)
+      e[i] = mvg::feature::ErrorIndex(mvg::sfm::ResectionSquaredResidualError::Error(M, xn.col(i), x3d.col(i)), i);
+    std::sort(e.begin(), e.end());
+    const mvg::feature::ErrorIndex best = mvg::feature::bestNFA(
+        (int)s, kernel.logalpha0(), e, loge0, std::numeric_limits<double>::infinity(), logc_n, logc_k,
+        kernel.multError());
+    nfa.push_back(best.first);
+    k.push_back((double)best.second);
+    emax.push_back(best.second > s ? e[best.second - 1].first : std::numeric_limits<double>::infinity());
+  }
+  std::vector<double> xnv, inl(inliers.begin(), inliers.end()), Pv;
+  for (size_t i = 0; i < n; ++i) { xnv.push_back(xn(0, i)); xnv.push_back(xn(1, i)); }
+  for (int r = 0; r < 3; ++r) for (int c = 0; c < 4; ++c) Pv.push_back(P(r, c));
+  w.put("x2d_normalized", xnv);
+  w.put("models", models);
+  w.put("models_per_fit", kernel.per_fit);
+  w.put("nfa", nfa);
+  w.put("k", k);
+  w.put("error_max", emax);
+  w.put1("sample_size", (double)s);
+  w.put1("max_models", (double)Kernel::MAX_MODELS);
+  w.put1("logalpha0", kernel.logalpha0());
+  w.put1("normalizer", kernel.normalizer1()(0, 0));
+  w.put1("result_error_max", res.first);
+  w.put1("result_min_nfa", res.second);
+  w.put("result_inliers", inl);
+  w.put("result_P", Pv);
+}
+
+static int RunAcransac(const KV& kv, const char* out) {
+  const std::vector<double>& x2 = Get(kv, "x2d");
+  const std::vector<double>& x3 = Get(kv, "x3d");
+  const size_t n = x2.size() / 2;
+  Mat x2d(2, n), x3d(3, n);
+  for (size_t i = 0; i < n; ++i) {
+    x2d(0, i) = x2[2 * i];
+    x2d(1, i) = x2[2 * i + 1];
+    for (int r = 0; r < 3; ++r) x3d(r, i) = x3[3 * i + r];
+  }
+  srand((unsigned)Get1(kv, "seed", 1));
+  const size_t iters = (size_t)Get1(kv, "iterations", 4096);
+  KVWriter w(out);
+  if (kv.count("K")) {
+    const std::vector<double>& kk = Get(kv, "K");
+    Mat3 K;
+    for (int r = 0; r < 3; ++r) for (int c = 0; c < 3; ++c) K(r, c) = kk[3 * r + c];
+    typedef mvg::feature::ACKernelAdaptorResection_K<mvg::multiview::P3PSolver,
+        mvg::sfm::ResectionSquaredResidualError, mvg::feature::UnnormalizerResection, Mat34> Base;
+    RecordingKernel<Base> kernel(x2d, x3d, K);
+    Mat xn;
+    mvg::multiview::applyTransformationToPoints(x2d, K.inverse(), &xn);
+    RecordAcransac(kernel, xn, x3d, iters, w);
+  } else {
+    const int width = (int)Get1(kv, "width", 1920), height = (int)Get1(kv, "height", 1080);
+    typedef mvg::feature::ACKernelAdaptorResection<mvg::multiview::resection::SixPointResectionSolver,
+        mvg::sfm::ResectionSquaredResidualError, mvg::feature::UnnormalizerResection, Mat34> Base;
+    RecordingKernel<Base> kernel(x2d, width, height, x3d);
+    Mat xn;
+    Mat3 N1;
+    mvg::multiview::NormalizePoints(x2d, &xn, &N1, width, height);
+    RecordAcransac(kernel, xn, x3d, iters, w);
+  }
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc < 3) { fprintf(stderr, "usage: ref_harness <mode> ...\n"); return 2; }
   const std::string mode = argv[1];
@@ -526,6 +780,8 @@ int main(int argc, char** argv) {
   if (mode == "two-view" && argc == 4) return RunTwoView(ReadKV(argv[2]), argv[3]);
   if (mode == "reject" && argc == 4) return RunReject(ReadKV(argv[2]), argv[3]);
   if (mode == "histogram" && argc == 4) return RunHistogram(ReadKV(argv[2]), argv[3]);
+  if (mode == "pack" && argc == 4) return RunPack(ReadKV(argv[2]), argv[3]);
+  if (mode == "acransac" && argc == 4) return RunAcransac(ReadKV(argv[2]), argv[3]);
   fprintf(stderr, "bad arguments\n");
   return 2;
 }

@@ -161,7 +161,31 @@ def sfm_scans(tmp):
          **{"ref_hist_" + k: v for k, v in h.items()})
 
 
+def sfm_pack(tmp):
+    """The engine's BA assembly and write-back from its own std::map state,
+    with ceres's rotation conversions."""
+    st = scenes.engine_state()
+    kv = {k: v for k, v in st.items() if k != "intrinsic_group"}
+    kv["image_group_key"] = st["group_keys"][st["intrinsic_group"]]
+    r = oracle.ref_run("pack", kv, tmp)
+    save("sfm_pack.npz", **st, **{"ref_" + k: v for k, v in r.items()})
+
+
+def sfm_acransac(tmp):
+    """robustResection's AC-RANSAC from the reference: the six-point DLT
+    kernel (unknown K, 4,096 iterations) and the P3P kernel (known K, 1,024
+    iterations), every model drawn recorded with its reference score."""
+    sc = scenes.resection_scene()
+    base = {"x2d": sc["x2d"], "x3d": sc["x3d"], "width": sc["width"], "height": sc["height"], "seed": 1}
+    r = oracle.ref_run("acransac", dict(base, iterations=4096), tmp)
+    save("sfm_acransac_6pt.npz", **sc, **{"ref_" + k: v for k, v in r.items()})
+    r = oracle.ref_run("acransac", dict(base, iterations=1024, K=sc["K"]), tmp)
+    save("sfm_acransac_p3p.npz", **sc, **{"ref_" + k: v for k, v in r.items()})
+
+
 GENERATORS = {
+    "sfm_acransac": sfm_acransac,
+    "sfm_pack": sfm_pack,
     "sfm_scans": sfm_scans,
     "tri_ring": lambda tmp: (tri_ring(tmp, 2, 12), tri_ring(tmp, 5, 6)),
     "tri_noisy": tri_noisy,
@@ -226,6 +250,8 @@ def main():
     ba_iterative(tmp)
     ba_windows(tmp)
     sfm_scans(tmp)
+    sfm_pack(tmp)
+    sfm_acransac(tmp)
 
 
 if __name__ == "__main__":
