@@ -8,12 +8,18 @@
 // reduced camera system <= 256 unknowns), so one CTA owns one problem for its
 // whole solve:
 //   - in FP32 the lower triangle of S lives in shared memory (n(n+1)/2
-//     values, <= 131.6 KB) and the pair products are accumulated into it
-//     with shared atomics;
+//     values, <= 131.6 KB);
 //   - in FP64 (the plain FP64 path and the mixed path's FP64 polish) S lives
-//     in a per-CTA slice of global memory (L2-resident), accumulated with
-//     native global FP64 reductions: shared memory has no FP64 add, and an
-//     FP64 S of n = 256 would not fit it;
+//     in a per-CTA slice of global memory (L2-resident): an FP64 S of
+//     n = 256 would not fit shared memory;
+//   - every sum the Schur build scatters (S, rhs, column norms, gradient) is
+//     accumulated in fixed point, integers under atomics: integer addition is
+//     associative, so the result does not depend on the order in which warps
+//     reach an entry and a solve is bitwise repeatable.  The scale is a power
+//     of two chosen from a bound on the sums (int32 entries of S with 2^30 of
+//     headroom in FP32, int64 with 2^60 in FP64; int64 vectors); a build whose
+//     column norms exceed the bound it was scaled for runs again with the new
+//     bound;
 //   - the cost pass runs one thread per observation (FP64 residuals from the
 //     window's FP64 poses in shared memory);
 //   - the Schur build runs one warp per point (V, V^-1, g_p, W, W V^-1) and
@@ -26,6 +32,8 @@
 // CTAs never wait on each other, so the launch cannot deadlock; the hardware
 // schedules the next problem onto an SM as soon as one finishes (problems are
 // ordered largest first to shorten the tail).
+#include <math_constants.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -128,8 +136,12 @@ struct Shared {
   T zs[N];  // the camera step in the original parameterisation, z * scale_c
   double scale_c[N];
   double diag_c[N];
-  float scale_cf[N];      // FP32 path: scale_c, and the column norms and
-  float colsq[N], grad[N];  // gradient of the Schur build's Jacobian
+  float scale_cf[N];  // FP32 path: scale_c
+  // FP32 path: fixed-point sums of rhs, column norms and gradient of the
+  // Schur build's Jacobian
+  long long fxv[3][N];
+  double fx[4];    // scales of S, column norms, gradient, rhs
+  double cbound;   // bound on the scaled column norms the scales are chosen for
   double red[kWarps];
   double bcast[8];
   int flag;
@@ -170,6 +182,21 @@ __device__ __forceinline__ double block_max(double v, double* red, double* out) 
   }
   __syncthreads();
   return *out;
+}
+
+// Largest power of two s with bound * s <= 2^bits (1 for a bound that is not
+// a positive finite number), its exponent clamped to [-lim, lim].
+__device__ __forceinline__ double pow2_scale(double bound, int bits, int lim = 1000) {
+  if (!(bound > 0.0) || !isfinite(bound)) return 1.0;
+  int e;
+  frexp(bound, &e);  // bound < 2^e
+  return ldexp(1.0, max(-lim, min(lim, bits - e)));
+}
+__device__ __forceinline__ void fx_add(long long* p, double v, double scale) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double2ll_rn(v * scale));
+}
+__device__ __forceinline__ void fx_add(long long* p, float v, float scale) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__float2ll_rn(v * scale));
 }
 
 // Linearisation of observation o (point p) at the current parameters: the
@@ -266,23 +293,27 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     if constexpr (kGS) __stcg(g_S + i, (double)v);
     else sh.S[i] = v;
   };
+  // Fixed-point accumulation of the Schur build (scales sh.fx, set before
+  // each build): S as int64 in the global slice (FP64) or int32 in shared
+  // memory (FP32); rhs, the column norms (Nadd) and the gradient (Gadd) of
+  // the scaled Jacobian as int64 in the global slice (FP64) or in shared
+  // memory (FP32).
+  float fxf[4] = {1.f, 1.f, 1.f, 1.f};  // the FP32 path's copy of the scales
   auto Sadd = [&](int i, SS v) {
-    if constexpr (kGS) atomicAdd(g_S + i, (double)v);
-    else atomicAdd(&sh.S[i], v);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_S + i), (double)v, sh.fx[0]);
+    else atomicAdd(reinterpret_cast<int*>(&sh.S[i]), __float2int_rn((float)v * fxf[0]));
   };
-  auto Radd = [&](int i, SS v) {
-    if constexpr (kGS) atomicAdd(g_rhs + i, (double)v);
-    else atomicAdd(&sh.rhs[i], v);
-  };
-  // the Schur build's column norms (Nadd) and gradient (Gadd) of the scaled
-  // Jacobian: FP64 in the global slice, FP32 in shared memory
   auto Nadd = [&](int i, T v) {
-    if constexpr (kGS) atomicAdd(g_acc + i, (double)v);
-    else atomicAdd(&sh.colsq[i], (float)v);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_acc + i), (double)v, sh.fx[1]);
+    else fx_add(&sh.fxv[1][i], (float)v, fxf[1]);
   };
   auto Gadd = [&](int i, T v) {
-    if constexpr (kGS) atomicAdd(g_grad + i, (double)v);
-    else atomicAdd(&sh.grad[i], (float)v);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_grad + i), (double)v, sh.fx[2]);
+    else fx_add(&sh.fxv[2][i], (float)v, fxf[2]);
+  };
+  auto Radd = [&](int i, SS v) {
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_rhs + i), (double)v, sh.fx[3]);
+    else fx_add(&sh.fxv[0][i], (float)v, fxf[3]);
   };
 
   const bool use_pose = P.nc <= (uint32_t)kPoseCams;
@@ -409,9 +440,31 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
   // the gradient from its own Jacobian; this pass only runs again to check
   // the gradient of an accepted last step at the iteration limit.
   auto linearize = [&](bool first) -> double {
+    // Column norms and gradient are fixed-point sums (order-independent).
+    // Pass 1 finds the largest single term of each, which with the window's
+    // observation count bounds every partial sum; pass 2 accumulates.
+    double mc = 0.0, mg = 0.0;
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      for (uint32_t o = a.pt_off[p] + lane; o < a.pt_off[p + 1]; o += 32) {
+        T rr[2], Jc[2][B], Jp[2][3];
+        int col[B];
+        obs_lin<M, T>(a, o, p, rc_cur(), rr, Jc, Jp, col);
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+          if (col[j] < 0) continue;
+          const double x0 = Jc[0][j], x1 = Jc[1][j];
+          mc = fmax(mc, x0 * x0 + x1 * x1);
+          mg = fmax(mg, fabs(x0 * (double)rr[0] + x1 * (double)rr[1]));
+        }
+      }
+    }
+    mc = block_max(mc, sh.red, &sh.bcast[5]);
+    mg = block_max(mg, sh.red, &sh.bcast[6]);
+    const double nobs = (double)(a.pt_off[P.x1] - a.pt_off[P.x0]);
+    const double sc = pow2_scale(mc * nobs, 62), sg = pow2_scale(mg * nobs, 62);
     for (int i = tid; i < n; i += kThreads) {
-      __stcg(g_acc + i, 0.0);
-      __stcg(g_grad + i, 0.0);
+      __stcg(reinterpret_cast<long long*>(g_acc + i), 0ll);
+      __stcg(reinterpret_cast<long long*>(g_grad + i), 0ll);
     }
     __syncthreads();
     double gm = 0.0;
@@ -426,8 +479,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
           const double x0 = Jc[0][j], x1 = Jc[1][j];
-          atomicAdd(g_acc + col[j], x0 * x0 + x1 * x1);
-          atomicAdd(g_grad + col[j], x0 * r[0] + x1 * r[1]);
+          fx_add(reinterpret_cast<long long*>(g_acc + col[j]), x0 * x0 + x1 * x1, sc);
+          fx_add(reinterpret_cast<long long*>(g_grad + col[j]), x0 * r[0] + x1 * r[1], sg);
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -450,6 +503,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         }
         gm = fmax(gm, fabs(lane == 0 ? gp3[0] : lane == 1 ? gp3[1] : gp3[2]));
       }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += kThreads) {
+      __stcg(g_acc + i, (double)__ldcg(reinterpret_cast<const long long*>(g_acc + i)) / sc);
+      __stcg(g_grad + i, (double)__ldcg(reinterpret_cast<const long long*>(g_grad + i)) / sg);
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
@@ -485,6 +543,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     return;
   }
   double gmax = linearize(true), xnorm = param_norm();
+  {
+    // bound on the scaled column norms for the first build's fixed-point scale
+    double cb = 0.0;
+    for (int i = tid; i < n; i += kThreads) cb = fmax(cb, __ldcg(g_acc + i) * sh.scale_c[i] * sh.scale_c[i]);
+    cb = block_max(cb, sh.red, &sh.bcast[7]);
+    if (tid == 0) sh.cbound = fmax(cb, 1e-300);
+    __syncthreads();
+  }
   bool check_grad = false;  // an accepted step's gradient is checked by the next Schur build
   int term = gmax <= a.gtol ? GBBA_CONVERGENCE : -1;
   double radius = a.r0, decrease = 2.0;
@@ -496,7 +562,24 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       break;
     }
     // ---- S = sum F'F - sum (F'E) V^-1 (E'F) + diag(D_c^2), rhs, and from
-    // the same Jacobian the column norms (LM diagonal) and the gradient
+    // the same Jacobian the column norms (LM diagonal) and the gradient, in
+    // fixed point scaled for column norms up to 4 cbound (partial sums of S
+    // stay within twice the largest column norm: every term is an entry of a
+    // per-observation U or of a per-point W V^-1 W^T, both bounded by U's
+    // diagonal).  A build that finds larger norms runs again.
+    const double irad_d = 1.0 / radius;
+    T gmt = T(0);  // gradient max norm (unscaled) over this thread's points
+    double cmax = 0.0;
+    for (int attempt = 0;; ++attempt) {
+    if (tid == 0) {
+      const double cb = sh.cbound;
+      const double G = 2.0 * sqrt(4.0 * cb * (2.0 * cost + 1e-300));
+      sh.fx[0] = pow2_scale(8.0 * cb, kGS ? 60 : 30, kGS ? 1000 : 120);
+      sh.fx[1] = pow2_scale(4.0 * cb, 60, kGS ? 1000 : 120);
+      sh.fx[2] = pow2_scale(G, 58, kGS ? 1000 : 120);
+      sh.fx[3] = pow2_scale(4.0 * G, 58, kGS ? 1000 : 120);
+      sh.flag = 0;
+    }
     for (int i = tid; i < n * (n + 1) / 2; i += kThreads) Sst(i, SS(0));
     for (int i = tid; i < n; i += kThreads) {
       if constexpr (kGS) {
@@ -504,13 +587,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         __stcg(g_acc + i, 0.0);
         __stcg(g_grad + i, 0.0);
       } else {
-        sh.rhs[i] = SS(0);
-        sh.colsq[i] = 0.f;
-        sh.grad[i] = 0.f;
+        sh.fxv[0][i] = sh.fxv[1][i] = sh.fxv[2][i] = 0;
       }
     }
-    if (tid == 0) sh.flag = 0;
+    gmt = T(0);
     __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) fxf[q] = (float)sh.fx[q];
     // One intrinsic group per window (the local-BA case): the intrinsic
     // columns are common to every observation, so their terms factor through
     // per-point sums (no observation pairs):
@@ -519,8 +602,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     // and only the 6x6 extrinsic blocks need the observation pairs (one lane
     // per pair; an observation's own pair carries its U_ee).
     const bool one_group = P.ni == 1;
-    const T irad = T(1.0 / radius), dmin = (T)a.dmin, dmax = (T)a.dmax;
-    T gmt = T(0);  // gradient max norm (unscaled) over this thread's points
+    const T irad = T(irad_d), dmin = (T)a.dmin, dmax = (T)a.dmax;
     for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
       const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1], m = oe - ob;
       const T sp[3] = {psc(p, 0), psc(p, 1), psc(p, 2)};
@@ -752,16 +834,50 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       __syncwarp();
     }
     __syncthreads();
+    // the column norms against the bound the build was scaled for
+    {
+      double cm = 0.0;
+      bool sat = false;
+      for (int i = tid; i < n; i += kThreads) {
+        const long long v = kGS ? __ldcg(reinterpret_cast<const long long*>(g_acc + i)) : sh.fxv[1][i];
+        sat |= v >= (1ll << 62) || v < 0;
+        cm = fmax(cm, (double)v / sh.fx[1]);
+      }
+      cmax = block_max(sat ? CUDART_INF : cm, sh.red, &sh.bcast[7]);
+    }
+    if (cmax <= 4.0 * sh.cbound || attempt >= 16) break;
+    __syncthreads();
+    if (tid == 0) sh.cbound = isfinite(cmax) ? cmax : sh.cbound * 65536.0;
+    __syncthreads();
+    }  // build attempts
+    if (cmax > 4.0 * sh.cbound && tid == 0) sh.flag = 4;  // no scale fitted: the step is invalid
+    // back to floating point: S in place, then the next build's bound
+    for (int i = tid; i < n * (n + 1) / 2; i += kThreads) {
+      if constexpr (kGS) __stcg(g_S + i, (double)__ldcg(reinterpret_cast<const long long*>(g_S + i)) / sh.fx[0]);
+      else sh.S[i] = (float)(*reinterpret_cast<const int*>(&sh.S[i])) * (float)(1.0 / sh.fx[0]);
+    }
+    __syncthreads();
+    if (tid == 0 && isfinite(cmax)) sh.cbound = fmax(cmax, 1e-300);
     // LM diagonal D_c^2 = clamp(column norms), rhs = gradient + Schur
     // correction, gradient max norm of this linearisation
     double gm = (double)gmt;
     for (int i = tid; i < n; i += kThreads) {
-      const double acc = kGS ? __ldcg(g_acc + i) : (double)sh.colsq[i];
-      const double gi = kGS ? __ldcg(g_grad + i) : (double)sh.grad[i];
+      long long vr, vn, vg;
+      if constexpr (kGS) {
+        vr = __ldcg(reinterpret_cast<const long long*>(g_rhs + i));
+        vn = __ldcg(reinterpret_cast<const long long*>(g_acc + i));
+        vg = __ldcg(reinterpret_cast<const long long*>(g_grad + i));
+      } else {
+        vr = sh.fxv[0][i];
+        vn = sh.fxv[1][i];
+        vg = sh.fxv[2][i];
+      }
+      const double acc = (double)vn / sh.fx[1];
+      const double gi = (double)vg / sh.fx[2];
       const double d = fmin(fmax(acc, a.dmin), a.dmax);
       sh.diag_c[i] = d;
       Sst(tri(i, i), Sld(tri(i, i)) + (SS)(d / radius));
-      sh.rhs[i] = (SS)(gi + (kGS ? __ldcg(g_rhs + i) : (double)sh.rhs[i]));
+      sh.rhs[i] = (SS)(gi + (double)vr / sh.fx[3]);
       gm = fmax(gm, fabs(gi / sh.scale_c[i]));
     }
     gmax = block_max(gm, sh.red, &sh.bcast[1]);

@@ -157,6 +157,12 @@ struct Prob {
   // mixed path's FP32 Jacobian reads them instead of converting per
   // observation (conversions and FP64 products run on GB300's FP64 pipe).
   const float *ext_f, *intr_f, *pts_f, *scale_cf, *scale_pf;
+  // Residual cache of the mixed path, or null: per observation r sqrt(rho')
+  // and sqrt(rho') from the FP64 cost pass at these parameters (read by the
+  // Schur build instead of a second FP64 residual), and where the cost pass
+  // writes them.
+  const float4* rc;
+  float4* rc_out;
 };
 
 template <int M, typename T>
@@ -184,6 +190,7 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
   for (int i = 0; i < 3; ++i) Xd[i] = __ldg(&P.pts[3 * (int64_t)p + i]);
   T Je[2][6], Jk[2][K], Jx[2][3];
   double r[2];
+  double r_sr1 = -1.0;  // >= 0: r is already corrected and this is sqrt(rho') (residual cache)
   if constexpr (sizeof(T) == 8) {
     double Ed[6];
 #pragma unroll
@@ -191,7 +198,12 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
     residual<M, T, true>(Kd, Ed, Xd, ob.x, ob.y, r, Je, Jk, Jx, (T*)nullptr);
   } else {
     T Ef[6], Kf[K], Xf[3], rf[2];
-    if (P.pose) {
+    if (P.rc) {
+      const float4 q = __ldg(&P.rc[o]);
+      r[0] = q.x;
+      r[1] = q.y;
+      r_sr1 = q.z;
+    } else if (P.pose) {
       residual_pose<M, double>(Kd, P.pose + 12 * (int64_t)c, Xd, ob.x, ob.y, r);
     } else {
       double Ed[6], dJe[2][6], dJk[2][K], dJx[2][3];
@@ -217,9 +229,16 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
     residual<M, T, true>(Kf, Ef, Xf, (T)ob.x, (T)ob.y, rf, Je, Jk, Jx, (T*)nullptr);
   }
   double sr1;
-  *cost = robust<double>(P.loss_type, P.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
-  J.r[0] = r[0] * sr1;
-  J.r[1] = r[1] * sr1;
+  if (r_sr1 >= 0.0) {
+    sr1 = r_sr1;
+    *cost = 0.0;  // not evaluated: the cost pass has it
+    J.r[0] = r[0];
+    J.r[1] = r[1];
+  } else {
+    *cost = robust<double>(P.loss_type, P.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
+    J.r[0] = r[0] * sr1;
+    J.r[1] = r[1] * sr1;
+  }
   const T s = (T)sr1;
 #pragma unroll
   for (int j = 0; j < 6; ++j) J.col[j] = __ldg(&P.ext_col[6 * (int64_t)c + j]);
@@ -1062,8 +1081,10 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
 // blocks of S (ceres SCHUR_JACOBI, internal/ceres/schur_jacobi_preconditioner.cc;
 // implicit products as in internal/ceres/implicit_schur_complement.cc:69-110):
 //   S p = (U + D_c^2) p - sum_o W_o V_p(o)^-1 W_o^T p
-// The operator data (W, V^-1, U) are in the compute type T, the PCG vectors
-// and every accumulation are FP64.
+// The operator data (W, V^-1, U) are in the compute type T and the PCG
+// vectors in FP64.  The FP64 path accumulates in FP64; the mixed path forms
+// the per-observation products and their sums in FP32 (Kahan-compensated
+// where a camera sums thousands of them) and widens the per-camera sums.
 
 // Scalars of the device-resident CG loop (see k_pcg_direction and the other
 // k_pcg_* kernels below).
@@ -1076,6 +1097,15 @@ struct PcgState {
   int failure;    // LINEAR_SOLVER_FAILURE (rho, beta or alpha not usable)
   int pad;
 };
+
+// Kahan (compensated) summation: s + v with the lost low part kept in c;
+// the sum is s - c.
+__device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
 
 // Camera diagonal blocks U_c = sum Jc^T Jc, the preconditioner block
 // (U_c + D_c^2 - sum (W V^-1) W^T)^-1 (identity on held coordinates); one warp per camera.
@@ -1096,18 +1126,47 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
   double accU[E], accS[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) accU[e] = accS[e] = 0.0;
-  for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
-    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+  if constexpr (sizeof(T) == 4) {
+    // FP32 products and Kahan-compensated FP32 sums (GB300 runs FP64 at a
+    // small fraction of the FP32 rate; a camera sums thousands of terms)
+    float su[E], cu[E], ss[E], cs[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e) su[e] = cu[e] = ss[e] = cs[e] = 0.0f;
+    for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
+      const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int idx = lane + 32 * e;
+        if (idx < B * B) {
+          const int i = idx / B, j = idx % B;
+          const float u = r[R::kJc + i] * r[R::kJc + j] + r[R::kJc + B + i] * r[R::kJc + B + j];
+          const float w = r[R::kWh + 3 * i] * r[R::kW + 3 * j] + r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
+                          r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
+          kahan_add(su[e], cu[e], u);
+          kahan_add(ss[e], cs[e], u - w);
+        }
+      }
+    }
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int idx = lane + 32 * e;
-      if (idx < B * B) {
-        const int i = idx / B, j = idx % B;
-        const double u = (double)r[R::kJc + i] * r[R::kJc + j] + (double)r[R::kJc + B + i] * r[R::kJc + B + j];
-        const double w = (double)r[R::kWh + 3 * i] * r[R::kW + 3 * j] + (double)r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
-                         (double)r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
-        accU[e] += u;
-        accS[e] += u - w;
+      accU[e] = (double)su[e] - (double)cu[e];
+      accS[e] = (double)ss[e] - (double)cs[e];
+    }
+  } else {
+    for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
+      const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int idx = lane + 32 * e;
+        if (idx < B * B) {
+          const int i = idx / B, j = idx % B;
+          const double u = (double)r[R::kJc + i] * r[R::kJc + j] + (double)r[R::kJc + B + i] * r[R::kJc + B + j];
+          const double w = (double)r[R::kWh + 3 * i] * r[R::kW + 3 * j] +
+                           (double)r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
+                           (double)r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
+          accU[e] += u;
+          accS[e] += u - w;
+        }
       }
     }
   }
@@ -1171,12 +1230,38 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
                                                     const int32_t* __restrict__ intr_col,
                                                     const int32_t* __restrict__ cam_group, int K, int64_t np,
                                                     const double* __restrict__ x, double* __restrict__ y,
+                                                    const float* __restrict__ xf, float* __restrict__ yf,
                                                     const PcgState* __restrict__ ps, int reset_period) {
   using R = Rec<B>;
   const int lane = threadIdx.x & 31;
   const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
   if (p >= np) return;
+  if constexpr (sizeof(T) == 4) {
+    // FP32 operand copy in, FP32 products and sums (a point has few
+    // observations), FP32 point temporaries out
+    float t[3] = {0.0f, 0.0f, 0.0f};
+    for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
+      const T* r = rec + (int64_t)o * R::kSize;
+      const uint32_t c = cam[o];
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
+        if (ci < 0) continue;
+        const float xi = xf[ci];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] += r[R::kW + 3 * i + j] * xi;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+    if (lane < 3) {
+      const T* v = Vinv + 6 * p;
+      const float row[3][3] = {{v[0], v[1], v[2]}, {v[1], v[3], v[4]}, {v[2], v[4], v[5]}};
+      yf[3 * p + lane] = row[lane][0] * t[0] + row[lane][1] * t[1] + row[lane][2] * t[2];
+    }
+    return;
+  }
   double t[3] = {0.0, 0.0, 0.0};
   for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
     const T* r = rec + (int64_t)o * R::kSize;
@@ -1211,9 +1296,9 @@ __global__ void __launch_bounds__(128) k_spmv_camera(const uint32_t* __restrict_
                                                      const int32_t* __restrict__ cam_group, int K, int64_t nc,
                                                      const double* __restrict__ diag_c,
                                                      const double* __restrict__ radius, const double* __restrict__ x,
-                                                     const double* __restrict__ y, double* __restrict__ out,
-                                                     double* __restrict__ part, const PcgState* __restrict__ ps,
-                                                     int reset_period) {
+                                                     const double* __restrict__ y, const float* __restrict__ yf,
+                                                     double* __restrict__ out, double* __restrict__ part,
+                                                     const PcgState* __restrict__ ps, int reset_period) {
   using R = Rec<B>;
   __shared__ double pdot[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1224,14 +1309,33 @@ __global__ void __launch_bounds__(128) k_spmv_camera(const uint32_t* __restrict_
     double acc[B];
 #pragma unroll
     for (int i = 0; i < B; ++i) acc[i] = 0.0;
-    for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
-      const uint32_t o = cam_obs[q];
-      const T* r = rec + (int64_t)o * R::kSize;
-      const double* yp = y + 3 * (int64_t)pt[o];
-      const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
+    if constexpr (sizeof(T) == 4) {
+      // FP32 products, Kahan-compensated FP32 sums per lane (a camera has
+      // thousands of observations), FP64 from the lane sums on
+      float sa[B], ca[B];
 #pragma unroll
-      for (int i = 0; i < B; ++i)
-        acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
+      for (int i = 0; i < B; ++i) sa[i] = ca[i] = 0.0f;
+      for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+        const uint32_t o = cam_obs[q];
+        const T* r = rec + (int64_t)o * R::kSize;
+        const float* yp = yf + 3 * (int64_t)pt[o];
+        const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+          kahan_add(sa[i], ca[i], -(r[R::kW + 3 * i] * y0 + r[R::kW + 3 * i + 1] * y1 + r[R::kW + 3 * i + 2] * y2));
+      }
+#pragma unroll
+      for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
+    } else {
+      for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
+        const uint32_t o = cam_obs[q];
+        const T* r = rec + (int64_t)o * R::kSize;
+        const double* yp = y + 3 * (int64_t)pt[o];
+        const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
+#pragma unroll
+        for (int i = 0; i < B; ++i)
+          acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
+      }
     }
 #pragma unroll
     for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
@@ -1281,6 +1385,15 @@ __device__ __forceinline__ double sum_partials(const double* __restrict__ part, 
   double v = 0.0;
   for (int i = threadIdx.x; i < n; i += 256) v += part[i];
   return block_sum256(v, sh);
+}
+
+// FP32 copy of the operand of an implicit product (mixed path); a no-op on
+// the iterations where that product does not run.
+__global__ void __launch_bounds__(256) k_pcg_to_float(const double* __restrict__ x, float* __restrict__ xf, int64_t n,
+                                                      const PcgState* __restrict__ ps, int reset_period) {
+  if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    xf[i] = (float)x[i];
 }
 
 // b = rhs (widened), x = 0, r = b; partials of |b|^2.
@@ -1820,6 +1933,7 @@ __global__ void __launch_bounds__(256) k_cost(Prob P, const double* ext, const d
     double sr1;
     const double cst = robust<double>(P.loss_type, P.loss_a, r[0] * r[0] + r[1] * r[1], &sr1);
     if (!isfinite(cst)) atomicExch(nonfinite, 1);
+    if (P.rc_out) P.rc_out[o] = make_float4((float)(r[0] * sr1), (float)(r[1] * sr1), (float)sr1, 0.0f);
     acc += cst;
   }
   acc = warp_sum(acc);
@@ -1892,6 +2006,8 @@ struct Solve {
   double *ext, *intr, *pts, *ext2, *intr2, *pts2;
   double *pose = nullptr, *pose2 = nullptr;  // FP64 poses of ext / ext2 (mixed path)
   float *ext_f = nullptr, *intr_f = nullptr, *pts_f = nullptr;  // FP32 copies of ext, intr, pts (mixed path)
+  float4* rcache = nullptr;  // mixed path: residual cache, [2][no] (current parameters, candidate)
+  float *pcg_xf = nullptr, *pcg_yf = nullptr;  // mixed path: FP32 copies of the PCG operand and point temporaries
   float *scale_cf = nullptr, *scale_pf = nullptr;               // FP32 copies of the Jacobi scales
   uint32_t *pt_grp = nullptr, *pgrp_cnt = nullptr, *pgrp_off = nullptr;  // point groups (k_pt_groups)
   int64_t n_pgrp = 0;
@@ -1953,6 +2069,8 @@ static Prob make_prob(const Solve& s, const double* ext, const double* intr, con
   P.loss_a = o ? o->loss_scale : 1.0;
   P.pose = nullptr;
   P.ext_f = P.intr_f = P.pts_f = P.scale_cf = P.scale_pf = nullptr;
+  P.rc = nullptr;
+  P.rc_out = nullptr;
   return P;
 }
 
@@ -1970,6 +2088,8 @@ static void carve(A& a, Solve& s, size_t tsize) {
   s.pts_f = a.template take<float>(3 * s.np);
   s.scale_cf = a.template take<float>(s.n_red + 1);
   s.scale_pf = a.template take<float>(3 * s.np);
+  s.rcache = a.template take<float4>(tsize == 4 ? 2 * s.no : 0);
+  if (tsize != 4) s.rcache = nullptr;
   s.intr2 = a.template take<double>(s.k * s.ni);
   s.pts2 = a.template take<double>(3 * s.np);
   s.obs = a.template take<double2>(s.no);
@@ -2222,6 +2342,8 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     // PCG vectors (x, r, z, p, q, b), point temporaries, camera blocks
     p1.take<double>(6 * n_pcg);
     p1.take<double>(3 * np);
+    p1.take<float>(tsize == 4 && n_pcg ? n_pcg : 0);
+    p1.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
     p1.take<double>((size_t)nc * B * B);
     p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
     p1.take<double>(2 * std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1));  // PCG partial sums
@@ -2252,6 +2374,9 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     s.pcg_q = A.take<double>(n_pcg);
     s.pcg_b = A.take<double>(n_pcg);
     s.pcg_y = A.take<double>(3 * np);
+    s.pcg_xf = A.take<float>(tsize == 4 && n_pcg ? n_pcg : 0);
+    s.pcg_yf = A.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
+    if (!(tsize == 4 && n_pcg)) s.pcg_xf = s.pcg_yf = nullptr;
     s.pcg_minv = A.take<double>((size_t)nc * B * B);
     s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
     s.pcg_part_n = std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1);
@@ -2412,14 +2537,18 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   check_launch(h);
   auto spmv = [&](const double* x, double* out, double* part, int reset) {
     if (s.np > 0) {
+      if constexpr (sizeof(T) == 4) {
+        k_pcg_to_float<<<nbv, 256, 0, st>>>(x, s.pcg_xf, n, ps, reset);
+        check_launch(h);
+      }
       k_spmv_point<B, T><<<(unsigned)ceil_div(s.np * 32, 128), 128, 0, st>>>(
           s.pt_off, s.cam, (const T*)s.rec, (const T*)s.Vinv, s.ext_col, s.intr_col, s.cam_group, s.k, s.np, x, s.pcg_y,
-          ps, reset);
+          s.pcg_xf, s.pcg_yf, ps, reset);
       check_launch(h);
     }
     k_spmv_camera<B, T><<<(unsigned)nbs, 128, 0, st>>>(
         s.cam_off, s.cam_obs, s.pt, (const T*)s.rec, (const T*)s.pcg_u, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc,
-        s.diag_c, s.radius, x, s.pcg_y, out, part, ps, reset);
+        s.diag_c, s.radius, x, s.pcg_y, s.pcg_yf, out, part, ps, reset);
     check_launch(h);
   };
   auto iteration = [&]() {
@@ -2507,6 +2636,9 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
   };
   auto launch_cost = [&](const double* e, const double* i, const double* p) {
     Prob Pc = make_prob(s, e, i, p, o);
+    // the mixed path's residual cache: current parameters in slot 0, the
+    // candidate in slot 1 (copied to slot 0 when the step is accepted)
+    if (kPose && s.rcache) Pc.rc_out = s.rcache + (e == s.ext ? 0 : s.no);
     if (kPose && s.nc > 0) {
       k_cam_pose<<<nb_cam_pose, 128, 0, st>>>(e, s.nc, s.pose2);
       check_launch(h);
@@ -2646,6 +2778,7 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     P.pts_f = s.pts_f;
     P.scale_cf = s.scale_cf;
     P.scale_pf = s.scale_pf;
+    P.rc = s.rcache;  // residuals of the current parameters from the last cost pass
   }
   const int nb_back = s.pair_path ? s.nb_pgrp : s.nb_pt;  // blocks (partials) of the back substitution
   auto record_phase = [&](int ph) {
@@ -2864,6 +2997,8 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       GBBA_CUDA(cudaMemcpyAsync(s.ext, s.ext2, sizeof(double) * n_e, cudaMemcpyDeviceToDevice, st));
       GBBA_CUDA(cudaMemcpyAsync(s.intr, s.intr2, sizeof(double) * n_i, cudaMemcpyDeviceToDevice, st));
       GBBA_CUDA(cudaMemcpyAsync(s.pts, s.pts2, sizeof(double) * 3 * s.np, cudaMemcpyDeviceToDevice, st));
+      if (kPose && s.rcache)
+        GBBA_CUDA(cudaMemcpyAsync(s.rcache, s.rcache + s.no, sizeof(float4) * s.no, cudaMemcpyDeviceToDevice, st));
       if (fused) {
         refresh();
         need_grad = true;

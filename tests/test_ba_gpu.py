@@ -439,12 +439,8 @@ def test_batched_mixed_reaches_fp64_cost(handle, abi, scenes):
     """Mixed-precision windows reach the FP64 minimum within 1e-6.  Some local
     windows have flat valleys in which ceres's default stopping rule
     (|dcost| <= 1e-6 cost) stops up to a few 1e-6 above the minimum, so the
-    FP64 reference here is run with a tight function tolerance.  The FP32
-    Schur sums of a window are accumulated with shared-memory atomics, whose
-    order varies from run to run; on weakly constrained windows (200-600
-    points for up to 40 cameras) that occasionally led the mixed solve to a
-    different local minimum, so the windows here carry 400-1,200 points."""
-    probs = local_problems(scenes, 16, seed=112, cams=(5, 40), points=(400, 1200))
+    FP64 reference here is run with a tight function tolerance."""
+    probs = local_problems(scenes, 16, seed=112, cams=(5, 40), points=(200, 600))
     o64 = abi.default_options(max_num_iterations=300, function_tolerance=1e-12)
     o32 = abi.default_options(max_num_iterations=100, precision=abi.PRECISION_MIXED)
     st, b32, _ = batched_solve(handle, abi, probs, o32)
@@ -452,6 +448,27 @@ def test_batched_mixed_reaches_fp64_cost(handle, abi, scenes):
     for p, s in zip(probs, b32):
         si, _ = solve(handle, abi, p, o64)
         assert s.usable and s.final_cost <= si.final_cost * (1 + 1e-6), (s.final_cost, si.final_cost)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_solves_are_bitwise_repeatable(handle, abi, scenes, precision):
+    """The Schur build's sums are fixed-point integer sums, so the order in
+    which warps reach an entry cannot change them: repeated launches give the
+    same parameters, costs and iteration counts bit for bit."""
+    probs = local_problems(scenes, 24, seed=115, cams=(5, 40), points=(200, 1200))
+    opts = abi.default_options(max_num_iterations=30)
+    if precision == "mixed":
+        opts = abi.default_options(max_num_iterations=30, precision=abi.PRECISION_MIXED)
+    runs = [batched_solve(handle, abi, probs, opts) for _ in range(3)]
+    for st, _, _ in runs:
+        assert st == abi.SUCCESS
+    _, s0, p0 = runs[0]
+    for _, s1, p1 in runs[1:]:
+        for a, b in zip(s0, s1):
+            assert a.final_cost == b.final_cost and a.num_iterations == b.num_iterations
+        for a, b in zip(p0, p1):
+            for k in ("extrinsics", "intrinsics", "points"):
+                np.testing.assert_array_equal(a[k], b[k])
 
 
 def test_batched_rejects_oversized_window(handle, abi, scenes):
