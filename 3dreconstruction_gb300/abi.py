@@ -107,7 +107,7 @@ class GbbaOptions(C.Structure):
         ("trace_cost", C.c_void_p),
         ("trace_time_s", C.c_void_p),
         ("trace_capacity", C.c_int32),
-        ("trace_reserved", C.c_int32),
+        ("mixed_flags", C.c_uint32),
     ]
 
 
@@ -161,6 +161,7 @@ class GbsfmResidualStats(C.Structure):
 
 
 LOCK_AS_REFERENCE, LOCK_FIRST_ADDED, LOCK_NONE = 0, 1, 2
+MIXED_KAHAN_SCHUR, MIXED_FP64_POINT_INVERSE = 1, 2
 
 
 class GbsfmAcransacParams(C.Structure):

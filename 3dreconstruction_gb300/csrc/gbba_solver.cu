@@ -449,12 +449,15 @@ struct Rec {
 // triangle of V (00 01 02 11 12 22).  Returns false on a non-positive pivot
 // or a non-finite inverse.
 template <typename T>
-__device__ __forceinline__ bool point_vinv(const T v[6], const double* __restrict__ dp, double rad, T vi[6]) {
+__device__ __forceinline__ bool point_vinv(const T v[6], const double* __restrict__ dp, double rad, T vi[6],
+                                           T* pivot_ratio = nullptr) {
   const T a00 = v[0] + (T)(dp[0] / rad), a11 = v[3] + (T)(dp[1] / rad), a22 = v[5] + (T)(dp[2] / rad);
   const T l00 = sqrt(a00), l10 = v[1] / l00, l20 = v[2] / l00;
   const T d1 = a11 - l10 * l10;
   const T l11 = sqrt(d1), l21 = (v[4] - l20 * l10) / l11;
   const T d2 = a22 - l20 * l20 - l21 * l21;
+  // smallest over largest squared pivot: a lower bound of 1 / cond(V)
+  if (pivot_ratio) *pivot_ratio = fmin(a00, fmin(d1, d2)) / fmax(a00, fmax(d1, d2));
   const T l22 = sqrt(d2);
   const T i00 = T(1) / l00, i11 = T(1) / l11, i22 = T(1) / l22;
   const T i10 = -l10 * i00 * i11, i21 = -l21 * i11 * i22, i20 = -(l20 * i00 + l21 * i10) * i22;
@@ -527,7 +530,7 @@ __device__ __forceinline__ void gmax_update(unsigned long long* shards, double m
               (unsigned long long)__double_as_longlong(m));
 }
 
-template <int M, typename T>
+template <int M, typename T, bool kFp64Inverse = false>
 __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                          const double* __restrict__ scale_c,
                                                          const double* __restrict__ scale_p,
@@ -588,8 +591,39 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     if (!valid) return;
     const double dp[3] = {fmin(fmax((double)v[0], dmin), dmax), fmin(fmax((double)v[3], dmin), dmax),
                           fmin(fmax((double)v[5], dmin), dmax)};
-    T vi[6];
-    const bool ok = point_vinv<T>(v, dp, rad, vi);
+    T vi[6], pr = T(1);
+    bool ok = point_vinv<T>(v, dp, rad, vi, &pr);
+    if constexpr (sizeof(T) == 4 && kFp64Inverse) {
+      // FP32 pivots spanning more than 1e4: V again from an FP64 Jacobian,
+      // summed and inverted in FP64 (the point's lanes; the warp's scan)
+      const bool bad = valid && ok && !(pr >= T(1e-4));
+      if (__any_sync(0xffffffffu, bad)) {
+        double v64[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (bad) {
+          ObsJac<M, double> J64;
+          double c64, g64[3];
+          obs_jacobian<M, double, true>(P, o, scale_c, scale_p, J64, &c64);
+          point_terms<M, double>(J64, v64, g64);
+        }
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+          const bool take = lane - d >= head;
+#pragma unroll
+          for (int i = 0; i < 6; ++i) {
+            const double y = __shfl_up_sync(0xffffffffu, v64[i], d);
+            if (take) v64[i] += y;
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 6; ++i) v64[i] = __shfl_sync(0xffffffffu, v64[i], tail);
+        if (bad) {
+          double vi64[6];
+          ok = point_vinv<double>(v64, dp, rad, vi64);
+#pragma unroll
+          for (int i = 0; i < 6; ++i) vi[i] = (T)vi64[i];
+        }
+      }
+    }
     if (lane == head) {
       if (!ok) atomicExch(flag, 2);
 #pragma unroll
@@ -805,7 +839,7 @@ __device__ __forceinline__ void lds12(const T* p, T v[12]) {
   for (int q = 0; q < 3; ++q) ld4<T>(p + 4 * q, v + 4 * q);
 }
 
-template <int B, typename T>
+template <int B, typename T, bool kKahan = false>
 __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict__ items, int64_t nitems,
                                                      const unsigned long long* __restrict__ pairs,
                                                      const T* __restrict__ rec, const int32_t* __restrict__ ext_col,
@@ -853,11 +887,21 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
   const int grp = lane / PT::LPG, t = lane % PT::LPG;
   const bool active = grp < PT::G && t < PT::NT;
   const int ti = active ? t / PT::TPD : 0, tj = active ? t % PT::TPD : 0;
-  T acc[3][3];
+  T acc[3][3], cmp[3][3];  // cmp: Kahan compensation (kKahan)
 #pragma unroll
   for (int r = 0; r < 3; ++r)
 #pragma unroll
-    for (int c = 0; c < 3; ++c) acc[r][c] = T(0);
+    for (int c = 0; c < 3; ++c) acc[r][c] = cmp[r][c] = T(0);
+  auto add = [&](int r, int c, T v) {
+    if constexpr (kKahan) {
+      const T y = v - cmp[r][c];
+      const T t = acc[r][c] + y;
+      cmp[r][c] = (t - acc[r][c]) - y;
+      acc[r][c] = t;
+    } else {
+      acc[r][c] += v;
+    }
+  };
   // The item's pair list (at most kPairChunk = 128 entries) is loaded once,
   // four per lane; pair q of the item is then a shuffle away.
   static_assert(kPairChunk <= 128, "pair list held in four registers per lane");
@@ -928,7 +972,7 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
         for (int r = 0; r < 3; ++r)
 #pragma unroll
           for (int c = 0; c < 3; ++c)
-            acc[r][c] -= A[3 * r] * Bv[3 * c] + A[3 * r + 1] * Bv[3 * c + 1] + A[3 * r + 2] * Bv[3 * c + 2];
+            add(r, c, -(A[3 * r] * Bv[3 * c] + A[3 * r + 1] * Bv[3 * c + 1] + A[3 * r + 2] * Bv[3 * c + 2]));
         if (same_bits & (1u << q)) {
           T ja0[4], ja1[4], jb0[4], jb1[4];
           ld4<T>(sp + 2 * PT::WSZ + ti * 4, ja0);
@@ -938,10 +982,16 @@ __global__ void __launch_bounds__(128) k_schur_pairs(const PairItem* __restrict_
 #pragma unroll
           for (int r = 0; r < 3; ++r)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) acc[r][c] += ja0[r] * jb0[c] + ja1[r] * jb1[c];
+            for (int c = 0; c < 3; ++c) add(r, c, ja0[r] * jb0[c] + ja1[r] * jb1[c]);
         }
       }
     }
+  }
+  if constexpr (kKahan) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[r][c] -= cmp[r][c];
   }
   if (PT::G == 2) {
 #pragma unroll
@@ -2797,14 +2847,24 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       case 1:
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
-          k_schur_point_rec<M, T><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
-              P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
-              gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+          if (kPose && (o->mixed_flags & GBBA_MIXED_FP64_POINT_INVERSE))
+            k_schur_point_rec<M, T, true><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
+                P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
+                gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+          else
+            k_schur_point_rec<M, T><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
+                P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
+                gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
           check_launch(h);
           if (s.dense && s.n_blocks > 0) {
-            k_schur_pairs<B, T><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
-                (const PairItem*)s.pair_items, s.n_blocks, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col,
-                s.cam_group, s.k, s.nc, S, s.n_pad, (T*)s.pair_partial);
+            if (kPose && (o->mixed_flags & GBBA_MIXED_KAHAN_SCHUR))
+              k_schur_pairs<B, T, true><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
+                  (const PairItem*)s.pair_items, s.n_blocks, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col,
+                  s.cam_group, s.k, s.nc, S, s.n_pad, (T*)s.pair_partial);
+            else
+              k_schur_pairs<B, T><<<(unsigned)ceil_div(s.n_blocks * 32, 128), 128, 0, st>>>(
+                  (const PairItem*)s.pair_items, s.n_blocks, s.pairs, (const T*)s.rec, s.ext_col, s.intr_col,
+                  s.cam_group, s.k, s.nc, S, s.n_pad, (T*)s.pair_partial);
             check_launch(h);
             if (s.n_merges > 0) {
               k_pair_merge<B, T><<<(unsigned)ceil_div(s.n_merges * 32, 128), 128, 0, st>>>(

@@ -533,3 +533,48 @@ def resection_scene(num_points=600, seed=13, outlier_frac=0.3, sigma=0.5, width=
     out = rng.random(num_points) < outlier_frac
     x[out] = rng.uniform([0, 0], [width, height], (out.sum(), 2))
     return {"x2d": x, "x3d": X, "K": K, "width": width, "height": height, "outlier": out.astype(np.uint8)}
+
+
+def illconditioned_scene(num_cameras=24, num_points=3000, seed=17, baseline=0.01, radius=10.0, extent=2.0,
+                         sigma=0.5, pair_frac=0.4, huber=4.0):
+    """A scene whose point blocks are ill-conditioned: cameras come in twins
+    `baseline` apart on a ring of radius 10, and a share of the points is
+    seen by one twin pair only (rays meeting at ~0.06 degrees, so V's depth
+    direction is ~1e6 times weaker than the others); the other points are
+    seen by 3-8 cameras around the ring.  Per-camera radial K3 with the
+    intrinsics held, Huber loss, cameras 0 and 1 held."""
+    rng = np.random.default_rng(seed)
+    half = num_cameras // 2
+    theta = np.arange(half) * 2 * math.pi / half
+    base = radius * np.stack([np.sin(theta), np.zeros_like(theta), np.cos(theta)], -1)
+    tang = np.stack([np.cos(theta), np.zeros_like(theta), -np.sin(theta)], -1)
+    centers = np.concatenate([base, base + baseline * tang])
+    R, t = _cameras_facing_origin(centers)
+    ext_true = np.concatenate([rotation_to_angle_axis(R), t], 1)
+    intr = np.zeros((num_cameras, 6))
+    intr[:, 0] = 1000.0
+    intr[:, 1], intr[:, 2] = PP
+    X_true = rng.uniform(-extent, extent, size=(num_points, 3))
+    pairs = rng.random(num_points) < pair_frac
+    cams, pts = [], []
+    for p in range(num_points):
+        if pairs[p]:
+            k = int(rng.integers(0, half))
+            c = np.array([k, half + k])
+        else:
+            c = np.sort(rng.choice(num_cameras, int(rng.integers(3, 9)), replace=False))
+        cams.append(c)
+        pts.append(np.full(len(c), p))
+    cam = np.concatenate(cams)
+    pt = np.concatenate(pts)
+    intr_idx = cam.copy()
+    obs, _, _ = _observe(rng, abi.RADIAL_K3, ext_true, intr, X_true, cam, intr_idx, pt, sigma)
+    ext, X = _perturb(rng, ext_true.copy(), X_true, 0.002, 0.01, 0.02, fixed_cams=(0, 1))
+    cam_const = np.zeros(num_cameras, np.uint8)
+    cam_const[[0, 1]] = 1
+    sc = _scene_dict(abi.RADIAL_K3, ext, intr, X, obs, cam, intr_idx, pt, camera_constant=cam_const,
+                     intrinsic_constant=np.ones(num_cameras, np.uint8),
+                     truth={"extrinsics": ext_true, "points": X_true, "intrinsics": intr.copy()},
+                     name="illconditioned", seed=seed)
+    sc["loss_scale"] = huber
+    return sc

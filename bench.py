@@ -766,7 +766,7 @@ def run_ours(args):
         line["pack"] = measure_pack(h, torch, args.steps, args.warmup, peak)
         line["acransac"] = measure_acransac(h, torch, args.steps, args.warmup)
     if rank == 0 and args.large:
-        line["large"] = measure_large(h, abi)
+        line["large"] = measure_large(h, abi, args.large_iters)
     if rank == 0 and args.batched_windows > 0:
         line["batched"] = measure_batched(h, abi, args.batched_windows)
     if rank == 0 and args.cpu_baseline:
@@ -788,6 +788,7 @@ def main():
     ap.add_argument("--workload", default="medium")
     ap.add_argument("--iters", type=int, default=20, help="LM iterations per step")
     ap.add_argument("--ttc-iters", type=int, default=200)
+    ap.add_argument("--large-iters", type=int, default=100, help="LM iterations of each large-workload solve")
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")

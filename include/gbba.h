@@ -126,6 +126,17 @@ typedef struct gbba_problem {
                                     (ceres::SubsetParameterization, :1396-1409) */
 } gbba_problem;
 
+/* Extra precision safeguards of the mixed path (options.mixed_flags). */
+typedef enum gbba_mixed_flags {
+  /* Kahan-compensated FP32 sums of the camera-pair blocks of S (the Schur
+   * complement's cancellation: U - W V^-1 W^T) */
+  GBBA_MIXED_KAHAN_SCHUR = 1,
+  /* point blocks V whose FP32 Cholesky pivots span more than 1e4 (condition
+   * above ~1e4: near-parallel rays, short baselines) are summed and inverted
+   * again in FP64 from an FP64 Jacobian */
+  GBBA_MIXED_FP64_POINT_INVERSE = 2
+} gbba_mixed_flags;
+
 typedef struct gbba_options {
   /* ceres::Solver::Options names and defaults (include/ceres/solver.h:81-129) */
   int32_t max_num_iterations;             /* 50 */
@@ -165,7 +176,7 @@ typedef struct gbba_options {
   double* trace_cost;
   double* trace_time_s;
   int32_t trace_capacity;
-  int32_t trace_reserved;
+  uint32_t mixed_flags;                   /* gbba_mixed_flags of the mixed path: 0 */
 } gbba_options;
 
 typedef struct gbba_summary {

@@ -161,6 +161,15 @@ def sfm_scans(tmp):
          **{"ref_hist_" + k: v for k, v in h.items()})
 
 
+def ba_illconditioned(tmp):
+    """A scene with ill-conditioned point blocks (twin cameras 0.01 apart,
+    40% of the points seen by one twin pair only), solved by ceres to a tight
+    tolerance: the minimum the mixed path's precision safeguards must reach."""
+    sc = scenes.illconditioned_scene()
+    ba_case(tmp, "illconditioned", sc, max_num_iterations=100, function_tolerance=1e-12,
+            loss_type=abi.LOSS_HUBER, loss_scale=4.0)
+
+
 def sfm_pack(tmp):
     """The engine's BA assembly and write-back from its own std::map state,
     with ceres's rotation conversions."""
@@ -184,6 +193,7 @@ def sfm_acransac(tmp):
 
 
 GENERATORS = {
+    "ba_illconditioned": ba_illconditioned,
     "sfm_acransac": sfm_acransac,
     "sfm_pack": sfm_pack,
     "sfm_scans": sfm_scans,
@@ -252,6 +262,7 @@ def main():
     sfm_scans(tmp)
     sfm_pack(tmp)
     sfm_acransac(tmp)
+    ba_illconditioned(tmp)
 
 
 if __name__ == "__main__":

@@ -27,10 +27,10 @@ def scene_from(g):
     return sc
 
 
-# ceres SPARSE_SCHUR solves (ba_iterative_* are ceres ITERATIVE_SCHUR runs,
-# compared separately)
+# ceres SPARSE_SCHUR solves (ba_iterative_* are ceres ITERATIVE_SCHUR runs and
+# ba_illconditioned a tight-tolerance run, compared separately)
 BA_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "ba_*.npz"))
-                  if not os.path.basename(p).startswith("ba_iterative"))
+                  if not os.path.basename(p).startswith(("ba_iterative", "ba_illconditioned")))
 EVAL_CASES = sorted(os.path.basename(p) for p in glob.glob(os.path.join(GOLDEN, "eval_*.npz")))
 
 
@@ -151,3 +151,22 @@ def test_reference_unit_test_assertions_hold_for_oracle(oracle_mod):
         assert np.abs(rep - xy.reshape(6, 5, 2)).max() < 1e-9
     X, err = oracle_mod.tri_nview(2, P.reshape(-1, 12), off, cam, xy)
     assert err.max() < 1e-9
+
+
+def illconditioned_options(abi):
+    """The options the ill-conditioned fixture was solved with: ceres to a
+    tight function tolerance (1e-12), at most 100 iterations, Huber(4)."""
+    return abi.default_options(max_num_iterations=100, function_tolerance=1e-12, loss_type=abi.LOSS_HUBER,
+                               loss_scale=4.0)
+
+
+def test_oracle_illconditioned_reaches_ceres_minimum(abi, oracle_mod):
+    """Twin cameras 0.01 apart, 40% of the points seen by one twin pair only:
+    the FP64 restatement reaches ceres's minimum (both stop on the iteration
+    limit or the tolerance near it)."""
+    g = load_golden("ba_illconditioned.npz")
+    st, s, _, _ = oracle_mod.ba_solve(scene_from(g), illconditioned_options(abi))
+    ref = float(g["ref_final_cost"][0])
+    assert st == 0 and s["usable"]
+    assert abs(s["initial_cost"] - g["ref_initial_cost"][0]) <= 1e-12 * g["ref_initial_cost"][0]
+    assert abs(s["final_cost"] - ref) <= 1e-9 * ref, (s["final_cost"], ref)
