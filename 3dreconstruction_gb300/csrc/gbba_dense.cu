@@ -747,7 +747,10 @@ void dense_cholesky_solve_impl(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, 
 
 template <typename T>
 void dense_cholesky_solve(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, T* Linv_all, int* flag, cudaStream_t st) {
-  dense_cholesky_solve_impl<T, std::is_same<T, float>::value>(h, S, n_pad, b, x, Linv_all, flag, st);
+  if (std::is_same<T, float>::value && h->factor_tensor)
+    dense_cholesky_solve_impl<T, std::is_same<T, float>::value>(h, S, n_pad, b, x, Linv_all, flag, st);
+  else
+    dense_cholesky_solve_impl<T, false>(h, S, n_pad, b, x, Linv_all, flag, st);
 }
 
 template void dense_cholesky_solve_impl<float, false>(gbba_handle*, float*, int64_t, float*, float*, float*, int*,

@@ -121,6 +121,11 @@ struct gbba_handle {
   int prio_hi = 0;
   // observation pairs per work item of the camera-pair products (gbba_autotune)
   int pair_chunk = 128;
+  // FP32 dense factorisation: trailing update on the tensor cores (3xTF32
+  // tcgen05) or on the FP32 pipes (gbba_autotune)
+  bool factor_tensor = true;
+  // iterative path: warps per camera of the camera-side PCG kernels (2, 4 or 8; gbba_autotune)
+  int camera_warps = 4;
   // device time of the main kernel(s) of the last triangulation or engine-scan call
   cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr;
   bool kernel_timed = false;

@@ -31,6 +31,7 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 
 #include <cub/device/device_radix_sort.cuh>
 
@@ -1157,21 +1158,27 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
   s = t;
 }
 
-// Camera diagonal blocks U_c = sum Jc^T Jc, the preconditioner block
-// (U_c + D_c^2 - sum (W V^-1) W^T)^-1 (identity on held coordinates); one warp per camera.
-template <int B, typename T>
-__global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__ cam_off,
-                                                    const uint32_t* __restrict__ cam_obs, const T* __restrict__ rec,
-                                                    const int32_t* __restrict__ ext_col,
-                                                    const int32_t* __restrict__ intr_col,
-                                                    const int32_t* __restrict__ cam_group, int K, int64_t nc,
-                                                    const double* __restrict__ diag_c, const double* __restrict__ radius,
-                                                    T* __restrict__ U, double* __restrict__ Minv, int* __restrict__ flag) {
+// Camera diagonal blocks U_c = sum Jc^T Jc and the preconditioner block
+// S_c = U_c + D_c^2 - sum (W V^-1) W^T (identity on held coordinates), into
+// Mblk, which k_cam_inverse then inverts in place.  One block of kCamWarps
+// (2, 4 or 8: the handle's camera_warps) warps per camera: warp w takes every kCamWarps-th of the camera's
+// observations (lanes over the block's entries, two observations in flight),
+// and the warps' partial blocks are added in warp order.
+template <int B, typename T, int kCamWarps>
+__global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* __restrict__ cam_off,
+                                                               const uint32_t* __restrict__ cam_obs,
+                                                               const T* __restrict__ rec,
+                                                               const int32_t* __restrict__ ext_col,
+                                                               const int32_t* __restrict__ intr_col,
+                                                               const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                               const double* __restrict__ diag_c,
+                                                               const double* __restrict__ radius, T* __restrict__ U,
+                                                               double* __restrict__ Mblk) {
   using R = Rec<B>;
   constexpr int E = (B * B + 31) / 32;
-  __shared__ double sm[4][B * B];
+  __shared__ double part[kCamWarps][2][E * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t c = blockIdx.x;
   if (c >= nc) return;
   double accU[E], accS[E];
 #pragma unroll
@@ -1182,7 +1189,8 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
     float su[E], cu[E], ss[E], cs[E];
 #pragma unroll
     for (int e = 0; e < E; ++e) su[e] = cu[e] = ss[e] = cs[e] = 0.0f;
-    for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
+#pragma unroll 2
+    for (uint32_t q = cam_off[c] + warp; q < cam_off[c + 1]; q += kCamWarps) {
       const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
@@ -1203,7 +1211,7 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
       accS[e] = (double)ss[e] - (double)cs[e];
     }
   } else {
-    for (uint32_t q = cam_off[c]; q < cam_off[c + 1]; ++q) {
+    for (uint32_t q = cam_off[c] + warp; q < cam_off[c + 1]; q += kCamWarps) {
       const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
 #pragma unroll
       for (int e = 0; e < E; ++e) {
@@ -1220,23 +1228,45 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
       }
     }
   }
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    part[warp][0][lane + 32 * e] = accU[e];
+    part[warp][1][lane + 32 * e] = accS[e];
+  }
+  __syncthreads();
+  if (warp != 0) return;
   const double rad = *radius;
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int idx = lane + 32 * e;
     if (idx >= B * B) continue;
+    double u = 0.0, v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kCamWarps; ++w) {  // warp order: fixed
+      u += part[w][0][idx];
+      v += part[w][1][idx];
+    }
     const int i = idx / B, j = idx % B;
-    U[c * B * B + idx] = (T)accU[e];
+    U[c * B * B + idx] = (T)u;
     const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, i);
     const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
-    double v = accS[e];
     if (i == j && ci >= 0) v += diag_c[ci] / rad;
     if (ci < 0 || cj < 0) v = (i == j) ? 1.0 : 0.0;
-    sm[warp][idx] = v;
+    Mblk[c * B * B + idx] = v;
   }
-  __syncwarp();
-  if (lane == 0) {
-    double* A = sm[warp];
+}
+
+// In place: each camera's preconditioner block (row-major B x B) replaced by
+// its inverse, FP64 Cholesky and two triangular solves per column; one
+// thread per camera.  A block that is not positive definite sets *flag = 4.
+template <int B>
+__global__ void __launch_bounds__(128) k_cam_inverse(double* __restrict__ Minv, int64_t nc, int* __restrict__ flag) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double A[B * B];
+  double* Mi = Minv + c * B * B;
+  for (int e = 0; e < B * B; ++e) A[e] = Mi[e];
+  {
     bool ok = true;
     for (int j = 0; j < B && ok; ++j) {  // Cholesky, lower, in place
       double d = A[j * B + j];
@@ -1254,7 +1284,6 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
       }
     }
     if (!ok) atomicExch(flag, 4);
-    double* Mi = Minv + c * B * B;
     for (int col = 0; col < B; ++col) {  // columns of the inverse by two triangular solves
       double y[B];
       for (int i = 0; i < B; ++i) {
@@ -1271,6 +1300,7 @@ __global__ void __launch_bounds__(128) k_cam_blocks(const uint32_t* __restrict__
     }
   }
 }
+
 
 // y_p = V_p^-1 sum_{o in p} W_o^T x_c(o); one warp per point.
 template <int B, typename T>
@@ -1336,81 +1366,85 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
   }
 }
 
-// out_c = (U_c + D_c^2) x_c - sum_{o in c} W_o y_p(o); one warp per camera.
-template <int B, typename T>
-__global__ void __launch_bounds__(128) k_spmv_camera(const uint32_t* __restrict__ cam_off,
-                                                     const uint32_t* __restrict__ cam_obs,
-                                                     const uint32_t* __restrict__ pt, const T* __restrict__ rec,
-                                                     const T* __restrict__ U, const int32_t* __restrict__ ext_col,
-                                                     const int32_t* __restrict__ intr_col,
-                                                     const int32_t* __restrict__ cam_group, int K, int64_t nc,
-                                                     const double* __restrict__ diag_c,
-                                                     const double* __restrict__ radius, const double* __restrict__ x,
-                                                     const double* __restrict__ y, const float* __restrict__ yf,
-                                                     double* __restrict__ out, double* __restrict__ part,
-                                                     const PcgState* __restrict__ ps, int reset_period) {
+// out_c = (U_c + D_c^2) x_c - sum_{o in c} W_o y_p(o).  One block of
+// kCamWarps warps per camera, one lane per observation; the warps' sums are
+// added in warp order.  part[c] receives x_c . out_c (the partials of p.q).
+template <int B, typename T, int kCamWarps>
+__global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
+    const uint32_t* __restrict__ cam_off, const uint32_t* __restrict__ cam_obs, const uint32_t* __restrict__ pt,
+    const T* __restrict__ rec, const T* __restrict__ U, const int32_t* __restrict__ ext_col,
+    const int32_t* __restrict__ intr_col, const int32_t* __restrict__ cam_group, int K, int64_t nc,
+    const double* __restrict__ diag_c, const double* __restrict__ radius, const double* __restrict__ x,
+    const double* __restrict__ y, const float* __restrict__ yf, double* __restrict__ out, double* __restrict__ part,
+    const PcgState* __restrict__ ps, int reset_period) {
   using R = Rec<B>;
-  __shared__ double pdot[4];
+  __shared__ double red[kCamWarps][B];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t c = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t c = blockIdx.x;
   if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
-  double xo = 0.0;  // this lane's x . out (the partials of p.q)
-  if (c < nc) {
-    double acc[B];
+  if (c >= nc) {
+    if (part && threadIdx.x == 0) part[c] = 0.0;
+    return;
+  }
+  double acc[B];
 #pragma unroll
-    for (int i = 0; i < B; ++i) acc[i] = 0.0;
-    if constexpr (sizeof(T) == 4) {
-      // FP32 products, Kahan-compensated FP32 sums per lane (a camera has
-      // thousands of observations), FP64 from the lane sums on
-      float sa[B], ca[B];
+  for (int i = 0; i < B; ++i) acc[i] = 0.0;
+  const uint32_t q0 = cam_off[c] + warp * 32 + lane, q1 = cam_off[c + 1];
+  if constexpr (sizeof(T) == 4) {
+    // FP32 products, Kahan-compensated FP32 sums per lane (a camera has
+    // thousands of observations), FP64 from the lane sums on
+    float sa[B], ca[B];
 #pragma unroll
-      for (int i = 0; i < B; ++i) sa[i] = ca[i] = 0.0f;
-      for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
-        const uint32_t o = cam_obs[q];
-        const T* r = rec + (int64_t)o * R::kSize;
-        const float* yp = yf + 3 * (int64_t)pt[o];
-        const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
+    for (int i = 0; i < B; ++i) sa[i] = ca[i] = 0.0f;
+    for (uint32_t q = q0; q < q1; q += kCamWarps * 32) {
+      const uint32_t o = cam_obs[q];
+      const T* r = rec + (int64_t)o * R::kSize;
+      const float* yp = yf + 3 * (int64_t)pt[o];
+      const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
 #pragma unroll
-        for (int i = 0; i < B; ++i)
-          kahan_add(sa[i], ca[i], -(r[R::kW + 3 * i] * y0 + r[R::kW + 3 * i + 1] * y1 + r[R::kW + 3 * i + 2] * y2));
-      }
-#pragma unroll
-      for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
-    } else {
-      for (uint32_t q = cam_off[c] + lane; q < cam_off[c + 1]; q += 32) {
-        const uint32_t o = cam_obs[q];
-        const T* r = rec + (int64_t)o * R::kSize;
-        const double* yp = y + 3 * (int64_t)pt[o];
-        const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
-#pragma unroll
-        for (int i = 0; i < B; ++i)
-          acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
-      }
+      for (int i = 0; i < B; ++i)
+        kahan_add(sa[i], ca[i], -(r[R::kW + 3 * i] * y0 + r[R::kW + 3 * i + 1] * y1 + r[R::kW + 3 * i + 2] * y2));
     }
 #pragma unroll
-    for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
-    if (lane < B) {
-      double v = acc[0];
+    for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
+  } else {
+    for (uint32_t q = q0; q < q1; q += kCamWarps * 32) {
+      const uint32_t o = cam_obs[q];
+      const T* r = rec + (int64_t)o * R::kSize;
+      const double* yp = y + 3 * (int64_t)pt[o];
+      const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
 #pragma unroll
-      for (int i = 1; i < B; ++i)
-        if (lane == i) v = acc[i];
-      const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
-      if (ci >= 0) {
-        double u = diag_c[ci] / *radius * x[ci];
-        for (int j = 0; j < B; ++j) {
-          const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
-          if (cj >= 0) u += (double)U[c * B * B + lane * B + j] * x[cj];
-        }
-        out[ci] = v + u;
-        xo = x[ci] * (v + u);
+      for (int i = 0; i < B; ++i)
+        acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < B; ++i) acc[i] = warp_sum(acc[i]);
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < B; ++i) red[warp][i] = acc[i];
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  double xo = 0.0;  // this lane's x . out
+  if (lane < B) {
+    double v = 0.0;
+#pragma unroll
+    for (int w = 0; w < kCamWarps; ++w) v += red[w][lane];
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, lane);
+    if (ci >= 0) {
+      double u = diag_c[ci] / *radius * x[ci];
+      for (int j = 0; j < B; ++j) {
+        const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
+        if (cj >= 0) u += (double)U[c * B * B + lane * B + j] * x[cj];
       }
+      out[ci] = v + u;
+      xo = x[ci] * (v + u);
     }
   }
   if (!part) return;
   xo = warp_sum(xo);
-  if (lane == 0) pdot[warp] = xo;
-  __syncthreads();
-  if (threadIdx.x == 0) part[blockIdx.x] = (pdot[0] + pdot[1]) + (pdot[2] + pdot[3]);
+  if (lane == 0) part[c] = xo;
 }
 
 // ---- device-resident CG (ceres ConjugateGradientsSolver::Solve,
@@ -2396,7 +2430,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p1.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
     p1.take<double>((size_t)nc * B * B);
     p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
-    p1.take<double>(2 * std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1));  // PCG partial sums
+    p1.take<double>(2 * std::max<int64_t>(4096, nc + 1));  // PCG partial sums (one per camera block at most)
     p1.take<PcgState>(1);
     size_t cam_sort_bytes = 0;
     cub::DeviceRadixSort::SortPairs(nullptr, cam_sort_bytes, (const uint32_t*)nullptr, (uint32_t*)nullptr,
@@ -2429,7 +2463,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     if (!(tsize == 4 && n_pcg)) s.pcg_xf = s.pcg_yf = nullptr;
     s.pcg_minv = A.take<double>((size_t)nc * B * B);
     s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
-    s.pcg_part_n = std::max<int64_t>(4096, ceil_div(nc * 32, 128) + 1);
+    s.pcg_part_n = std::max<int64_t>(4096, nc + 1);
     s.pcg_part = A.take<double>(2 * s.pcg_part_n);
     s.pcg_state = A.take<PcgState>(1);
     s.nb_pcg = 256;
@@ -2576,7 +2610,7 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   const int64_t n = s.n_red;
   const int nbv = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), s.nb_pcg));
   const int nbc = (int)std::max<int64_t>(1, ceil_div(s.nc, 256));      // k_pcg_precond blocks
-  const int nbs = (int)std::max<int64_t>(1, ceil_div(s.nc * 32, 128));  // k_spmv_camera blocks
+  const int nbs = (int)std::max<int64_t>(1, s.nc);  // k_spmv_camera blocks (one per camera)
   const int period = std::max(1, o->refinement_interval);
   PcgState* ps = s.pcg_state;
   double* part_a = s.pcg_part;                 // r.z, then p.q
@@ -2596,9 +2630,15 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
           s.pcg_xf, s.pcg_yf, ps, reset);
       check_launch(h);
     }
-    k_spmv_camera<B, T><<<(unsigned)nbs, 128, 0, st>>>(
-        s.cam_off, s.cam_obs, s.pt, (const T*)s.rec, (const T*)s.pcg_u, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc,
-        s.diag_c, s.radius, x, s.pcg_y, s.pcg_yf, out, part, ps, reset);
+    auto cam = [&](auto warps) {
+      constexpr int W = decltype(warps)::value;
+      k_spmv_camera<B, T, W><<<(unsigned)nbs, W * 32, 0, st>>>(
+          s.cam_off, s.cam_obs, s.pt, (const T*)s.rec, (const T*)s.pcg_u, s.ext_col, s.intr_col, s.cam_group, s.k,
+          s.nc, s.diag_c, s.radius, x, s.pcg_y, s.pcg_yf, out, part, ps, reset);
+    };
+    if (h->camera_warps == 2) cam(std::integral_constant<int, 2>());
+    else if (h->camera_warps == 8) cam(std::integral_constant<int, 8>());
+    else cam(std::integral_constant<int, 4>());
     check_launch(h);
   };
   auto iteration = [&]() {
@@ -2880,10 +2920,18 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
                 s.n_pad, gshards);
             check_launch(h);
           }
-          if (!s.dense) {
-            k_cam_blocks<B, T><<<(unsigned)ceil_div(s.nc * 32, 128), 128, 0, st>>>(
-                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.diag_c,
-                s.radius, (T*)s.pcg_u, s.pcg_minv, s.flag);
+          if (!s.dense && s.nc > 0) {
+            auto cam_blocks = [&](auto warps) {
+              constexpr int W = decltype(warps)::value;
+              k_cam_blocks<B, T, W><<<(unsigned)s.nc, W * 32, 0, st>>>(
+                  s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, s.diag_c,
+                  s.radius, (T*)s.pcg_u, s.pcg_minv);
+            };
+            if (h->camera_warps == 2) cam_blocks(std::integral_constant<int, 2>());
+            else if (h->camera_warps == 8) cam_blocks(std::integral_constant<int, 8>());
+            else cam_blocks(std::integral_constant<int, 4>());
+            check_launch(h);
+            k_cam_inverse<B><<<(unsigned)ceil_div(s.nc, 128), 128, 0, st>>>(s.pcg_minv, s.nc, s.flag);
             check_launch(h);
           }
         } else if (s.np > 0) {

@@ -100,10 +100,12 @@ def factor_flops(n_red):
 
 # DRAM bytes (read + write) per observation of one Schur phase, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum summed over the
-# phase's kernels) of the current kernels on the medium workload; multiplied
-# by the observation count (the phase's traffic grows with the observations).
-SCHUR_TRAFFIC_PER_OBS = None
-SCHUR_TRAFFIC_SOURCE = "not captured for the current kernels"
+# phase's four kernels, two executions averaged) of the current kernels on
+# the medium workload: 4.999 GB for 1,999,428 observations; multiplied by the
+# observation count (the phase's traffic grows with the observations).
+SCHUR_TRAFFIC_PER_OBS = 2500.1
+SCHUR_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_schur_point_rec, k_schur_pairs, "
+                        "k_pair_merge, k_rhs_camera on the medium workload, per observation, times the observations")
 
 # FP32 SIMT peak of a GB300: 152 SMs x 128 FP32 lanes x 2 flops x 2.07 GHz.
 FP32_SIMT_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12

@@ -146,7 +146,7 @@ typedef enum gbsfm_lock {
  * ceres::RotationMatrixToAngleAxis, then t) in ascending image id,
  * intrinsic groups in key order, points in track order; observations keep
  * the track-major order, dropping entries of images without a camera.  It is
- * a gbba_problem of camera model GBBA_MODEL_RADIAL_K3 as it stands. */
+ * a gbba_problem of camera model GBBA_RADIAL_K3 as it stands. */
 typedef struct gbsfm_ba_arrays {
   double* extrinsics;
   double* intrinsics;
