@@ -145,6 +145,10 @@ class GbbaTuning(C.Structure):
         ("num_candidates", C.c_int32),
         ("candidates", C.c_int32 * TUNE_MAX_CANDIDATES),
         ("schur_time_s", C.c_double * TUNE_MAX_CANDIDATES),
+        ("factor_tensor", C.c_int32),
+        ("camera_warps", C.c_int32),
+        ("factor_time_s", C.c_double * 2),
+        ("pcg_time_s", C.c_double * 3),
     ]
 
 

@@ -362,36 +362,76 @@ gbba_status gbba_autotune(gbba_handle* h, const gbba_problem* P, const gbba_opti
     t.gradient_tolerance = 0.0;
     t.parameter_tolerance = 0.0;
     t.fp64_polish_iterations = 0;
-    const int32_t cand[3] = {32, 64, 128};
-    const int keep_chunk = h->pair_chunk;
-    out->num_candidates = 3;
-    int best = -1;
-    for (int c = 0; c < 3; ++c) {
-      h->pair_chunk = cand[c];
-      double per_iter = 0.0;
-      for (int rep = 0; rep < 2; ++rep) {  // the first run warms the workspace
-        gbba_summary sum;
+    // one trial: two solves (the first warms the workspace), the second's
+    // summary; the handle's choices are restored if a solve fails
+    const int keep_chunk = h->pair_chunk, keep_cw = h->camera_warps;
+    const bool keep_ft = h->factor_tensor;
+    gbba_summary sum;
+    auto trial = [&]() -> gbba_status {
+      for (int rep = 0; rep < 2; ++rep) {
         std::memset(&sum, 0, sizeof(sum));
         gbba_status s = GBBA_SUCCESS;
         try {
           s = solve_impl(h, P, &t, &sum);
         } catch (...) {
           h->pair_chunk = keep_chunk;
+          h->camera_warps = keep_cw;
+          h->factor_tensor = keep_ft;
           throw;
         }
         move(false);
         if (s != GBBA_SUCCESS) {
           h->pair_chunk = keep_chunk;
+          h->camera_warps = keep_cw;
+          h->factor_tensor = keep_ft;
           return s;
         }
-        per_iter = sum.num_iterations > 0 ? sum.schur_kernel_time_s / sum.num_iterations : sum.schur_kernel_time_s;
       }
+      return GBBA_SUCCESS;
+    };
+    auto per_iter = [&](double total) { return sum.num_iterations > 0 ? total / sum.num_iterations : total; };
+    // 1. work-item size of the camera-pair products
+    const int32_t cand[3] = {32, 64, 128};
+    out->num_candidates = 3;
+    int best = -1;
+    bool iterative = false;
+    for (int c = 0; c < 3; ++c) {
+      h->pair_chunk = cand[c];
+      const gbba_status s = trial();
+      if (s != GBBA_SUCCESS) return s;
+      iterative = sum.linear_solver_iterations > 0;
       out->candidates[c] = cand[c];
-      out->schur_time_s[c] = per_iter;
-      if (best < 0 || per_iter < out->schur_time_s[best]) best = c;
+      out->schur_time_s[c] = per_iter(sum.schur_kernel_time_s);
+      if (best < 0 || out->schur_time_s[c] < out->schur_time_s[best]) best = c;
     }
     h->pair_chunk = cand[best];
     out->pair_chunk = cand[best];
+    out->factor_tensor = -1;
+    out->camera_warps = 0;
+    if (!iterative && t.precision == GBBA_PRECISION_MIXED) {
+      // 2. trailing-update engine of the dense FP32 factorisation
+      for (int e = 0; e < 2; ++e) {
+        h->factor_tensor = e == 1;
+        const gbba_status s = trial();
+        if (s != GBBA_SUCCESS) return s;
+        out->factor_time_s[e] = per_iter(sum.factor_time_s);
+      }
+      h->factor_tensor = out->factor_time_s[1] <= out->factor_time_s[0];
+      out->factor_tensor = h->factor_tensor ? 1 : 0;
+    } else if (iterative) {
+      // 3. warps per camera of the PCG camera kernels
+      const int warps[3] = {2, 4, 8};
+      int wb = 1;
+      for (int w = 0; w < 3; ++w) {
+        h->camera_warps = warps[w];
+        const gbba_status s = trial();
+        if (s != GBBA_SUCCESS) return s;
+        out->pcg_time_s[w] = per_iter(sum.linear_solver_time_s + sum.jacobian_time_s);
+        if (out->pcg_time_s[w] < out->pcg_time_s[wb]) wb = w;
+      }
+      h->camera_warps = warps[wb];
+      out->camera_warps = warps[wb];
+    }
     return GBBA_SUCCESS;
   });
 }

@@ -655,6 +655,19 @@ def run_ours(args):
         h.check(rc, "gbba_solve")
         return summ.num_iterations
 
+    # ---- the library's autotuner on this problem, once, before any timing
+    # (it leaves the parameters unchanged and keeps its choices in the handle)
+    autotune = None
+    if args.autotune:
+        tun = abi.GbbaTuning()
+        t_at = time.perf_counter()
+        h.check(h.lib.gbba_autotune(h.h, ctypes.byref(st), ctypes.byref(opts), 2, ctypes.byref(tun)), "gbba_autotune")
+        autotune = {"seconds": time.perf_counter() - t_at, "pair_chunk": tun.pair_chunk,
+                    "schur_ms": dict(zip(map(str, tun.candidates[:tun.num_candidates]),
+                                         [1e3 * v for v in tun.schur_time_s[:tun.num_candidates]])),
+                    "factor_engine": {1: "tensor cores (tcgen05 3xTF32)", 0: "FP32 pipes", -1: None}[tun.factor_tensor],
+                    "factor_ms": {"fp32_pipes": 1e3 * tun.factor_time_s[0], "tensor": 1e3 * tun.factor_time_s[1]}}
+
     for _ in range(args.warmup):
         step()
     barrier()
@@ -740,6 +753,7 @@ def run_ours(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "working set > L2 (obs 56 MB + W scratch 576 MB + S 144 MB per iteration)"},
             "gpu_launches": int(launches),
+            "autotune": autotune,
             "clocks": clk,
             "e2e": e2e,
             "roofline": {"kernel": "Schur elimination phase (k_schur_point_rec + k_schur_pairs + k_pair_merge"
@@ -791,6 +805,8 @@ def main():
     ap.add_argument("--iters", type=int, default=20, help="LM iterations per step")
     ap.add_argument("--ttc-iters", type=int, default=200)
     ap.add_argument("--large-iters", type=int, default=100, help="LM iterations of each large-workload solve")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false",
+                    help="time with the handle's default kernel choices instead of gbba_autotune's")
     ap.add_argument("--no-time-to-cost", dest="time_to_cost", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-triangulation", dest="triangulation", action="store_false")

@@ -232,21 +232,33 @@ gbba_status gbba_solve_batched(gbba_handle* handle, const gbba_problem* problems
                                int32_t num_problems, const gbba_options* options,
                                gbba_summary* summaries);
 
-/* Autotuner of the atomic-free Schur build (no counterpart in the reference,
- * whose ceres solve has no tunable kernels).  Its camera-pair products run one
- * warp per work item of at most `pair_chunk` observation pairs of one
- * camera-pair block; smaller items spread the long diagonal blocks over more
- * warps, larger ones read fewer partial sums.  gbba_autotune runs
- * `iterations` LM iterations of `problem` with `options` for each candidate
- * item size, times the Schur phase on the device, and keeps the fastest in
- * the handle for its later solves.  The problem's parameters are restored
- * after each trial, so the call leaves them unchanged. */
+/* Autotuner (no counterpart in the reference, whose ceres solve has no
+ * tunable kernels).  It times `iterations` LM iterations of `problem` with
+ * `options` on the device for each candidate of three choices, one after the
+ * other, and keeps the fastest of each in the handle for its later solves:
+ *   - the work-item size of the camera-pair products of the Schur build (one
+ *     warp per item of at most `pair_chunk` observation pairs of one
+ *     camera-pair block: smaller items spread the long diagonal blocks over
+ *     more warps, larger ones read fewer partial sums), by the Schur phase's
+ *     time;
+ *   - for the dense FP32 factorisation, the engine of its trailing update:
+ *     the tensor cores (tcgen05, 3xTF32) or the FP32 pipes, by the
+ *     factorisation's time;
+ *   - for the iterative (PCG) path, the warps per camera of its camera-side
+ *     kernels (preconditioner blocks, implicit Schur products), by the linear
+ *     solver's time.
+ * The problem's parameters are restored after each trial, so the call leaves
+ * them unchanged. */
 #define GBBA_TUNE_MAX_CANDIDATES 4
 typedef struct gbba_tuning {
   int32_t pair_chunk;                                    /* chosen work-item size (pairs) */
   int32_t num_candidates;
   int32_t candidates[GBBA_TUNE_MAX_CANDIDATES];          /* 32, 64, 128 */
   double schur_time_s[GBBA_TUNE_MAX_CANDIDATES];         /* Schur-phase device time per LM iteration */
+  int32_t factor_tensor;                                 /* chosen: 1 tensor cores, 0 FP32 pipes (-1: not tuned) */
+  int32_t camera_warps;                                  /* chosen: 2, 4 or 8 (0: not tuned) */
+  double factor_time_s[2];                               /* dense factorisation per LM iteration: FP32 pipes, tensor */
+  double pcg_time_s[3];                                  /* linear solver per LM iteration: 2, 4, 8 warps */
 } gbba_tuning;
 gbba_status gbba_autotune(gbba_handle* handle, const gbba_problem* problem, const gbba_options* options,
                           int32_t iterations, gbba_tuning* tuning);

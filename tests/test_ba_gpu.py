@@ -289,11 +289,45 @@ def test_autotune_keeps_the_fastest_work_item_size(gb, abi, scenes):
         times = list(tun.schur_time_s[:3])
         assert all(t > 0 for t in times)
         assert tun.pair_chunk == tun.candidates[times.index(min(times))]
+        assert tun.factor_tensor == -1 and tun.camera_warps == 0  # FP64 dense: nothing else to tune
         for k, v in hp.params().items():
             np.testing.assert_array_equal(v, before[k])
         s_tuned = h.solve(hp, opts)
         assert s_tuned.usable
         assert abs(s_tuned.final_cost - s_ref.final_cost) <= 1e-9 * s_ref.final_cost
+    finally:
+        h.close()
+
+
+@pytest.mark.parametrize("path", ["dense_mixed", "pcg_mixed"])
+def test_autotune_factor_engine_and_camera_warps(gb, abi, scenes, path):
+    """In mixed precision the autotuner also times the dense factorisation's
+    trailing-update engine (tensor cores or FP32 pipes) or, on the PCG path,
+    the warps per camera of the camera-side kernels, keeps the faster, and the
+    tuned handle's solve reaches the untuned one's final cost within 1e-6."""
+    sc = scenes.medium_scene(num_cameras=40, num_points=3000, seed=132)
+    sc["camera_constant"][1] = 1
+    opts = scenes.ba_options_for(sc, max_num_iterations=15, precision=abi.PRECISION_MIXED)
+    if path == "pcg_mixed":
+        opts.linear_solver = abi.SOLVER_ITERATIVE_SCHUR
+    h = gb.Handle(0)
+    try:
+        s_ref, _ = solve(h, abi, sc, opts)
+        hp = abi.HostProblem(sc)
+        tun = abi.GbbaTuning()
+        p = hp.struct()
+        assert h.lib.gbba_autotune(h.h, C.byref(p), C.byref(opts), 2, C.byref(tun)) == abi.SUCCESS
+        if path == "dense_mixed":
+            ft = list(tun.factor_time_s)
+            assert all(t > 0 for t in ft) and tun.factor_tensor == (1 if ft[1] <= ft[0] else 0)
+            assert tun.camera_warps == 0
+        else:
+            pt = list(tun.pcg_time_s)
+            assert all(t > 0 for t in pt) and tun.camera_warps == (2, 4, 8)[pt.index(min(pt))]
+            assert tun.factor_tensor == -1
+        s_tuned = h.solve(hp, opts)
+        assert s_tuned.usable
+        assert abs(s_tuned.final_cost - s_ref.final_cost) <= 1e-6 * s_ref.final_cost
     finally:
         h.close()
 
