@@ -15,17 +15,18 @@
 //   - every sum the Schur build scatters (S, rhs, column norms, gradient) is
 //     accumulated in fixed point, integers under atomics: integer addition is
 //     associative, so the result does not depend on the order in which warps
-//     reach an entry and a solve is bitwise repeatable.  The scale is a power
-//     of two chosen from a bound on the sums (int32 entries of S with 2^30 of
-//     headroom in FP32, int64 with 2^60 in FP64; int64 vectors); a build whose
-//     column norms exceed the bound it was scaled for runs again with the new
-//     bound;
+//     reach an entry and a solve is bitwise repeatable.  The scales are
+//     powers of two: S_ij is scaled by 2^(e_i + e_j), e_i chosen from a bound
+//     on column i's norm, so that each entry keeps the resolution of its own
+//     columns (int32 entries of S in FP32, int64 in FP64); the vectors take
+//     one scale per window (int64).  A build that finds a column norm above
+//     the bound it was scaled for runs again with the norms it found;
 //   - the cost pass runs one thread per observation (FP64 residuals from the
 //     window's FP64 poses in shared memory);
 //   - the Schur build runs one warp per point (V, V^-1, g_p, W, W V^-1) and
 //     also forms the column norms and the gradient of its Jacobian (the LM
-//     diagonal and ceres's gradient check): FP64 sums in the global slice,
-//     FP32 sums in shared memory;
+//     diagonal and ceres's gradient check): the FP64 path's sums in the
+//     global slice, the FP32 path's in shared memory;
 //   - the Cholesky factorisation and both triangular solves run where S
 //     lives; every thread evaluates the step and takes the same accept /
 //     reject decision.
@@ -140,8 +141,14 @@ struct Shared {
   // FP32 path: fixed-point sums of rhs, column norms and gradient of the
   // Schur build's Jacobian
   long long fxv[3][N];
-  double fx[4];    // scales of S, column norms, gradient, rhs
-  double cbound;   // bound on the scaled column norms the scales are chosen for
+  double fx[4];    // scales of the column norms, gradient and rhs (fx[0] unused)
+  int fxk[4];      // their exponents
+  double cbnd[N];  // per column: bound on its scaled column norm the scales are chosen for
+  T fxs[N];        // per column: the power-of-two factor of S's fixed-point scale (FP32)
+  T fxi[N];        // its inverse
+  int32_t fxe[N];  // its exponent (FP64)
+  int fxbits;      // S's budget: 2^(2 e_i) bound_i < 2^fxbits
+  int fxbad;       // a term out of range or not finite (FP64)
   double red[kWarps];
   double bcast[8];
   int flag;
@@ -184,16 +191,52 @@ __device__ __forceinline__ double block_max(double v, double* red, double* out) 
   return *out;
 }
 
-// Largest power of two s with bound * s <= 2^bits (1 for a bound that is not
-// a positive finite number), its exponent clamped to [-lim, lim].
-__device__ __forceinline__ double pow2_scale(double bound, int bits, int lim = 1000) {
-  if (!(bound > 0.0) || !isfinite(bound)) return 1.0;
+// Exponent of the power of two 2^e with bound * 2^e <= 2^bits (0 for a
+// bound that is not a positive finite number), clamped to [-lim, lim].
+__device__ __forceinline__ int pow2_exp(double bound, int bits, int lim) {
+  if (!(bound > 0.0) || !isfinite(bound)) return 0;
   int e;
   frexp(bound, &e);  // bound < 2^e
-  return ldexp(1.0, max(-lim, min(lim, bits - e)));
+  return max(-lim, min(lim, bits - e));
 }
-__device__ __forceinline__ void fx_add(long long* p, double v, double scale) {
-  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__double2ll_rn(v * scale));
+// Exponent e of a column's factor 2^e with 2^(2e) * bound < 2^bits (lim for
+// a bound that is not a positive number), clamped to [-lim, lim].  S_ij is
+// accumulated scaled by 2^(e_i + e_j).  Every term added to S_ij is an entry
+// of a per-observation U or a W_x V^-1 W_y^T of two observations x, y of one
+// point, and U >= W_x V^-1 W_x^T: with every column norm within its bound,
+// Cauchy-Schwarz (over the observations, then over the points) keeps the
+// partial sums within (1 + m) sqrt(bound_i bound_j), m the most
+// observations of one point that touch one column.  So the scaled sums stay
+// below (1 + m) 2^bits, and each entry's resolution follows its own columns
+// instead of the largest column of the window.
+__device__ __forceinline__ int col_exp(double bound, int bits, int lim) {
+  if (!(bound > 0.0)) return lim;
+  if (!isfinite(bound)) return -lim;
+  int be;
+  frexp(bound, &be);  // bound < 2^be
+  return max(-lim, min(lim, (bits - be) >> 1));
+}
+// v * 2^k rounded to the nearest integer (ties away from zero) with integer
+// operations only (FP64 arithmetic is slow on this GPU); a result that
+// would reach 2^62 sets bit 0 of *bad, a value that is not finite bit 1,
+// and either gives 0.  Any rounding rule serves: a sum of integers does not
+// depend on the order.
+__device__ __forceinline__ long long fx_round(double v, int k, int* bad) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)(b >> 52) & 0x7ff;
+  const int sh = ex - 1075 + k;  // |v| 2^k = m 2^sh, m < 2^53
+  if (ex == 0x7ff || sh > 9) {
+    atomicOr(bad, ex == 0x7ff ? 2 : 1);
+    return 0;
+  }
+  const long long m = ex ? (long long)((b & 0xfffffffffffffull) | 0x10000000000000ull) : 0ll;
+  const int rs = min(max(-sh, 0), 63);
+  const long long ml = m << max(sh, 0);
+  const long long r = rs ? (ml + (1ll << (rs - 1))) >> rs : ml;
+  return (b >> 63) ? -r : r;
+}
+__device__ __forceinline__ void fx_add(long long* p, double v, int k, int* bad) {
+  atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)fx_round(v, k, bad));
 }
 __device__ __forceinline__ void fx_add(long long* p, float v, float scale) {
   atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)__float2ll_rn(v * scale));
@@ -293,26 +336,44 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     if constexpr (kGS) __stcg(g_S + i, (double)v);
     else sh.S[i] = v;
   };
-  // Fixed-point accumulation of the Schur build (scales sh.fx, set before
-  // each build): S as int64 in the global slice (FP64) or int32 in shared
-  // memory (FP32); rhs, the column norms (Nadd) and the gradient (Gadd) of
-  // the scaled Jacobian as int64 in the global slice (FP64) or in shared
-  // memory (FP32).
-  float fxf[4] = {1.f, 1.f, 1.f, 1.f};  // the FP32 path's copy of the scales
-  auto Sadd = [&](int i, SS v) {
-    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_S + i), (double)v, sh.fx[0]);
-    else atomicAdd(reinterpret_cast<int*>(&sh.S[i]), __float2int_rn((float)v * fxf[0]));
+  // Fixed-point accumulation of the Schur build (scales set before each
+  // build): S as int64 in the global slice (FP64) or int32 in shared memory
+  // (FP32), scaled per column pair; rhs, the column norms (Nadd) and the
+  // gradient (Gadd) of the scaled Jacobian as int64 in the global slice
+  // (FP64) or in shared memory (FP32), one scale each.  FP32 scales as
+  // factors, FP64 ones as exponents (integer rounding).
+  float fxf[4] = {1.f, 1.f, 1.f, 1.f};  // the FP32 path's copy of the vector scales
+  int fxk[4] = {0, 0, 0, 0};            // the FP64 path's copy of their exponents
+  // a column's factor of S's scale (a register copy: the atomics below
+  // keep the compiler from reusing a shared-memory load)
+  struct ColScale {
+    SS s;
+    int e;
   };
+  auto cscale = [&](int i) -> ColScale {
+    if constexpr (kGS) return {SS(0), sh.fxe[i]};
+    else return {sh.fxs[i], 0};
+  };
+  // S_ij (i >= j) += v, scaled by the columns' factors
+  auto Sadd_s = [&](int i, int j, SS v, ColScale fi, ColScale fj) {
+    const int e = tri(i, j);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_S + e), (double)v, fi.e + fj.e, &sh.fxbad);
+    else atomicAdd(reinterpret_cast<int*>(&sh.S[e]), __float2int_rn((float)v * (fi.s * fj.s)));
+  };
+  auto Sadd = [&](int i, int j, SS v) { Sadd_s(i, j, v, cscale(i), cscale(j)); };
   auto Nadd = [&](int i, T v) {
-    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_acc + i), (double)v, sh.fx[1]);
-    else fx_add(&sh.fxv[1][i], (float)v, fxf[1]);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_acc + i), (double)v, fxk[1], &sh.fxbad);
+    else {
+      if (!isfinite((float)v)) atomicOr(&sh.fxbad, 2);
+      fx_add(&sh.fxv[1][i], (float)v, fxf[1]);
+    }
   };
   auto Gadd = [&](int i, T v) {
-    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_grad + i), (double)v, sh.fx[2]);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_grad + i), (double)v, fxk[2], &sh.fxbad);
     else fx_add(&sh.fxv[2][i], (float)v, fxf[2]);
   };
   auto Radd = [&](int i, SS v) {
-    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_rhs + i), (double)v, sh.fx[3]);
+    if constexpr (kGS) fx_add(reinterpret_cast<long long*>(g_rhs + i), (double)v, fxk[3], &sh.fxbad);
     else fx_add(&sh.fxv[0][i], (float)v, fxf[3]);
   };
 
@@ -328,10 +389,13 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     const T* Su = base + (int64_t)u * SL::kSize;
     const T* Sw = base + (int64_t)w * SL::kSize;
     int ci[6], cj[6];
+    ColScale fi[6], fj[6];
 #pragma unroll
     for (int j = 0; j < 6; ++j) {
       ci[j] = ecol(cu, j);
       cj[j] = ecol(cw, j);
+      fi[j] = ci[j] >= 0 ? cscale(ci[j]) : ColScale{};
+      fj[j] = cj[j] >= 0 ? cscale(cj[j]) : ColScale{};
     }
     // W_w (and for an observation's own pair its Jc_e) in registers; the
     // rows of (W V^-1)_u are read as they are used (FP64: register budget)
@@ -356,7 +420,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         if (cj[j] < 0 || cj[j] > ci[i]) continue;
         const T s = j0[i] * j0[j] + j1[i] * j1[j] -
                     (hu[3 * i] * ww[3 * j] + hu[3 * i + 1] * ww[3 * j + 1] + hu[3 * i + 2] * ww[3 * j + 2]);
-        Sadd(tri(ci[i], cj[j]), (SS)s);
+        Sadd_s(ci[i], cj[j], (SS)s, fi[i], fj[j]);
       }
     }
   };
@@ -461,7 +525,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     mc = block_max(mc, sh.red, &sh.bcast[5]);
     mg = block_max(mg, sh.red, &sh.bcast[6]);
     const double nobs = (double)(a.pt_off[P.x1] - a.pt_off[P.x0]);
-    const double sc = pow2_scale(mc * nobs, 62), sg = pow2_scale(mg * nobs, 62);
+    const int kc = pow2_exp(mc * nobs, 62, 1000), kg = pow2_exp(mg * nobs, 62, 1000);
     for (int i = tid; i < n; i += kThreads) {
       __stcg(reinterpret_cast<long long*>(g_acc + i), 0ll);
       __stcg(reinterpret_cast<long long*>(g_grad + i), 0ll);
@@ -479,8 +543,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
         for (int j = 0; j < B; ++j) {
           if (col[j] < 0) continue;
           const double x0 = Jc[0][j], x1 = Jc[1][j];
-          fx_add(reinterpret_cast<long long*>(g_acc + col[j]), x0 * x0 + x1 * x1, sc);
-          fx_add(reinterpret_cast<long long*>(g_grad + col[j]), x0 * r[0] + x1 * r[1], sg);
+          fx_add(reinterpret_cast<long long*>(g_acc + col[j]), x0 * x0 + x1 * x1, kc, &sh.fxbad);
+          fx_add(reinterpret_cast<long long*>(g_grad + col[j]), x0 * r[0] + x1 * r[1], kg, &sh.fxbad);
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
@@ -506,8 +570,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
-      __stcg(g_acc + i, (double)__ldcg(reinterpret_cast<const long long*>(g_acc + i)) / sc);
-      __stcg(g_grad + i, (double)__ldcg(reinterpret_cast<const long long*>(g_grad + i)) / sg);
+      __stcg(g_acc + i, ldexp((double)__ldcg(reinterpret_cast<const long long*>(g_acc + i)), -kc));
+      __stcg(g_grad + i, ldexp((double)__ldcg(reinterpret_cast<const long long*>(g_grad + i)), -kg));
     }
     __syncthreads();
     for (int i = tid; i < n; i += kThreads) {
@@ -542,13 +606,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     return;
   }
+  {
+    // the most observations of one point that touch one column: of one
+    // camera (extrinsic columns; in a one-group window also the intrinsic
+    // ones, whose terms are summed per point first) or of one intrinsic
+    // group; S's sums stay below (1 + m) 2^fxbits
+    int mult = 1;
+    for (uint32_t p = P.x0 + warp; p < P.x1; p += kWarps) {
+      const uint32_t ob = a.pt_off[p], oe = a.pt_off[p + 1];
+      for (uint32_t x = ob + lane; x < oe; x += 32) {
+        const uint32_t cx = a.cam[x], gx = a.icam[x];
+        int nc = 0, ng = 0;
+        for (uint32_t y = ob; y < oe; ++y) {
+          nc += a.cam[y] == cx;
+          ng += a.icam[y] == gx;
+        }
+        mult = max(mult, P.ni == 1 ? nc : max(nc, ng));
+      }
+    }
+    mult = (int)block_max((double)mult, sh.red, &sh.bcast[7]);
+    // one bit spare below int32 / int64
+    if (tid == 0) sh.fxbits = (kGS ? 61 : 30) - (32 - __clz(mult));  // 32 - clz(m) = ceil(log2(1 + m))
+    __syncthreads();
+  }
   double gmax = linearize(true), xnorm = param_norm();
   {
-    // bound on the scaled column norms for the first build's fixed-point scale
-    double cb = 0.0;
-    for (int i = tid; i < n; i += kThreads) cb = fmax(cb, __ldcg(g_acc + i) * sh.scale_c[i] * sh.scale_c[i]);
-    cb = block_max(cb, sh.red, &sh.bcast[7]);
-    if (tid == 0) sh.cbound = fmax(cb, 1e-300);
+    // bounds on the scaled column norms for the first build's fixed-point scales
+    for (int i = tid; i < n; i += kThreads) sh.cbnd[i] = __ldcg(g_acc + i) * sh.scale_c[i] * sh.scale_c[i];
     __syncthreads();
   }
   bool check_grad = false;  // an accepted step's gradient is checked by the next Schur build
@@ -563,22 +647,34 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     }
     // ---- S = sum F'F - sum (F'E) V^-1 (E'F) + diag(D_c^2), rhs, and from
     // the same Jacobian the column norms (LM diagonal) and the gradient, in
-    // fixed point scaled for column norms up to 4 cbound (partial sums of S
-    // stay within twice the largest column norm: every term is an entry of a
-    // per-observation U or of a per-point W V^-1 W^T, both bounded by U's
-    // diagonal).  A build that finds larger norms runs again.
+    // fixed point: S_ij scaled by 2^(e_i + e_j), e_i chosen for a column
+    // norm of up to 4 cbnd[i] (col_exp gives the bound on S's sums); the
+    // vectors with one scale for the window.  A build that finds a column
+    // above its bound runs again.
     const double irad_d = 1.0 / radius;
     T gmt = T(0);  // gradient max norm (unscaled) over this thread's points
-    double cmax = 0.0;
+    double cover = 0.0;  // largest column norm / its bound of the last build
     for (int attempt = 0;; ++attempt) {
-    if (tid == 0) {
-      const double cb = sh.cbound;
-      const double G = 2.0 * sqrt(4.0 * cb * (2.0 * cost + 1e-300));
-      sh.fx[0] = pow2_scale(8.0 * cb, kGS ? 60 : 30, kGS ? 1000 : 120);
-      sh.fx[1] = pow2_scale(4.0 * cb, 60, kGS ? 1000 : 120);
-      sh.fx[2] = pow2_scale(G, 58, kGS ? 1000 : 120);
-      sh.fx[3] = pow2_scale(4.0 * G, 58, kGS ? 1000 : 120);
-      sh.flag = 0;
+    {
+      double cb = 0.0;
+      for (int i = tid; i < n; i += kThreads) {
+        const int e = col_exp(4.0 * sh.cbnd[i], sh.fxbits, kGS ? 500 : 60);
+        sh.fxe[i] = e;
+        sh.fxs[i] = (SS)ldexp(1.0, e);
+        sh.fxi[i] = (SS)ldexp(1.0, -e);
+        cb = fmax(cb, sh.cbnd[i]);
+      }
+      cb = block_max(cb, sh.red, &sh.bcast[7]);
+      if (tid == 0) {
+        const double G = 2.0 * sqrt(4.0 * cb * (2.0 * cost + 1e-300));
+        const int lim = kGS ? 1000 : 120;
+        sh.fxk[1] = pow2_exp(4.0 * cb, 60, lim);
+        sh.fxk[2] = pow2_exp(G, 58, lim);
+        sh.fxk[3] = pow2_exp(4.0 * G, 58, lim);
+        for (int q = 1; q < 4; ++q) sh.fx[q] = ldexp(1.0, sh.fxk[q]);
+        sh.flag = 0;
+        sh.fxbad = 0;
+      }
     }
     for (int i = tid; i < n * (n + 1) / 2; i += kThreads) Sst(i, SS(0));
     for (int i = tid; i < n; i += kThreads) {
@@ -593,7 +689,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
     gmt = T(0);
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 4; ++q) fxf[q] = (float)sh.fx[q];
+    for (int q = 1; q < 4; ++q) {
+      fxf[q] = (float)sh.fx[q];
+      fxk[q] = sh.fxk[q];
+    }
     // One intrinsic group per window (the local-BA case): the intrinsic
     // columns are common to every observation, so their terms factor through
     // per-point sums (no observation pairs):
@@ -672,7 +771,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
               const int cj = col[j];
               if (cj < 0) continue;
               const T u = Jc[0][i] * Jc[0][j] + Jc[1][i] * Jc[1][j];
-              Sadd(cj <= ci ? tri(ci, cj) : tri(cj, ci), (SS)u);
+              Sadd(max(ci, cj), min(ci, cj), (SS)u);
             }
           }
         }
@@ -748,7 +847,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
             while ((i + 1) * (i + 2) / 2 <= e) ++i;
             const int j = e - i * (i + 1) / 2;
             if (sh.kcol[i] >= 0 && sh.kcol[j] >= 0) {
-              Sadd(tri(sh.kcol[i], sh.kcol[j]), (SS)acc);
+              Sadd(sh.kcol[i], sh.kcol[j], (SS)acc);
               if (i == j) Nadd(sh.kcol[i], acc);
             }
           } else if (e < KK + K) {
@@ -767,7 +866,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
           if (ci < 0 || cj < 0) continue;
           const T sacc = sums[3 * i] * sums[3 * K + 3 * j] + sums[3 * i + 1] * sums[3 * K + 3 * j + 1] +
                          sums[3 * i + 2] * sums[3 * K + 3 * j + 2];
-          Sadd(tri(ci, cj), (SS)(-sacc));
+          Sadd(ci, cj, (SS)(-sacc));
         }
         // S_k,c(y) += U_ke(y) - Wh_K W_ey^T: one lane per observation y
         // (intrinsic columns follow every extrinsic column: lower triangle)
@@ -778,6 +877,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
 #pragma unroll
           for (int j = 0; j < 6; ++j) cj[j] = ecol(cy, j);
           if (cj[0] < 0 && cj[1] < 0 && cj[2] < 0 && cj[3] < 0 && cj[4] < 0 && cj[5] < 0) continue;
+          ColScale fj[6];
+#pragma unroll
+          for (int j = 0; j < 6; ++j) fj[j] = cj[j] >= 0 ? cscale(cj[j]) : ColScale{};
           T wy[18], j0[6], j1[6];
           ld18<T>(Wy + SL::kW, wy);
 #pragma unroll
@@ -791,11 +893,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
             if (ci < 0) continue;
             const T s0 = sums[3 * i], s1 = sums[3 * i + 1], s2 = sums[3 * i + 2];
             const T k0 = Wy[SL::kJ + 6 + i], k1 = Wy[SL::kJ + B + 6 + i];
+            const ColScale fi = cscale(ci);
 #pragma unroll
             for (int j = 0; j < 6; ++j) {
               if (cj[j] < 0) continue;
               const T val = k0 * j0[j] + k1 * j1[j] - (s0 * wy[3 * j] + s1 * wy[3 * j + 1] + s2 * wy[3 * j + 2]);
-              Sadd(tri(ci, cj[j]), (SS)val);
+              Sadd_s(ci, cj[j], (SS)val, fi, fj[j]);
             }
           }
         }
@@ -825,7 +928,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
               const int ci = i < 6 ? ecol(ca, i) : a.intr_col[K * (int64_t)ga + (i - 6)];
               const int cj = j < 6 ? ecol(cb, j) : a.intr_col[K * (int64_t)gb + (j - 6)];
               if (ci < 0 || cj < 0 || cj > ci) continue;
-              Sadd(tri(ci, cj),
+              Sadd(ci, cj,
                    (SS)(-(Wha[3 * i] * Wb[3 * j] + Wha[3 * i + 1] * Wb[3 * j + 1] + Wha[3 * i + 2] * Wb[3 * j + 2])));
             }
           }
@@ -834,30 +937,38 @@ __global__ void __launch_bounds__(kThreads, 1) k_lm_batched(BArgs a) {
       __syncwarp();
     }
     __syncthreads();
-    // the column norms against the bound the build was scaled for
+    // the column norms against the bounds the build was scaled for; the
+    // next build (this one again, or the next iteration's) takes the norms
+    // found as its bounds
     {
       double cm = 0.0;
-      bool sat = false;
       for (int i = tid; i < n; i += kThreads) {
         const long long v = kGS ? __ldcg(reinterpret_cast<const long long*>(g_acc + i)) : sh.fxv[1][i];
-        sat |= v >= (1ll << 62) || v < 0;
-        cm = fmax(cm, (double)v / sh.fx[1]);
+        const double c = (double)v / sh.fx[1];
+        const bool sat = v >= (1ll << 62) || v < 0;
+        cm = fmax(cm, sat ? CUDART_INF : c / (4.0 * sh.cbnd[i]));
+        sh.cbnd[i] = sat ? 65536.0 * sh.cbnd[i] + 1e-300 : c;
       }
-      cmax = block_max(sat ? CUDART_INF : cm, sh.red, &sh.bcast[7]);
+      cover = block_max(cm, sh.red, &sh.bcast[7]);
+      if (sh.fxbad & 1) cover = CUDART_INF;
     }
-    if (cmax <= 4.0 * sh.cbound || attempt >= 16) break;
-    __syncthreads();
-    if (tid == 0) sh.cbound = isfinite(cmax) ? cmax : sh.cbound * 65536.0;
-    __syncthreads();
+    // (a point block that failed to factor, or a Jacobian that is not
+    // finite, invalidates the step whatever the scales)
+    if (cover <= 1.0 || attempt >= 16 || sh.flag != 0 || (sh.fxbad & 2)) break;
     }  // build attempts
-    if (cmax > 4.0 * sh.cbound && tid == 0) sh.flag = 4;  // no scale fitted: the step is invalid
-    // back to floating point: S in place, then the next build's bound
-    for (int i = tid; i < n * (n + 1) / 2; i += kThreads) {
-      if constexpr (kGS) __stcg(g_S + i, (double)__ldcg(reinterpret_cast<const long long*>(g_S + i)) / sh.fx[0]);
-      else sh.S[i] = (float)(*reinterpret_cast<const int*>(&sh.S[i])) * (float)(1.0 / sh.fx[0]);
+    if ((cover > 1.0 || (sh.fxbad & 2)) && tid == 0 && sh.flag == 0) sh.flag = 4;  // the step is invalid
+    // back to floating point: S in place, a row per warp
+    for (int i = warp; i < n; i += kWarps) {
+      const SS si = sh.fxi[i];
+      for (int j = lane; j <= i; j += 32) {
+        const SS inv = si * sh.fxi[j];  // a power of two: exact
+        if constexpr (kGS)
+          __stcg(g_S + tri(i, j), (double)__ldcg(reinterpret_cast<const long long*>(g_S + tri(i, j))) * inv);
+        else
+          sh.S[tri(i, j)] = (float)(*reinterpret_cast<const int*>(&sh.S[tri(i, j)])) * inv;
+      }
     }
     __syncthreads();
-    if (tid == 0 && isfinite(cmax)) sh.cbound = fmax(cmax, 1e-300);
     // LM diagonal D_c^2 = clamp(column norms), rhs = gradient + Schur
     // correction, gradient max norm of this linearisation
     double gm = (double)gmt;

@@ -611,8 +611,24 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64
   T* xk = vec_at<T>(1);
   const int tid = threadIdx.x;
   const int64_t k0 = (int64_t)kb * NB;
+  // the next block row's kernel may start now (programmatic dependent
+  // launch): it touches b only after its griddepcontrol.wait
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
   load_tile<T>(Li, Linv_all + (int64_t)kb * NB * NB, NB, tid);
-  if (tid < NB) yk[tid] = b[k0 + tid];
+  const int jb = blockIdx.x;
+  const int c = tid & (NB - 1), q = tid >> 6;
+  // this block's column of L_kj^T (written by the factorisation, complete
+  // before the backward substitution began) is loaded before the wait
+  T v[NB / 4];
+  if (jb != kb) {
+    const T* col = S + (k0 + q) * ld + (int64_t)jb * NB + c;
+#pragma unroll
+    for (int t = 0; t < NB / 4; ++t) v[t] = col[(int64_t)(4 * t) * ld];
+  }
+  // y_k and the b entries this kernel updates were written by the previous
+  // block row's kernel: wait for it, and read b through L2
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  if (tid < NB) yk[tid] = __ldcg(b + k0 + tid);
   __syncthreads();
   if (tid < NB) {
     T s = T(0);
@@ -621,18 +637,12 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64
     xk[tid] = s;
   }
   __syncthreads();
-  const int jb = blockIdx.x;
   if (jb == kb) {
     if (tid < NB) x[k0 + tid] = xk[tid];
     return;
   }
   // y_j -= L_kj^T x_k : thread (q, c) sums rows q, q+4, ... of column c;
   // consecutive threads read consecutive columns of a row (coalesced)
-  const int c = tid & (NB - 1), q = tid >> 6;
-  const T* col = S + (k0 + q) * ld + (int64_t)jb * NB + c;
-  T v[NB / 4];
-#pragma unroll
-  for (int t = 0; t < NB / 4; ++t) v[t] = col[(int64_t)(4 * t) * ld];
   T s = T(0);
 #pragma unroll
   for (int t = 0; t < NB / 4; ++t) s += v[t] * xk[q + 4 * t];
@@ -640,7 +650,9 @@ __global__ void __launch_bounds__(256) k_trsv_bwd(const T* __restrict__ S, int64
   __syncthreads();
   part[q * NB + c] = s;
   __syncthreads();
-  if (tid < NB) b[(int64_t)jb * NB + tid] -= part[tid] + part[NB + tid] + part[2 * NB + tid] + part[3 * NB + tid];
+  if (tid < NB)
+    b[(int64_t)jb * NB + tid] = __ldcg(b + (int64_t)jb * NB + tid) -
+                                (part[tid] + part[NB + tid] + part[2 * NB + tid] + part[3 * NB + tid]);
 }
 
 // Opt the kernels into their dynamic shared memory (once per device and type;
@@ -739,10 +751,11 @@ void dense_cholesky_solve_impl(gbba_handle* h, T* S, int64_t n_pad, T* b, T* x, 
                 b, 1);
   }
   if (side_pending) GBBA_CUDA(cudaStreamWaitEvent(st, h->ev_side, 0));
-  for (int kb = nb - 1; kb >= 0; --kb) {
-    k_trsv_bwd<T><<<kb + 1, 256, sm, st>>>(S, n_pad, kb, Linv_all, b, x);
-    check_launch(h);
-  }
+  // backward substitution: each block row's kernel starts while the previous
+  // one finishes (programmatic dependent launch; the first one waits fully)
+  for (int kb = nb - 1; kb >= 0; --kb)
+    launch_hi(h, kb != nb - 1, k_trsv_bwd<T>, (unsigned)(kb + 1), 256, sm, st, S, n_pad, kb,
+              (const T*)Linv_all, b, x);
 }
 
 template <typename T>

@@ -1161,9 +1161,13 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 // Camera diagonal blocks U_c = sum Jc^T Jc and the preconditioner block
 // S_c = U_c + D_c^2 - sum (W V^-1) W^T (identity on held coordinates), into
 // Mblk, which k_cam_inverse then inverts in place.  One block of kCamWarps
-// (2, 4 or 8: the handle's camera_warps) warps per camera: warp w takes every kCamWarps-th of the camera's
-// observations (lanes over the block's entries, two observations in flight),
-// and the warps' partial blocks are added in warp order.
+// (2, 4 or 8: the handle's camera_warps) warps per camera: warp w takes every
+// kCamWarps-th of the camera's observations.  The warp copies an
+// observation's Jc, W and (W V^-1) (the first 8B values of its record) with
+// coalesced loads into shared memory, as Jc column pairs and 4-wide W and
+// W V^-1 rows, the next observation's copy in flight while it computes; its
+// lanes take the lower triangle's entries.  The warps' partial blocks are
+// added in warp order and written to both triangles.
 template <int B, typename T, int kCamWarps>
 __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* __restrict__ cam_off,
                                                                const uint32_t* __restrict__ cam_obs,
@@ -1175,63 +1179,82 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
                                                                const double* __restrict__ radius, T* __restrict__ U,
                                                                double* __restrict__ Mblk) {
   using R = Rec<B>;
-  constexpr int E = (B * B + 31) / 32;
+  constexpr int NT = B * (B + 1) / 2;       // lower-triangle entries
+  constexpr int E = (NT + 31) / 32;         // per lane
+  constexpr int NV = 8 * B;                 // staged record values: Jc (2B), W (3B), W V^-1 (3B)
+  constexpr int F = (NV + 31) / 32;         // per lane
+  static_assert(R::kJc == 0 && R::kW == 2 * B && R::kWh == 5 * B, "record layout: Jc, W, W V^-1 first");
+  // staged layout: jc[i] = (Jc[0][i], Jc[1][i]), w[i] / wh[i] = row i padded to 4
+  constexpr int kJ = 0, kWr = 2 * B, kWhr = 6 * B, kStage = 10 * B;
+  __shared__ __align__(16) T stage[kCamWarps][kStage];
   __shared__ double part[kCamWarps][2][E * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c = blockIdx.x;
   if (c >= nc) return;
-  double accU[E], accS[E];
+  T* sw = stage[warp];
+  // this lane's staged destinations and its entries (i >= j)
+  int dst[F];
 #pragma unroll
-  for (int e = 0; e < E; ++e) accU[e] = accS[e] = 0.0;
-  if constexpr (sizeof(T) == 4) {
-    // FP32 products and Kahan-compensated FP32 sums (GB300 runs FP64 at a
-    // small fraction of the FP32 rate; a camera sums thousands of terms)
-    float su[E], cu[E], ss[E], cs[E];
+  for (int f = 0; f < F; ++f) {
+    const int v = lane + 32 * f;
+    if (v < 2 * B) dst[f] = kJ + 2 * (v % B) + v / B;
+    else if (v < 5 * B) dst[f] = kWr + 4 * ((v - 2 * B) / 3) + (v - 2 * B) % 3;
+    else if (v < NV) dst[f] = kWhr + 4 * ((v - 5 * B) / 3) + (v - 5 * B) % 3;
+    else dst[f] = -1;
+  }
+  if (lane < B) sw[kWr + 4 * lane + 3] = sw[kWhr + 4 * lane + 3] = T(0);  // row padding
+  int ei[E], ej[E];
 #pragma unroll
-    for (int e = 0; e < E; ++e) su[e] = cu[e] = ss[e] = cs[e] = 0.0f;
-#pragma unroll 2
-    for (uint32_t q = cam_off[c] + warp; q < cam_off[c + 1]; q += kCamWarps) {
-      const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+  for (int e = 0; e < E; ++e) {
+    const int idx = lane + 32 * e;
+    int i = 0;
+    while ((i + 1) * (i + 2) / 2 <= idx) ++i;
+    ei[e] = idx < NT ? i : 0;
+    ej[e] = idx < NT ? idx - i * (i + 1) / 2 : 0;
+  }
+  const uint32_t q0 = cam_off[c] + warp, q1 = cam_off[c + 1];
+  T pre[F];
+  auto fetch = [&](uint32_t q) {
+    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
 #pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const int idx = lane + 32 * e;
-        if (idx < B * B) {
-          const int i = idx / B, j = idx % B;
-          const float u = r[R::kJc + i] * r[R::kJc + j] + r[R::kJc + B + i] * r[R::kJc + B + j];
-          const float w = r[R::kWh + 3 * i] * r[R::kW + 3 * j] + r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
-                          r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
-          kahan_add(su[e], cu[e], u);
-          kahan_add(ss[e], cs[e], u - w);
-        }
-      }
-    }
+    for (int f = 0; f < F; ++f) pre[f] = dst[f] >= 0 ? r[lane + 32 * f] : T(0);
+  };
+  if (q0 < q1) fetch(q0);
+  // FP32: FP32 products and Kahan-compensated FP32 sums (GB300 runs FP64 at
+  // a small fraction of the FP32 rate; a camera sums thousands of terms)
+  using A = T;
+  A su[E], cu[E], ss[E], cs[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) su[e] = cu[e] = ss[e] = cs[e] = A(0);
+  for (uint32_t q = q0; q < q1; q += kCamWarps) {
+    __syncwarp();
+#pragma unroll
+    for (int f = 0; f < F; ++f)
+      if (dst[f] >= 0) sw[dst[f]] = pre[f];
+    __syncwarp();
+    if (q + kCamWarps < q1) fetch(q + kCamWarps);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      accU[e] = (double)su[e] - (double)cu[e];
-      accS[e] = (double)ss[e] - (double)cs[e];
-    }
-  } else {
-    for (uint32_t q = cam_off[c] + warp; q < cam_off[c + 1]; q += kCamWarps) {
-      const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const int idx = lane + 32 * e;
-        if (idx < B * B) {
-          const int i = idx / B, j = idx % B;
-          const double u = (double)r[R::kJc + i] * r[R::kJc + j] + (double)r[R::kJc + B + i] * r[R::kJc + B + j];
-          const double w = (double)r[R::kWh + 3 * i] * r[R::kW + 3 * j] +
-                           (double)r[R::kWh + 3 * i + 1] * r[R::kW + 3 * j + 1] +
-                           (double)r[R::kWh + 3 * i + 2] * r[R::kW + 3 * j + 2];
-          accU[e] += u;
-          accS[e] += u - w;
-        }
+      if (lane + 32 * e >= NT) continue;
+      const int i = ei[e], j = ej[e];
+      const T a0 = sw[kJ + 2 * i], a1 = sw[kJ + 2 * i + 1], b0 = sw[kJ + 2 * j], b1 = sw[kJ + 2 * j + 1];
+      const T* hi = sw + kWhr + 4 * i;
+      const T* wj = sw + kWr + 4 * j;
+      const A u = a0 * b0 + a1 * b1;
+      const A w = hi[0] * wj[0] + hi[1] * wj[1] + hi[2] * wj[2];
+      if constexpr (sizeof(T) == 4) {
+        kahan_add(su[e], cu[e], u);
+        kahan_add(ss[e], cs[e], u - w);
+      } else {
+        su[e] += u;
+        ss[e] += u - w;
       }
     }
   }
 #pragma unroll
   for (int e = 0; e < E; ++e) {
-    part[warp][0][lane + 32 * e] = accU[e];
-    part[warp][1][lane + 32 * e] = accS[e];
+    part[warp][0][lane + 32 * e] = (double)su[e] - (double)cu[e];
+    part[warp][1][lane + 32 * e] = (double)ss[e] - (double)cs[e];
   }
   __syncthreads();
   if (warp != 0) return;
@@ -1239,20 +1262,20 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
 #pragma unroll
   for (int e = 0; e < E; ++e) {
     const int idx = lane + 32 * e;
-    if (idx >= B * B) continue;
+    if (idx >= NT) continue;
     double u = 0.0, v = 0.0;
 #pragma unroll
     for (int w = 0; w < kCamWarps; ++w) {  // warp order: fixed
       u += part[w][0][idx];
       v += part[w][1][idx];
     }
-    const int i = idx / B, j = idx % B;
-    U[c * B * B + idx] = (T)u;
+    const int i = ei[e], j = ej[e];
     const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, i);
     const int cj = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, j);
     if (i == j && ci >= 0) v += diag_c[ci] / rad;
     if (ci < 0 || cj < 0) v = (i == j) ? 1.0 : 0.0;
-    Mblk[c * B * B + idx] = v;
+    U[c * B * B + i * B + j] = U[c * B * B + j * B + i] = (T)u;
+    Mblk[c * B * B + i * B + j] = Mblk[c * B * B + j * B + i] = v;
   }
 }
 
@@ -1302,67 +1325,135 @@ __global__ void __launch_bounds__(128) k_cam_inverse(double* __restrict__ Minv, 
 }
 
 
-// y_p = V_p^-1 sum_{o in p} W_o^T x_c(o); one warp per point.
+// A camera's B operand values (compute type) into v: vector loads where the
+// row's size allows them.
 template <int B, typename T>
-__global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ cam,
-                                                    const T* __restrict__ rec, const T* __restrict__ Vinv,
-                                                    const int32_t* __restrict__ ext_col,
-                                                    const int32_t* __restrict__ intr_col,
-                                                    const int32_t* __restrict__ cam_group, int K, int64_t np,
-                                                    const double* __restrict__ x, double* __restrict__ y,
-                                                    const float* __restrict__ xf, float* __restrict__ yf,
-                                                    const PcgState* __restrict__ ps, int reset_period) {
-  using R = Rec<B>;
-  const int lane = threadIdx.x & 31;
-  const int64_t p = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-  if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
-  if (p >= np) return;
-  if constexpr (sizeof(T) == 4) {
-    // FP32 operand copy in, FP32 products and sums (a point has few
-    // observations), FP32 point temporaries out
-    float t[3] = {0.0f, 0.0f, 0.0f};
-    for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
-      const T* r = rec + (int64_t)o * R::kSize;
-      const uint32_t c = cam[o];
+__device__ __forceinline__ void load_cam_row(const T* __restrict__ p, T v[B]) {
+  constexpr int bytes = B * (int)sizeof(T);
+  if constexpr (bytes % 16 == 0) {
+    constexpr int P = 16 / (int)sizeof(T);
 #pragma unroll
-      for (int i = 0; i < B; ++i) {
-        const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
-        if (ci < 0) continue;
-        const float xi = xf[ci];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] += r[R::kW + 3 * i + j] * xi;
+    for (int i = 0; i < B; i += P) {
+      if constexpr (P == 4) {
+        const float4 q = *reinterpret_cast<const float4*>(p + i);
+        v[i] = q.x;
+        v[i + 1] = q.y;
+        v[i + 2] = q.z;
+        v[i + 3] = q.w;
+      } else {
+        const double2 q = *reinterpret_cast<const double2*>(p + i);
+        v[i] = q.x;
+        v[i + 1] = q.y;
       }
     }
+  } else if constexpr (bytes % 8 == 0 && sizeof(T) == 4) {
 #pragma unroll
-    for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
-    if (lane < 3) {
-      const T* v = Vinv + 6 * p;
-      const float row[3][3] = {{v[0], v[1], v[2]}, {v[1], v[3], v[4]}, {v[2], v[4], v[5]}};
-      yf[3 * p + lane] = row[lane][0] * t[0] + row[lane][1] * t[1] + row[lane][2] * t[2];
+    for (int i = 0; i < B; i += 2) {
+      const float2 q = *reinterpret_cast<const float2*>(p + i);
+      v[i] = q.x;
+      v[i + 1] = q.y;
     }
-    return;
+  } else {
+#pragma unroll
+    for (int i = 0; i < B; ++i) v[i] = p[i];
   }
-  double t[3] = {0.0, 0.0, 0.0};
-  for (uint32_t o = pt_off[p] + lane; o < pt_off[p + 1]; o += 32) {
-    const T* r = rec + (int64_t)o * R::kSize;
-    const uint32_t c = cam[o];
+}
+
+// y_p = V_p^-1 sum_{o in p} W_o^T x_c(o), one warp per point group (the
+// groups of k_pt_groups: a packed group holds one observation per lane, a
+// group of one point is taken 32 observations at a time).  A group's
+// records are consecutive: the warp copies their W blocks (3B values each)
+// into shared memory with coalesced loads, and each lane reads its own
+// observation's block there and its camera's operand row from xc (the
+// operand gathered per camera by k_pcg_gather_cam).  A grid of at most a few
+// waves strides over the groups, so that a launch after the solve has
+// stopped costs one flag read per block.
+template <int B, typename T>
+__global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__ pt_off,
+                                                    const uint32_t* __restrict__ pt,
+                                                    const uint32_t* __restrict__ pt_grp, int64_t n_groups,
+                                                    const uint32_t* __restrict__ cam,
+                                                    const T* __restrict__ rec, const T* __restrict__ Vinv,
+                                                    const T* __restrict__ xc, T* __restrict__ yt,
+                                                    const PcgState* __restrict__ ps, int reset_period) {
+  using R = Rec<B>;
+  // FP32 path: FP32 operand and products and sums (a point has few
+  // observations), FP32 point temporaries out
+  constexpr int NW = 3 * B, kPitch = NW + 1;  // odd pitch: no bank conflicts
+  __shared__ T wst[4][32 * kPitch];
+  const int lane = threadIdx.x & 31;
+  T* sw = wst[(threadIdx.x >> 5) & 3];
+  if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
+  const int64_t nw = (gridDim.x * (int64_t)blockDim.x) >> 5;
+  for (int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; w < n_groups; w += nw) {
+    const uint32_t p0 = pt_grp[w], p1 = pt_grp[w + 1];
+    const uint32_t o0 = pt_off[p0], o1 = pt_off[p1];
+    T t[3] = {T(0), T(0), T(0)};
+    for (uint32_t q0 = o0; q0 < o1; q0 += 32) {
+      const int total = (int)min(32u, o1 - q0) * NW;
+      const T* base = rec + (int64_t)q0 * R::kSize + R::kW;
+      __syncwarp();
+      for (int t0 = 0; t0 < total; t0 += 128) {
+        T v[4];
 #pragma unroll
-    for (int i = 0; i < B; ++i) {
-      const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
-      if (ci < 0) continue;
-      const double xi = x[ci];
+        for (int u = 0; u < 4; ++u) {
+          const int e = t0 + 32 * u + lane;
+          const int k = e / NW;
+          if (e < total) v[u] = base[(int64_t)k * R::kSize + (e - k * NW)];
+        }
 #pragma unroll
-      for (int j = 0; j < 3; ++j) t[j] += (double)r[R::kW + 3 * i + j] * xi;
+        for (int u = 0; u < 4; ++u) {
+          const int e = t0 + 32 * u + lane;
+          const int k = e / NW;
+          if (e < total) sw[k * kPitch + (e - k * NW)] = v[u];
+        }
+      }
+      __syncwarp();
+      const uint32_t o = q0 + lane;
+      if (o < o1) {
+        T xr[B];
+        load_cam_row<B, T>(xc + (int64_t)cam[o] * B, xr);
+        const T* wr = sw + lane * kPitch;
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+#pragma unroll
+          for (int j = 0; j < 3; ++j) t[j] += wr[3 * i + j] * xr[i];
+        }
+      }
     }
-  }
+    uint32_t p;
+    if (p1 - p0 == 1) {
 #pragma unroll
-  for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
-  if (lane < 3) {
-    const T* v = Vinv + 6 * p;
-    const double row[3][3] = {{(double)v[0], (double)v[1], (double)v[2]},
-                              {(double)v[1], (double)v[3], (double)v[4]},
-                              {(double)v[2], (double)v[4], (double)v[5]}};
-    y[3 * p + lane] = row[lane][0] * t[0] + row[lane][1] * t[1] + row[lane][2] * t[2];
+      for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
+      p = p0;
+      if (lane != 0) continue;
+    } else {
+      // packed: a segmented inclusive scan over each point's lanes; the
+      // point's last lane holds its sum
+      const uint32_t o = o0 + lane;
+      const bool valid = o < o1;
+      int head = lane, tail = lane;
+      p = 0;
+      if (valid) {
+        p = pt[o];
+        head = (int)(pt_off[p] - o0);
+        tail = (int)(pt_off[p + 1] - o0) - 1;
+      }
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const bool take = lane - d >= head;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const T u = __shfl_up_sync(0xffffffffu, t[j], d);
+          if (take) t[j] += u;
+        }
+      }
+      if (!valid || lane != tail) continue;
+    }
+    const T* v = Vinv + 6 * (int64_t)p;
+    const T row[3][3] = {{v[0], v[1], v[2]}, {v[1], v[3], v[4]}, {v[2], v[4], v[5]}};
+#pragma unroll
+    for (int j = 0; j < 3; ++j) yt[3 * (int64_t)p + j] = row[j][0] * t[0] + row[j][1] * t[1] + row[j][2] * t[2];
   }
 }
 
@@ -1389,26 +1480,47 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
   double acc[B];
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = 0.0;
-  const uint32_t q0 = cam_off[c] + warp * 32 + lane, q1 = cam_off[c + 1];
+  const uint32_t qb = cam_off[c], q1 = cam_off[c + 1];
   if constexpr (sizeof(T) == 4) {
-    // FP32 products, Kahan-compensated FP32 sums per lane (a camera has
-    // thousands of observations), FP64 from the lane sums on
+    // The warp takes its camera's observations 32 at a time, one per lane:
+    // it copies the 32 records' W blocks (3B values each) into shared memory
+    // with coalesced loads, record by record, and each lane then reads its
+    // own.  FP32 products, Kahan-compensated FP32 sums per lane (a camera
+    // has thousands of observations), FP64 from the lane sums on.
+    constexpr int NW = 3 * B, FW = (NW + 31) / 32, kPitch = NW + 1;  // odd pitch: no bank conflicts
+    __shared__ float wst[kCamWarps][32 * kPitch];
+    float* sw = wst[warp];
     float sa[B], ca[B];
 #pragma unroll
     for (int i = 0; i < B; ++i) sa[i] = ca[i] = 0.0f;
-    for (uint32_t q = q0; q < q1; q += kCamWarps * 32) {
-      const uint32_t o = cam_obs[q];
-      const T* r = rec + (int64_t)o * R::kSize;
+    for (uint32_t q0 = qb + warp * 32; q0 < q1; q0 += kCamWarps * 32) {
+      const uint32_t q = q0 + lane;
+      const bool valid = q < q1;
+      const uint32_t o = valid ? cam_obs[q] : 0u;
+      const int nv = (int)min(32u, q1 - q0);
+      __syncwarp();
+      for (int k = 0; k < nv; ++k) {
+        const T* r = rec + (int64_t)__shfl_sync(0xffffffffu, o, k) * R::kSize + R::kW;
+#pragma unroll
+        for (int f = 0; f < FW; ++f) {
+          const int v = lane + 32 * f;
+          if (v < NW) sw[k * kPitch + v] = r[v];
+        }
+      }
+      __syncwarp();
+      if (!valid) continue;
+      const float* w = sw + lane * kPitch;
       const float* yp = yf + 3 * (int64_t)pt[o];
       const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
 #pragma unroll
-      for (int i = 0; i < B; ++i)
-        kahan_add(sa[i], ca[i], -(r[R::kW + 3 * i] * y0 + r[R::kW + 3 * i + 1] * y1 + r[R::kW + 3 * i + 2] * y2));
+      for (int i = 0; i < B; ++i) kahan_add(sa[i], ca[i], -(w[3 * i] * y0 + w[3 * i + 1] * y1 + w[3 * i + 2] * y2));
     }
 #pragma unroll
     for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
   } else {
-    for (uint32_t q = q0; q < q1; q += kCamWarps * 32) {
+    // FP64: one observation per lane straight from its record (the FP64
+    // arithmetic bounds this path)
+    for (uint32_t q = qb + warp * 32 + lane; q < q1; q += kCamWarps * 32) {
       const uint32_t o = cam_obs[q];
       const T* r = rec + (int64_t)o * R::kSize;
       const double* yp = y + 3 * (int64_t)pt[o];
@@ -1471,13 +1583,22 @@ __device__ __forceinline__ double sum_partials(const double* __restrict__ part, 
   return block_sum256(v, sh);
 }
 
-// FP32 copy of the operand of an implicit product (mixed path); a no-op on
-// the iterations where that product does not run.
-__global__ void __launch_bounds__(256) k_pcg_to_float(const double* __restrict__ x, float* __restrict__ xf, int64_t n,
-                                                      const PcgState* __restrict__ ps, int reset_period) {
+// The operand of an implicit product gathered per camera: B values in the
+// compute type, 0 on held columns (k_spmv_point reads a camera's row as one
+// contiguous vector); a no-op on the iterations where that product does not
+// run.
+template <int B, typename T>
+__global__ void __launch_bounds__(256) k_pcg_gather_cam(const double* __restrict__ x, T* __restrict__ xc,
+                                                        const int32_t* __restrict__ ext_col,
+                                                        const int32_t* __restrict__ intr_col,
+                                                        const int32_t* __restrict__ cam_group, int K, int64_t nc,
+                                                        const PcgState* __restrict__ ps, int reset_period) {
   if (ps->done || (reset_period > 0 && ps->it % reset_period != 0)) return;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    xf[i] = (float)x[i];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nc * B; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / B;
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, (int)(e - c * B));
+    xc[e] = ci >= 0 ? (T)x[ci] : T(0);
+  }
 }
 
 // b = rhs (widened), x = 0, r = b; partials of |b|^2.
@@ -2091,7 +2212,8 @@ struct Solve {
   double *pose = nullptr, *pose2 = nullptr;  // FP64 poses of ext / ext2 (mixed path)
   float *ext_f = nullptr, *intr_f = nullptr, *pts_f = nullptr;  // FP32 copies of ext, intr, pts (mixed path)
   float4* rcache = nullptr;  // mixed path: residual cache, [2][no] (current parameters, candidate)
-  float *pcg_xf = nullptr, *pcg_yf = nullptr;  // mixed path: FP32 copies of the PCG operand and point temporaries
+  float* pcg_yf = nullptr;  // mixed path: FP32 point temporaries of the implicit product
+  char* pcg_xc = nullptr;   // the implicit product's operand per camera (B values, compute type)
   float *scale_cf = nullptr, *scale_pf = nullptr;               // FP32 copies of the Jacobi scales
   uint32_t *pt_grp = nullptr, *pgrp_cnt = nullptr, *pgrp_off = nullptr;  // point groups (k_pt_groups)
   int64_t n_pgrp = 0;
@@ -2426,7 +2548,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     // PCG vectors (x, r, z, p, q, b), point temporaries, camera blocks
     p1.take<double>(6 * n_pcg);
     p1.take<double>(3 * np);
-    p1.take<float>(tsize == 4 && n_pcg ? n_pcg : 0);
+    p1.take<char>((size_t)(n_pcg ? nc : 0) * B * tsize);
     p1.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
     p1.take<double>((size_t)nc * B * B);
     p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
@@ -2458,9 +2580,10 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     s.pcg_q = A.take<double>(n_pcg);
     s.pcg_b = A.take<double>(n_pcg);
     s.pcg_y = A.take<double>(3 * np);
-    s.pcg_xf = A.take<float>(tsize == 4 && n_pcg ? n_pcg : 0);
+    s.pcg_xc = A.take<char>((size_t)(n_pcg ? nc : 0) * B * tsize);
     s.pcg_yf = A.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
-    if (!(tsize == 4 && n_pcg)) s.pcg_xf = s.pcg_yf = nullptr;
+    if (!n_pcg) s.pcg_xc = nullptr;
+    if (!(tsize == 4 && n_pcg)) s.pcg_yf = nullptr;
     s.pcg_minv = A.take<double>((size_t)nc * B * B);
     s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
     s.pcg_part_n = std::max<int64_t>(4096, nc + 1);
@@ -2611,6 +2734,9 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   const int nbv = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), s.nb_pcg));
   const int nbc = (int)std::max<int64_t>(1, ceil_div(s.nc, 256));      // k_pcg_precond blocks
   const int nbs = (int)std::max<int64_t>(1, s.nc);  // k_spmv_camera blocks (one per camera)
+  // k_spmv_point blocks: at most 8 waves of 16 blocks per SM, striding over the point groups
+  const int nbp = (int)std::max<int64_t>(1, std::min<int64_t>(s.nb_pgrp, (int64_t)h->sm_count * 16 * 8));
+  const int nbx = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(s.nc * B, 256), 1024));  // k_pcg_gather_cam
   const int period = std::max(1, o->refinement_interval);
   PcgState* ps = s.pcg_state;
   double* part_a = s.pcg_part;                 // r.z, then p.q
@@ -2621,13 +2747,12 @@ static void pcg_solve(Solve& s, const gbba_options* o, gbba_summary* sum) {
   check_launch(h);
   auto spmv = [&](const double* x, double* out, double* part, int reset) {
     if (s.np > 0) {
-      if constexpr (sizeof(T) == 4) {
-        k_pcg_to_float<<<nbv, 256, 0, st>>>(x, s.pcg_xf, n, ps, reset);
-        check_launch(h);
-      }
-      k_spmv_point<B, T><<<(unsigned)ceil_div(s.np * 32, 128), 128, 0, st>>>(
-          s.pt_off, s.cam, (const T*)s.rec, (const T*)s.Vinv, s.ext_col, s.intr_col, s.cam_group, s.k, s.np, x, s.pcg_y,
-          s.pcg_xf, s.pcg_yf, ps, reset);
+      k_pcg_gather_cam<B, T><<<nbx, 256, 0, st>>>(x, (T*)s.pcg_xc, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc,
+                                                  ps, reset);
+      check_launch(h);
+      k_spmv_point<B, T><<<nbp, 128, 0, st>>>(s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, (const T*)s.rec,
+                                              (const T*)s.Vinv, (const T*)s.pcg_xc,
+                                              sizeof(T) == 4 ? (T*)s.pcg_yf : (T*)s.pcg_y, ps, reset);
       check_launch(h);
     }
     auto cam = [&](auto warps) {

@@ -232,19 +232,22 @@ def large_scene(seed=5, **kw):
 
 
 def local_problem(rng, num_cameras, num_points, model=abi.BROWN_T2, sigma=0.5, rot_sigma=0.02,
-                  t_sigma=0.05, x_sigma=0.05, radius=8.0, extent=2.0):
-    """One local-BA window: cameras on an arc, one shared intrinsic group."""
+                  t_sigma=0.05, x_sigma=0.05, radius=8.0, extent=2.0, num_groups=1):
+    """One local-BA window: cameras on an arc sharing one intrinsic group, or
+    `num_groups` groups assigned to the cameras round robin (camera c uses
+    group c % num_groups)."""
     ang = np.linspace(-0.6, 0.6, num_cameras) + rng.uniform(-0.05, 0.05, num_cameras)
     centers = radius * np.stack([np.sin(ang), rng.uniform(-0.1, 0.1, num_cameras), np.cos(ang)], -1)
     R, t = _cameras_facing_origin(centers)
     ext_true = np.concatenate([rotation_to_angle_axis(R), t], 1)
     k = abi.MODEL_K[model]
-    intr_true = np.zeros((1, k))
-    intr_true[0, :3] = (rng.uniform(900, 1100), PP[0], PP[1])
-    if k >= 6:
-        intr_true[0, 3:6] = rng.normal(0, (0.05, 0.01, 0.01))
-    if k == 8:
-        intr_true[0, 6:8] = rng.normal(0, 0.002, 2)
+    intr_true = np.zeros((num_groups, k))
+    for g in range(num_groups):
+        intr_true[g, :3] = (rng.uniform(900, 1100), PP[0], PP[1])
+        if k >= 6:
+            intr_true[g, 3:6] = rng.normal(0, (0.05, 0.01, 0.01))
+        if k == 8:
+            intr_true[g, 6:8] = rng.normal(0, 0.002, 2)
     X_true = rng.uniform(-extent, extent, size=(num_points, 3))
     views = rng.integers(2, num_cameras + 1, num_points)
     pt = np.repeat(np.arange(num_points), views)
@@ -255,11 +258,14 @@ def local_problem(rng, num_cameras, num_points, model=abi.BROWN_T2, sigma=0.5, r
     cam = (np.repeat(start, views) + j * np.repeat(step, views)) % num_cameras
     order = np.lexsort((cam, pt))
     pt, cam = pt[order], cam[order]
-    intr_idx = np.zeros_like(cam)
+    intr_idx = cam % num_groups
     obs, _, _ = _observe(rng, model, ext_true, intr_true, X_true, cam, intr_idx, pt, sigma)
     ext, pts = _perturb(rng, ext_true.copy(), X_true, rot_sigma, t_sigma, x_sigma, fixed_cams=(0,))
     intr = intr_true.copy()
-    intr[0, 0] *= 1 + rng.normal(0, 0.002)
+    if num_groups == 1:
+        intr[0, 0] *= 1 + rng.normal(0, 0.002)
+    else:
+        intr[:, 0] *= 1 + rng.normal(0, 0.002, num_groups)
     cam_const = np.zeros(num_cameras, np.uint8)
     cam_const[0] = 1
     return _scene_dict(model, ext, intr, pts, obs, cam, intr_idx, pt, camera_constant=cam_const)

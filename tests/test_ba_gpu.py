@@ -506,6 +506,40 @@ def test_batched_solves_are_bitwise_repeatable(handle, abi, scenes, precision):
                 np.testing.assert_array_equal(a[k], b[k])
 
 
+def test_batched_multi_group_windows(handle, abi, scenes):
+    """Windows with several intrinsic groups take the general Schur build
+    (observation pairs for every column, no per-point intrinsic sums); a
+    group shared by several cameras of one point tightens the fixed-point
+    budget.  FP64 matches the individual solves, mixed reaches the FP64 cost,
+    and both repeat bit for bit."""
+    rng = np.random.default_rng(211)
+    shapes = [(8, 300, 2), (12, 400, 3), (6, 250, 6), (10, 500, 4), (16, 600, 2)]
+    probs = []
+    for c, n, g in shapes:
+        p = scenes.local_problem(rng, c, n, num_groups=g)
+        p["camera_constant"][1] = 1
+        probs.append(p)
+    o64 = abi.default_options(max_num_iterations=100)
+    st, bs, _ = batched_solve(handle, abi, probs, o64)
+    assert st == abi.SUCCESS
+    for p, s in zip(probs, bs):
+        si, _ = solve(handle, abi, p, o64)
+        assert s.usable and si.usable
+        assert abs(s.final_cost - si.final_cost) <= 1e-6 * si.final_cost, (s.final_cost, si.final_cost)
+    om = abi.default_options(max_num_iterations=200, precision=abi.PRECISION_MIXED)
+    om.function_tolerance = 1e-8
+    om.fp64_polish_iterations = 0
+    runs = [batched_solve(handle, abi, probs, om) for _ in range(2)]
+    for st_m, _, _ in runs:
+        assert st_m == abi.SUCCESS
+    for s64, a, b in zip(bs, runs[0][1], runs[1][1]):
+        assert a.final_cost <= s64.final_cost * (1 + 1e-6), (a.final_cost, s64.final_cost)
+        assert a.final_cost == b.final_cost and a.num_iterations == b.num_iterations
+    for a, b in zip(runs[0][2], runs[1][2]):
+        for k in ("extrinsics", "intrinsics", "points"):
+            np.testing.assert_array_equal(a[k], b[k])
+
+
 def test_batched_rejects_oversized_window(handle, abi, scenes):
     probs = local_problems(scenes, 2, seed=113)
     rng = np.random.default_rng(5)
