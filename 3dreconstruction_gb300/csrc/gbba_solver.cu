@@ -1078,15 +1078,52 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
   T acc[B], nrm[B], grd[B];
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = nrm[i] = grd[i] = T(0);
-  for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
-    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
-    const T r0 = r[R::kR], r1 = r[R::kR + 1];
+  if constexpr (sizeof(T) == 4) {
+    // The warp takes observations 32 at a time (thread t still sums
+    // observations t, t + 256, ...): it copies the 32 records' Jc, q and r
+    // (3B + 2 values) into shared memory, record by record with coalesced
+    // loads, and each lane reads its own there.
+    constexpr int NV = 3 * B + 2, FW = (NV + 31) / 32, kPitch = NV + 1;  // odd pitch: no bank conflicts
+    __shared__ float rs[kRhsThreads / 32][32 * kPitch];
+    float* sw = rs[warp];
+    const uint32_t q1 = cam_off[c + 1];
+    for (uint32_t q0 = cam_off[c] + warp * 32; q0 < q1; q0 += kRhsThreads) {
+      const uint32_t q = q0 + lane;
+      const bool valid = q < q1;
+      const uint32_t o = valid ? cam_obs[q] : 0u;
+      const int nv = (int)min(32u, q1 - q0);
+      __syncwarp();
+      for (int k = 0; k < nv; ++k) {
+        const T* r = rec + (int64_t)__shfl_sync(0xffffffffu, o, k) * R::kSize;
 #pragma unroll
-    for (int i = 0; i < B; ++i) {
-      const T j0 = r[R::kJc + i], j1 = r[R::kJc + B + i];
-      acc[i] += r[R::kQ + i];
-      nrm[i] += j0 * j0 + j1 * j1;
-      grd[i] += j0 * r0 + j1 * r1;
+        for (int f = 0; f < FW; ++f) {
+          const int j = lane + 32 * f;
+          if (j < NV) sw[k * kPitch + j] = r[j < 2 * B ? R::kJc + j : j < 3 * B ? R::kQ + (j - 2 * B) : R::kR + (j - 3 * B)];
+        }
+      }
+      __syncwarp();
+      if (!valid) continue;
+      const float* v = sw + lane * kPitch;  // Jc rows [0, 2B), q [2B, 3B), r [3B, 3B + 2)
+      const T r0 = v[3 * B], r1 = v[3 * B + 1];
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T j0 = v[i], j1 = v[B + i];
+        acc[i] += v[2 * B + i];
+        nrm[i] += j0 * j0 + j1 * j1;
+        grd[i] += j0 * r0 + j1 * r1;
+      }
+    }
+  } else {
+    for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
+      const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+      const T r0 = r[R::kR], r1 = r[R::kR + 1];
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T j0 = r[R::kJc + i], j1 = r[R::kJc + B + i];
+        acc[i] += r[R::kQ + i];
+        nrm[i] += j0 * j0 + j1 * j1;
+        grd[i] += j0 * r0 + j1 * r1;
+      }
     }
   }
 #pragma unroll
@@ -1601,6 +1638,20 @@ __global__ void __launch_bounds__(256) k_pcg_gather_cam(const double* __restrict
   }
 }
 
+// The camera step z gathered per camera: B values, 0 on held columns (the
+// back substitution reads a camera's row as one contiguous vector).
+template <int B, typename T>
+__global__ void __launch_bounds__(256) k_gather_cam_rows(const T* __restrict__ z, T* __restrict__ zc,
+                                                         const int32_t* __restrict__ ext_col,
+                                                         const int32_t* __restrict__ intr_col,
+                                                         const int32_t* __restrict__ cam_group, int K, int64_t nc) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nc * B; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / B;
+    const int ci = cam_col(ext_col, intr_col, cam_group, K, (uint32_t)c, (int)(e - c * B));
+    zc[e] = ci >= 0 ? z[ci] : T(0);
+  }
+}
+
 // b = rhs (widened), x = 0, r = b; partials of |b|^2.
 template <typename T>
 __global__ void __launch_bounds__(256) k_pcg_init(const T* __restrict__ rhs, double* __restrict__ b,
@@ -1843,59 +1894,64 @@ __global__ void k_cam_groups(const uint32_t* cam, const uint32_t* icam, int64_t 
     atomicAdd(&cam_hist[c], 1u);
   }
 }
-__global__ void k_cam_scatter(const uint32_t* cam, int64_t no, const uint32_t* off, uint32_t* fill, uint32_t* out) {
-  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < no; o += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t c = cam[o];
-    out[off[c] + atomicAdd(&fill[c], 1u)] = (uint32_t)o;
-  }
-}
 
 // Back substitution from the observation records (no projection is
-// recomputed): one warp per point,
+// recomputed): one warp per point group (k_pt_groups),
 //   y_p = V^-1 (g_p - sum E'F z), step = -(z, y), m = J step,
 //   model_cost_change += -m.(r + m/2), candidate points.
+// z is read per camera (zc: B values per camera, k_gather_cam_rows).  A
+// packed group's records are consecutive: the warp copies their Jc, Jp and r
+// (2B + 8 values each) into shared memory with coalesced loads, and each lane
+// reads its own there.
 template <int B, typename T>
 __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ pt,
                                                      const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                      const uint32_t* __restrict__ cam,
-                                                     const int32_t* __restrict__ ext_col,
-                                                     const int32_t* __restrict__ intr_col,
-                                                     const int32_t* __restrict__ cam_group, int K,
-                                                     const T* __restrict__ rec, const T* __restrict__ z,
+                                                     const T* __restrict__ rec, const T* __restrict__ zc,
                                                      const T* __restrict__ Vinv, const T* __restrict__ gp,
                                                      const double* __restrict__ scale_p, const double* __restrict__ pts,
                                                      double* __restrict__ pts_new, double* __restrict__ part_mcc,
                                                      double* __restrict__ part_step, int* __restrict__ flag) {
   using R = Rec<B>;
+  static_assert(R::kJc == 0 && R::kR == R::kJp + 6 && R::kSize == R::kR + 2, "record layout: Jc first, Jp and r last");
+  constexpr int NV = 2 * B + 8, kPitch = NV + 1;  // staged values; odd pitch: no bank conflicts
+  __shared__ T rst[4][32 * kPitch];
   __shared__ double smcc[4], sstep[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   double mcc = 0.0, stp = 0.0;
+  // one observation's values: Jc rows, Jp rows (6) and r (2)
+  struct View {
+    const T* jc;
+    const T* jp;
+  };
   // F z of one observation: the camera block's part of J step
-  auto fz = [&](const T* r, uint32_t c, T& f0, T& f1) {
+  auto fz = [&](const View& v, uint32_t c, T& f0, T& f1) {
+    T zr[B];
+    load_cam_row<B, T>(zc + (int64_t)c * B, zr);
     f0 = T(0);
     f1 = T(0);
 #pragma unroll
     for (int i = 0; i < B; ++i) {
-      const int ci = cam_col(ext_col, intr_col, cam_group, K, c, i);
-      const T zi = ci >= 0 ? z[ci] : T(0);
-      f0 += r[R::kJc + i] * zi;
-      f1 += r[R::kJc + B + i] * zi;
+      f0 += v.jc[i] * zr[i];
+      f1 += v.jc[B + i] * zr[i];
     }
   };
-  // model cost change of one observation, m = -(F z + E y): m in the compute
-  // type (the Jacobian's own precision), -m.(r + m/2) in FP64
-  auto obs_mcc = [&](const T* r, uint32_t c, const T y[3]) {
-    T f0, f1;
-    fz(r, c, f0, f1);
+  // model cost change of one observation from its F z, m = -(F z + E y): m
+  // in the compute type (the Jacobian's own precision), -m.(r + m/2) in FP64
+  auto obs_mcc = [&](const View& v, T f0, T f1, const T y[3]) {
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      f0 += r[R::kJp + j] * y[j];
-      f1 += r[R::kJp + 3 + j] * y[j];
+      f0 += v.jp[j] * y[j];
+      f1 += v.jp[3 + j] * y[j];
     }
     const double m0 = -(double)f0, m1 = -(double)f1;
-    const double r0 = (double)r[R::kR], r1 = (double)r[R::kR + 1];
+    const double r0 = (double)v.jp[6], r1 = (double)v.jp[7];
     return -(m0 * (r0 + m0 / 2.0) + m1 * (r1 + m1 / 2.0));
+  };
+  auto rec_view = [&](uint32_t o) -> View {
+    const T* r = rec + (int64_t)o * R::kSize;
+    return {r + R::kJc, r + R::kJp};
   };
   // y_p = V^-1 (g_p - E^T F z) and the candidate point
   auto point_step = [&](uint32_t p, const T t[3], T y[3]) {
@@ -1910,21 +1966,39 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
     const uint32_t o0 = pt_off[p0], o1 = pt_off[p1];
     if (p1 - p0 > 1 || (o1 - o0 >= 1 && o1 - o0 <= 32)) {
       // packed: lane i holds observation o0 + i
+      T* sr = rst[warp];
+      const int total = (int)(o1 - o0) * NV;
+      const T* base = rec + (int64_t)o0 * R::kSize;
+      for (int e0 = 0; e0 < total; e0 += 128) {
+        T v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + 32 * u + lane;
+          const int k = e / NV, j = e - k * NV;
+          if (e < total) v[u] = base[(int64_t)k * R::kSize + (j < 2 * B ? R::kJc + j : R::kJp + (j - 2 * B))];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = e0 + 32 * u + lane;
+          const int k = e / NV, j = e - k * NV;
+          if (e < total) sr[k * kPitch + j] = v[u];
+        }
+      }
+      __syncwarp();
       const uint32_t o = o0 + lane;
       const bool valid = o < o1;
+      const View vw{sr + lane * kPitch, sr + lane * kPitch + 2 * B};
       T t[3] = {T(0), T(0), T(0)};
-      uint32_t p = 0, c = 0;
+      T f0 = T(0), f1 = T(0);
+      uint32_t p = 0;
       int head = lane, tail = lane;
-      const T* r = rec + (int64_t)o * R::kSize;
       if (valid) {
-        c = cam[o];
         p = pt[o];
         head = (int)(pt_off[p] - o0);
         tail = (int)(pt_off[p + 1] - o0) - 1;
-        T f0, f1;
-        fz(r, c, f0, f1);
+        fz(vw, cam[o], f0, f1);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] = r[R::kJp + j] * f0 + r[R::kJp + 3 + j] * f1;
+        for (int j = 0; j < 3; ++j) t[j] = vw.jp[j] * f0 + vw.jp[3 + j] * f1;
       }
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
@@ -1940,7 +2014,7 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
       if (valid) {
         T y[3];
         point_step(p, t, y);
-        mcc = obs_mcc(r, c, y);
+        mcc = obs_mcc(vw, f0, f1, y);
         if (lane == head) {
           if (!isfinite(y[0]) || !isfinite(y[1]) || !isfinite(y[2])) atomicExch(flag, 3);
 #pragma unroll
@@ -1956,11 +2030,11 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
       const uint32_t p = p0;
       T t[3] = {T(0), T(0), T(0)};
       for (uint32_t o = o0 + lane; o < o1; o += 32) {
-        const T* r = rec + (int64_t)o * R::kSize;
+        const View vw = rec_view(o);
         T f0, f1;
-        fz(r, cam[o], f0, f1);
+        fz(vw, cam[o], f0, f1);
 #pragma unroll
-        for (int j = 0; j < 3; ++j) t[j] += r[R::kJp + j] * f0 + r[R::kJp + 3 + j] * f1;
+        for (int j = 0; j < 3; ++j) t[j] += vw.jp[j] * f0 + vw.jp[3 + j] * f1;
       }
 #pragma unroll
       for (int j = 0; j < 3; ++j) t[j] = warp_sum(t[j]);
@@ -1969,7 +2043,12 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
       if (!isfinite(y[0]) || !isfinite(y[1]) || !isfinite(y[2])) {
         if (lane == 0) atomicExch(flag, 3);
       }
-      for (uint32_t o = o0 + lane; o < o1; o += 32) mcc += obs_mcc(rec + (int64_t)o * R::kSize, cam[o], y);
+      for (uint32_t o = o0 + lane; o < o1; o += 32) {
+        const View vw = rec_view(o);
+        T f0, f1;
+        fz(vw, cam[o], f0, f1);
+        mcc += obs_mcc(vw, f0, f1, y);
+      }
       if (lane < 3) {
         const double d = -(double)y[lane] * scale_p[3 * (int64_t)p + lane];
         pts_new[3 * (int64_t)p + lane] = pts[3 * (int64_t)p + lane] + d;
@@ -2214,6 +2293,7 @@ struct Solve {
   float4* rcache = nullptr;  // mixed path: residual cache, [2][no] (current parameters, candidate)
   float* pcg_yf = nullptr;  // mixed path: FP32 point temporaries of the implicit product
   char* pcg_xc = nullptr;   // the implicit product's operand per camera (B values, compute type)
+  char* zc = nullptr;       // the camera step per camera (B values, compute type; back substitution)
   float *scale_cf = nullptr, *scale_pf = nullptr;               // FP32 copies of the Jacobi scales
   uint32_t *pt_grp = nullptr, *pgrp_cnt = nullptr, *pgrp_off = nullptr;  // point groups (k_pt_groups)
   int64_t n_pgrp = 0;
@@ -2552,6 +2632,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p1.take<float>(tsize == 4 && n_pcg ? 3 * np : 0);
     p1.take<double>((size_t)nc * B * B);
     p1.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
+    p1.take<char>((size_t)nc * B * tsize);
     p1.take<double>(2 * std::max<int64_t>(4096, nc + 1));  // PCG partial sums (one per camera block at most)
     p1.take<PcgState>(1);
     size_t cam_sort_bytes = 0;
@@ -2586,6 +2667,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     if (!(tsize == 4 && n_pcg)) s.pcg_yf = nullptr;
     s.pcg_minv = A.take<double>((size_t)nc * B * B);
     s.pcg_u = A.take<char>((size_t)(n_pcg ? nc : 0) * B * B * tsize);
+    s.zc = A.take<char>((size_t)nc * B * tsize);
     s.pcg_part_n = std::max<int64_t>(4096, nc + 1);
     s.pcg_part = A.take<double>(2 * s.pcg_part_n);
     s.pcg_state = A.take<PcgState>(1);
@@ -3072,10 +3154,13 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       case 3:
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
-          k_backsub_rec<B, T><<<s.nb_pgrp, 128, 0, st>>>(s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, s.ext_col,
-                                                         s.intr_col, s.cam_group, s.k, (const T*)s.rec, z,
-                                                         (const T*)s.Vinv, (const T*)s.gpv, s.scale_p, s.pts, s.pts2,
-                                                         s.part_mcc, s.part_step_p, s.flag);
+          k_gather_cam_rows<B, T>
+              <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(s.nc * B, 256), 1024)), 256, 0, st>>>(
+                  z, (T*)s.zc, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc);
+          check_launch(h);
+          k_backsub_rec<B, T><<<s.nb_pgrp, 128, 0, st>>>(s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, (const T*)s.rec,
+                                                         (const T*)s.zc, (const T*)s.Vinv, (const T*)s.gpv, s.scale_p,
+                                                         s.pts, s.pts2, s.part_mcc, s.part_step_p, s.flag);
           check_launch(h);
         } else if (s.np > 0) {
           k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2,
