@@ -552,7 +552,7 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     // ---- packed: lane i holds observation o0 + i
     const uint32_t o = o0 + lane;
     const bool valid = o < o1;
-    ObsJac<M, T> J;
+    ObsJac<M, T> J{};
     T v[6] = {}, g[3] = {};
     uint32_t p = 0;
     int head = lane, tail = lane;
@@ -589,7 +589,8 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
       for (int j = 0; j < 3; ++j) gm = fmax(gm, fabs((double)g[j] / scale_p[3 * (int64_t)p + j]));
     }
     gmax_update(gmax_shards, gm);
-    if (!valid) return;
+    // lanes past the group's observations stay (the record copy below is
+    // the warp's); their side effects are masked
     const double dp[3] = {fmin(fmax((double)v[0], dmin), dmax), fmin(fmax((double)v[3], dmin), dmax),
                           fmin(fmax((double)v[5], dmin), dmax)};
     T vi[6], pr = T(1);
@@ -625,7 +626,7 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
         }
       }
     }
-    if (lane == head) {
+    if (valid && lane == head) {
       if (!ok) atomicExch(flag, 2);
 #pragma unroll
       for (int i = 0; i < 6; ++i) Vinv[6 * (int64_t)p + i] = vi[i];
@@ -638,6 +639,76 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
     const T r0 = (T)J.r[0], r1 = (T)J.r[1];
     T* rc = rec + (int64_t)o * R::kSize;
+    if constexpr (B % 4 == 0 && sizeof(T) == 4) {
+      // The group's records are consecutive: each lane writes its record
+      // into shared memory in two halves, [Jc W] and [W V^-1 q Jp r], and
+      // after each half the warp copies the 32 records' half out with
+      // coalesced 16-byte stores.
+      constexpr int H1 = 5 * B, H2 = 4 * B + 8;
+      constexpr int HM = H1 > H2 ? H1 : H2;
+      constexpr int kPitch = (HM / 4) % 2 == 1 ? HM : HM + 4;  // 16-byte rows, odd: no bank conflicts
+      __shared__ __align__(16) float rst[4][32 * kPitch];
+      float* sw0 = rst[(threadIdx.x >> 5) & 3];
+      float* sw = sw0 + lane * kPitch;
+      const int n = (int)(o1 - o0);
+      auto copy_out = [&](int H, int off) {
+        __syncwarp();
+        const int per = H / 4;
+        for (int u = lane; u < n * per; u += 32) {
+          const int k = u / per, e = u - k * per;
+          const float4 val = *reinterpret_cast<const float4*>(sw0 + k * kPitch + 4 * e);
+          *reinterpret_cast<float4*>(rec + (int64_t)(o0 + k) * R::kSize + off + 4 * e) = val;
+        }
+        __syncwarp();
+      };
+      static_assert(R::kW == 2 * B && R::kWh == 5 * B && R::kQ == 8 * B && R::kJp == 9 * B, "record layout");
+      if (valid) {
+#pragma unroll
+        for (int c4 = 0; c4 < 2 * B; c4 += 4) {
+          T t4[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) t4[e] = c4 + e < B ? J.Jc[0][c4 + e] : J.Jc[1][c4 + e - B];
+          st4<T>(sw + c4, t4);
+        }
+#pragma unroll
+        for (int i0 = 0; i0 < B; i0 += 4) {
+          T wc[12];
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) wc[3 * ii + j] = J.Jc[0][i0 + ii] * J.Jp[0][j] + J.Jc[1][i0 + ii] * J.Jp[1][j];
+#pragma unroll
+          for (int e = 0; e < 3; ++e) st4<T>(sw + 2 * B + 3 * i0 + 4 * e, wc + 4 * e);
+        }
+      }
+      copy_out(H1, R::kJc);
+      if (valid) {
+#pragma unroll
+        for (int i0 = 0; i0 < B; i0 += 4) {
+          T yc[12], qc[4];
+#pragma unroll
+          for (int ii = 0; ii < 4; ++ii) {
+            const int i = i0 + ii;
+            T wr[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) wr[j] = J.Jc[0][i] * J.Jp[0][j] + J.Jc[1][i] * J.Jp[1][j];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) yc[3 * ii + j] = wr[0] * Vf[0][j] + wr[1] * Vf[1][j] + wr[2] * Vf[2][j];
+            qc[ii] = (J.Jc[0][i] * r0 + J.Jc[1][i] * r1) -
+                     (yc[3 * ii] * g[0] + yc[3 * ii + 1] * g[1] + yc[3 * ii + 2] * g[2]);
+          }
+#pragma unroll
+          for (int e = 0; e < 3; ++e) st4<T>(sw + 3 * i0 + 4 * e, yc + 4 * e);
+          st4<T>(sw + 3 * B + i0, qc);
+        }
+        const T t8[8] = {J.Jp[0][0], J.Jp[0][1], J.Jp[0][2], J.Jp[1][0], J.Jp[1][1], J.Jp[1][2], r0, r1};
+        st4<T>(sw + 4 * B, t8);
+        st4<T>(sw + 4 * B + 4, t8 + 4);
+      }
+      copy_out(H2, R::kWh);
+      return;
+    }
+    if (!valid) return;
     if constexpr (B % 4 == 0) {
       // every field starts on a 16-byte boundary: write the record in 16-byte pieces
 #pragma unroll
