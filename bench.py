@@ -514,9 +514,11 @@ def measure_large(h, abi, max_iters=100):
     """The large workload (5,000 cameras with per-camera K3, 2,000,000 points,
     ~20M observations with geometric(10) views, 2% outliers, Huber) on the
     iterative path: block-Jacobi PCG on the implicit Schur complement.  The
-    plain FP64 run with ceres's stopping rule gives C*; the mixed run (FP32
-    Jacobians and Schur blocks, FP64 PCG vectors and cost) is traced and its
-    time to (1 + 1e-6) C* is the first traced iteration at or below it.
+    plain FP64 run with ceres's stopping rule (at most max_iters LM
+    iterations) gives C*; the mixed run (FP32 Jacobians and Schur blocks, FP64
+    PCG vectors and cost; at most 3 max_iters iterations, as its inexact steps
+    descend more slowly per iteration) is traced and its time to
+    (1 + 1e-6) C* is the first traced iteration at or below it.
     Device-resident inputs; wall times of whole gbba_solve calls, setup
     included."""
     import torch
@@ -532,12 +534,13 @@ def measure_large(h, abi, max_iters=100):
                        "per-camera K3, Huber(4), block-Jacobi PCG (ITERATIVE_SCHUR)",
            "observations": no, "generation_s": gen_s}
     traces = {}
-    for name, prec, ftol in (("fp64", abi.PRECISION_FP64, 1e-6), ("mixed", abi.PRECISION_MIXED, 1e-10)):
+    for name, prec, ftol, iters in (("fp64", abi.PRECISION_FP64, 1e-6, max_iters),
+                                    ("mixed", abi.PRECISION_MIXED, 1e-10, 3 * max_iters)):
         for f, v in pristine.items():
             getattr(dp, f).copy_(v)
-        o = scenes.ba_options_for(sc, max_num_iterations=max_iters, precision=prec, function_tolerance=ftol,
+        o = scenes.ba_options_for(sc, max_num_iterations=iters, precision=prec, function_tolerance=ftol,
                                   linear_solver=abi.SOLVER_ITERATIVE_SCHUR, fp64_polish_iterations=0)
-        cap = max_iters + 2
+        cap = iters + 2
         tc, tt = np.zeros(cap), np.zeros(cap)
         o.trace_cost, o.trace_time_s, o.trace_capacity = tc.ctypes.data, tt.ctypes.data, cap
         summ = abi.GbbaSummary()
@@ -549,6 +552,7 @@ def measure_large(h, abi, max_iters=100):
         out[name] = {"seconds": sec, "final_cost": summ.final_cost, "iterations": summ.num_iterations,
                      "cg_iterations": summ.linear_solver_iterations, "termination": summ.termination_type,
                      "obs_iter_per_s": no * summ.num_iterations / sec, "function_tolerance": ftol,
+                     "max_num_iterations": iters,
                      "phases_s": {"solver_total": summ.total_time_s, "schur": summ.jacobian_time_s,
                                   "pcg_and_back_substitution": summ.linear_solver_time_s,
                                   "candidate_cost": summ.residual_time_s,
