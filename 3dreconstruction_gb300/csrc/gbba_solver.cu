@@ -445,6 +445,33 @@ template <int B>
 struct Rec {
   static constexpr int kJc = 0, kW = 2 * B, kWh = 5 * B, kQ = 8 * B, kJp = 9 * B, kR = 9 * B + 6, kSize = 9 * B + 8;
 };
+// Compact record of the iterative path (2B + 16 values), which forms no
+// camera-pair products and recomputes the W products where it reads them:
+//   [ Jc (2 x B) | Jp (2 x 3) | Jp V^-1 (2 x 3) | r (2) | u = r - Jp V^-1 g_p (2) ]
+// (W = Jc^T Jp, W V^-1 W^T = Jc^T (Jp V^-1 Jp^T) Jc, q = Jc^T u).
+template <int B>
+struct RecC {
+  static constexpr int kJc = 0, kJp = 2 * B, kJpV = 2 * B + 6, kR = 2 * B + 12, kU = 2 * B + 14, kSize = 2 * B + 16;
+};
+static_assert(Rec<12>::kSize == 9 * 12 + 8 && RecC<12>::kSize == 2 * 12 + 16, "record sizes used by the workspace planner");
+// The record layout of a path: compact for the iterative solver.
+template <int B, bool kCompact>
+using RecOf = typename std::conditional<kCompact, RecC<B>, Rec<B>>::type;
+
+// n (a multiple of 4) consecutive FP32 values from a 16-byte aligned address,
+// in 16-byte loads issued together.
+template <int N>
+__device__ __forceinline__ void ld_vec4(const float* __restrict__ p, float v[N]) {
+  static_assert(N % 4 == 0, "whole 16-byte pieces");
+#pragma unroll
+  for (int i = 0; i < N; i += 4) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p + i));
+    v[i] = q.x;
+    v[i + 1] = q.y;
+    v[i + 2] = q.z;
+    v[i + 3] = q.w;
+  }
+}
 
 // (V + D_p^2 / radius)^-1 of one point by a 3x3 Cholesky; v = upper
 // triangle of V (00 01 02 11 12 22).  Returns false on a non-positive pivot
@@ -531,7 +558,7 @@ __device__ __forceinline__ void gmax_update(unsigned long long* shards, double m
               (unsigned long long)__double_as_longlong(m));
 }
 
-template <int M, typename T, bool kFp64Inverse = false>
+template <int M, typename T, bool kFp64Inverse = false, bool kCompact = false>
 __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                          const double* __restrict__ scale_c,
                                                          const double* __restrict__ scale_p,
@@ -542,6 +569,7 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
                                                          int* __restrict__ flag) {
   constexpr int B = ObsJac<M, T>::B;
   using R = Rec<B>;
+  using RC = RecC<B>;
   const int lane = threadIdx.x & 31;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   if (w >= n_groups) return;
@@ -638,6 +666,53 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     }
     const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
     const T r0 = (T)J.r[0], r1 = (T)J.r[1];
+    if constexpr (kCompact) {
+      // [Jc Jp JpV r u] (RecC); FP32: through shared memory, one coalesced copy
+      T jv[6], u[2];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) jv[3 * q + j] = J.Jp[q][0] * Vf[0][j] + J.Jp[q][1] * Vf[1][j] + J.Jp[q][2] * Vf[2][j];
+      }
+      u[0] = r0 - (jv[0] * g[0] + jv[1] * g[1] + jv[2] * g[2]);
+      u[1] = r1 - (jv[3] * g[0] + jv[4] * g[1] + jv[5] * g[2]);
+      auto put = [&](T* d) {
+#pragma unroll
+        for (int i = 0; i < B; ++i) {
+          d[RC::kJc + i] = J.Jc[0][i];
+          d[RC::kJc + B + i] = J.Jc[1][i];
+        }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          d[RC::kJp + j] = J.Jp[0][j];
+          d[RC::kJp + 3 + j] = J.Jp[1][j];
+        }
+#pragma unroll
+        for (int j = 0; j < 6; ++j) d[RC::kJpV + j] = jv[j];
+        d[RC::kR] = r0;
+        d[RC::kR + 1] = r1;
+        d[RC::kU] = u[0];
+        d[RC::kU + 1] = u[1];
+      };
+      if constexpr (sizeof(T) == 4) {
+        constexpr int H = RC::kSize;
+        constexpr int kPitch = H % 2 == 1 ? H : H + 1;  // odd: no bank conflicts
+        __shared__ float cst[4][32 * kPitch];
+        float* sw0 = cst[(threadIdx.x >> 5) & 3];
+        if (valid) put(sw0 + lane * kPitch);
+        __syncwarp();
+        const int n = (int)(o1 - o0);
+        float* dst = rec + (int64_t)o0 * RC::kSize;  // the group's records are consecutive
+        for (int e = lane; e < n * H; e += 32) {
+          const int k = e / H;
+          dst[e] = sw0[k * kPitch + (e - k * H)];
+        }
+        __syncwarp();
+      } else {
+        if (valid) put(rec + (int64_t)o * RC::kSize);
+      }
+      return;
+    }
     T* rc = rec + (int64_t)o * R::kSize;
     if constexpr (B % 4 == 0 && sizeof(T) == 4) {
       // The group's records are consecutive: each lane writes its record
@@ -783,6 +858,23 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
 #pragma unroll
     for (int i = 0; i < 3; ++i) g[i] += dg[i];
     const T r0 = (T)J.r[0], r1 = (T)J.r[1];
+    if constexpr (kCompact) {
+      // Jc, Jp and r now; Jp V^-1 and u once V^-1 is known
+      T* rc = rec + (int64_t)o * RC::kSize;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        rc[RC::kJp + j] = J.Jp[0][j];
+        rc[RC::kJp + 3 + j] = J.Jp[1][j];
+      }
+      rc[RC::kR] = r0;
+      rc[RC::kR + 1] = r1;
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        rc[RC::kJc + i] = J.Jc[0][i];
+        rc[RC::kJc + B + i] = J.Jc[1][i];
+      }
+      continue;
+    }
     T* rc = rec + (int64_t)o * R::kSize;
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
@@ -825,6 +917,24 @@ __global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t*
     }
   }
   const T Vf[3][3] = {{vi[0], vi[1], vi[2]}, {vi[1], vi[3], vi[4]}, {vi[2], vi[4], vi[5]}};
+  if constexpr (kCompact) {
+    for (uint32_t o = o0 + lane; o < o1; o += 32) {
+      T* rc = rec + (int64_t)o * RC::kSize;
+      T jv[6];
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          jv[3 * q + j] = rc[RC::kJp + 3 * q] * Vf[0][j] + rc[RC::kJp + 3 * q + 1] * Vf[1][j] +
+                          rc[RC::kJp + 3 * q + 2] * Vf[2][j];
+      }
+#pragma unroll
+      for (int j = 0; j < 6; ++j) rc[RC::kJpV + j] = jv[j];
+      rc[RC::kU] = rc[RC::kR] - (jv[0] * g[0] + jv[1] * g[1] + jv[2] * g[2]);
+      rc[RC::kU + 1] = rc[RC::kR + 1] - (jv[3] * g[0] + jv[4] * g[1] + jv[5] * g[2]);
+    }
+    return;
+  }
   for (uint32_t o = o0 + lane; o < o1; o += 32) {
     T* rc = rec + (int64_t)o * R::kSize;
 #pragma unroll
@@ -1131,7 +1241,7 @@ __global__ void __launch_bounds__(128) k_pair_merge(const PairMerge* __restrict_
 // Thread t sums observations t, t+256, ...; the per-thread sums are reduced
 // by a warp butterfly and then over the eight warps in order (a fixed order).
 constexpr int kRhsThreads = 256;
-template <int B, typename T>
+template <int B, typename T, bool kCompact = false>
 __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __restrict__ cam_off,
                                                             const uint32_t* __restrict__ cam_obs,
                                                             const T* __restrict__ rec,
@@ -1142,19 +1252,40 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
                                                             double* __restrict__ diag_c, double dmin, double dmax,
                                                             const double* __restrict__ radius, T* __restrict__ S,
                                                             int64_t ld, unsigned long long* __restrict__ gmax_shards) {
-  using R = Rec<B>;
+  using R = RecOf<B, kCompact>;
   __shared__ T part[3][kRhsThreads / 32][B];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c = blockIdx.x;
   T acc[B], nrm[B], grd[B];
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = nrm[i] = grd[i] = T(0);
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (sizeof(T) == 4 && kCompact && RecC<B>::kSize % 4 == 0) {
+    // compact records, 16-byte aligned: thread t reads its observations'
+    // Jc and (r, u) in 16-byte loads (q = Jc^T u)
+    using RC = RecC<B>;
+    static_assert((2 * B) % 4 == 0 && RC::kU == RC::kR + 2 && RC::kR % 4 == 0, "16-byte pieces");
+    for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
+      const float* r = rec + (int64_t)cam_obs[q] * RC::kSize;
+      float jc[2 * B], ru[4];
+      ld_vec4<2 * B>(r + RC::kJc, jc);
+      ld_vec4<4>(r + RC::kR, ru);
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T j0 = jc[i], j1 = jc[B + i];
+        acc[i] += j0 * ru[2] + j1 * ru[3];
+        nrm[i] += j0 * j0 + j1 * j1;
+        grd[i] += j0 * ru[0] + j1 * ru[1];
+      }
+    }
+  } else if constexpr (sizeof(T) == 4) {
     // The warp takes observations 32 at a time (thread t still sums
     // observations t, t + 256, ...): it copies the 32 records' Jc, q and r
     // (3B + 2 values) into shared memory, record by record with coalesced
     // loads, and each lane reads its own there.
-    constexpr int NV = 3 * B + 2, FW = (NV + 31) / 32, kPitch = NV + 1;  // odd pitch: no bank conflicts
+    // staged: Jc rows [0, 2B), then q [2B, 3B) and r (full record) or r
+    // and u (compact record, q = Jc^T u formed here)
+    constexpr int NV = kCompact ? 2 * B + 4 : 3 * B + 2, FW = (NV + 31) / 32;
+    constexpr int kPitch = NV % 2 == 1 ? NV : NV + 1;  // odd pitch: no bank conflicts
     __shared__ float rs[kRhsThreads / 32][32 * kPitch];
     float* sw = rs[warp];
     const uint32_t q1 = cam_off[c + 1];
@@ -1169,17 +1300,21 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
 #pragma unroll
         for (int f = 0; f < FW; ++f) {
           const int j = lane + 32 * f;
-          if (j < NV) sw[k * kPitch + j] = r[j < 2 * B ? R::kJc + j : j < 3 * B ? R::kQ + (j - 2 * B) : R::kR + (j - 3 * B)];
+          if (j < NV) {
+            if constexpr (kCompact) sw[k * kPitch + j] = r[j < 2 * B ? R::kJc + j : R::kR + (j - 2 * B)];
+            else sw[k * kPitch + j] = r[j < 2 * B ? R::kJc + j : j < 3 * B ? R::kQ + (j - 2 * B) : R::kR + (j - 3 * B)];
+          }
         }
       }
       __syncwarp();
       if (!valid) continue;
-      const float* v = sw + lane * kPitch;  // Jc rows [0, 2B), q [2B, 3B), r [3B, 3B + 2)
-      const T r0 = v[3 * B], r1 = v[3 * B + 1];
+      const float* v = sw + lane * kPitch;
+      const T r0 = v[kCompact ? 2 * B : 3 * B], r1 = v[kCompact ? 2 * B + 1 : 3 * B + 1];
 #pragma unroll
       for (int i = 0; i < B; ++i) {
         const T j0 = v[i], j1 = v[B + i];
-        acc[i] += v[2 * B + i];
+        if constexpr (kCompact) acc[i] += j0 * v[2 * B + 2] + j1 * v[2 * B + 3];
+        else acc[i] += v[2 * B + i];
         nrm[i] += j0 * j0 + j1 * j1;
         grd[i] += j0 * r0 + j1 * r1;
       }
@@ -1191,7 +1326,8 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
 #pragma unroll
       for (int i = 0; i < B; ++i) {
         const T j0 = r[R::kJc + i], j1 = r[R::kJc + B + i];
-        acc[i] += r[R::kQ + i];
+        if constexpr (kCompact) acc[i] += j0 * r[RecC<B>::kU] + j1 * r[RecC<B>::kU + 1];
+        else acc[i] += r[Rec<B>::kQ + i];
         nrm[i] += j0 * j0 + j1 * j1;
         grd[i] += j0 * r0 + j1 * r1;
       }
@@ -1271,11 +1407,12 @@ __device__ __forceinline__ void kahan_add(float& s, float& c, float v) {
 // Mblk, which k_cam_inverse then inverts in place.  One block of kCamWarps
 // (2, 4 or 8: the handle's camera_warps) warps per camera: warp w takes every
 // kCamWarps-th of the camera's observations.  The warp copies an
-// observation's Jc, W and (W V^-1) (the first 8B values of its record) with
-// coalesced loads into shared memory, as Jc column pairs and 4-wide W and
-// W V^-1 rows, the next observation's copy in flight while it computes; its
-// lanes take the lower triangle's entries.  The warps' partial blocks are
-// added in warp order and written to both triangles.
+// observation's Jc, Jp and Jp V^-1 (the first 2B + 12 values of its compact
+// record) with coalesced loads into shared memory, Jc as column pairs, the
+// next observation's copy in flight while it computes; its lanes take the
+// lower triangle's entries, (W V^-1 W^T)_ij = Jc_i^T (Jp V^-1 Jp^T) Jc_j.
+// The warps' partial blocks are added in warp order and written to both
+// triangles.
 template <int B, typename T, int kCamWarps>
 __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* __restrict__ cam_off,
                                                                const uint32_t* __restrict__ cam_obs,
@@ -1286,14 +1423,16 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
                                                                const double* __restrict__ diag_c,
                                                                const double* __restrict__ radius, T* __restrict__ U,
                                                                double* __restrict__ Mblk) {
-  using R = Rec<B>;
+  using R = RecC<B>;
   constexpr int NT = B * (B + 1) / 2;       // lower-triangle entries
   constexpr int E = (NT + 31) / 32;         // per lane
-  constexpr int NV = 8 * B;                 // staged record values: Jc (2B), W (3B), W V^-1 (3B)
+  constexpr int NV = 2 * B + 12;            // staged record values: Jc (2B), Jp (6), Jp V^-1 (6)
   constexpr int F = (NV + 31) / 32;         // per lane
-  static_assert(R::kJc == 0 && R::kW == 2 * B && R::kWh == 5 * B, "record layout: Jc, W, W V^-1 first");
-  // staged layout: jc[i] = (Jc[0][i], Jc[1][i]), w[i] / wh[i] = row i padded to 4
-  constexpr int kJ = 0, kWr = 2 * B, kWhr = 6 * B, kStage = 10 * B;
+  static_assert(R::kJc == 0 && R::kJp == 2 * B && R::kJpV == 2 * B + 6, "record layout: Jc, Jp, Jp V^-1 first");
+  // staged layout: jc[i] = (Jc[0][i], Jc[1][i]), then Jp and Jp V^-1 as stored
+  constexpr int kJ = 0, kP = 2 * B, kM = 2 * B + 12, kPc = 2 * B + 16, kStage = 4 * B + 16;
+  // stage: jc pairs, Jp, Jp V^-1, then M = Jp V^-1 Jp^T (4) and the column
+  // pairs P_j = M Jc_j (2B), formed once per observation
   __shared__ __align__(16) T stage[kCamWarps][kStage];
   __shared__ double part[kCamWarps][2][E * 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1306,11 +1445,9 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
   for (int f = 0; f < F; ++f) {
     const int v = lane + 32 * f;
     if (v < 2 * B) dst[f] = kJ + 2 * (v % B) + v / B;
-    else if (v < 5 * B) dst[f] = kWr + 4 * ((v - 2 * B) / 3) + (v - 2 * B) % 3;
-    else if (v < NV) dst[f] = kWhr + 4 * ((v - 5 * B) / 3) + (v - 5 * B) % 3;
+    else if (v < NV) dst[f] = kP + (v - 2 * B);
     else dst[f] = -1;
   }
-  if (lane < B) sw[kWr + 4 * lane + 3] = sw[kWhr + 4 * lane + 3] = T(0);  // row padding
   int ei[E], ej[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) {
@@ -1341,15 +1478,26 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
       if (dst[f] >= 0) sw[dst[f]] = pre[f];
     __syncwarp();
     if (q + kCamWarps < q1) fetch(q + kCamWarps);
+    if (lane < 4) {
+      const int a = lane >> 1, b = lane & 1;
+      const T* jp = sw + kP;
+      const T* jv = sw + kP + 6;
+      sw[kM + lane] = jv[3 * a] * jp[3 * b] + jv[3 * a + 1] * jp[3 * b + 1] + jv[3 * a + 2] * jp[3 * b + 2];
+    }
+    __syncwarp();
+    if (lane < B) {
+      const T b0 = sw[kJ + 2 * lane], b1 = sw[kJ + 2 * lane + 1];
+      sw[kPc + 2 * lane] = sw[kM] * b0 + sw[kM + 1] * b1;
+      sw[kPc + 2 * lane + 1] = sw[kM + 2] * b0 + sw[kM + 3] * b1;
+    }
+    __syncwarp();
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       if (lane + 32 * e >= NT) continue;
       const int i = ei[e], j = ej[e];
       const T a0 = sw[kJ + 2 * i], a1 = sw[kJ + 2 * i + 1], b0 = sw[kJ + 2 * j], b1 = sw[kJ + 2 * j + 1];
-      const T* hi = sw + kWhr + 4 * i;
-      const T* wj = sw + kWr + 4 * j;
       const A u = a0 * b0 + a1 * b1;
-      const A w = hi[0] * wj[0] + hi[1] * wj[1] + hi[2] * wj[2];
+      const A w = a0 * sw[kPc + 2 * j] + a1 * sw[kPc + 2 * j + 1];
       if constexpr (sizeof(T) == 4) {
         kahan_add(su[e], cu[e], u);
         kahan_add(ss[e], cs[e], u - w);
@@ -1469,11 +1617,11 @@ __device__ __forceinline__ void load_cam_row(const T* __restrict__ p, T v[B]) {
 
 // y_p = V_p^-1 sum_{o in p} W_o^T x_c(o), one warp per point group (the
 // groups of k_pt_groups: a packed group holds one observation per lane, a
-// group of one point is taken 32 observations at a time).  A group's
-// records are consecutive: the warp copies their W blocks (3B values each)
-// into shared memory with coalesced loads, and each lane reads its own
-// observation's block there and its camera's operand row from xc (the
-// operand gathered per camera by k_pcg_gather_cam).  A grid of at most a few
+// group of one point is taken 32 observations at a time), W^T x formed as
+// Jp^T (Jc x).  A group's compact records are consecutive: the warp copies
+// their Jc and Jp (2B + 6 values each) into shared memory with coalesced
+// loads, and each lane reads its own observation's there and its camera's
+// operand row from xc (the operand gathered per camera by k_pcg_gather_cam).  A grid of at most a few
 // waves strides over the groups, so that a launch after the solve has
 // stopped costs one flag read per block.
 template <int B, typename T>
@@ -1484,10 +1632,12 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
                                                     const T* __restrict__ rec, const T* __restrict__ Vinv,
                                                     const T* __restrict__ xc, T* __restrict__ yt,
                                                     const PcgState* __restrict__ ps, int reset_period) {
-  using R = Rec<B>;
+  using R = RecC<B>;
   // FP32 path: FP32 operand and products and sums (a point has few
   // observations), FP32 point temporaries out
-  constexpr int NW = 3 * B, kPitch = NW + 1;  // odd pitch: no bank conflicts
+  constexpr int NW = 2 * B + 6;  // staged: Jc (2B), Jp (6)
+  constexpr int kPitch = NW % 2 == 1 ? NW : NW + 1;  // odd pitch: no bank conflicts
+  static_assert(R::kJc == 0 && R::kJp == 2 * B, "record layout: Jc, Jp first");
   __shared__ T wst[4][32 * kPitch];
   const int lane = threadIdx.x & 31;
   T* sw = wst[(threadIdx.x >> 5) & 3];
@@ -1499,7 +1649,7 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
     T t[3] = {T(0), T(0), T(0)};
     for (uint32_t q0 = o0; q0 < o1; q0 += 32) {
       const int total = (int)min(32u, o1 - q0) * NW;
-      const T* base = rec + (int64_t)q0 * R::kSize + R::kW;
+      const T* base = rec + (int64_t)q0 * R::kSize;
       __syncwarp();
       for (int t0 = 0; t0 < total; t0 += 128) {
         T v[4];
@@ -1521,12 +1671,16 @@ __global__ void __launch_bounds__(128) k_spmv_point(const uint32_t* __restrict__
       if (o < o1) {
         T xr[B];
         load_cam_row<B, T>(xc + (int64_t)cam[o] * B, xr);
+        // W^T x = Jp^T (Jc x)
         const T* wr = sw + lane * kPitch;
+        T f0 = T(0), f1 = T(0);
 #pragma unroll
         for (int i = 0; i < B; ++i) {
-#pragma unroll
-          for (int j = 0; j < 3; ++j) t[j] += wr[3 * i + j] * xr[i];
+          f0 += wr[i] * xr[i];
+          f1 += wr[B + i] * xr[i];
         }
+#pragma unroll
+        for (int j = 0; j < 3; ++j) t[j] += wr[2 * B + j] * f0 + wr[2 * B + 3 + j] * f1;
       }
     }
     uint32_t p;
@@ -1576,7 +1730,7 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
     const double* __restrict__ diag_c, const double* __restrict__ radius, const double* __restrict__ x,
     const double* __restrict__ y, const float* __restrict__ yf, double* __restrict__ out, double* __restrict__ part,
     const PcgState* __restrict__ ps, int reset_period) {
-  using R = Rec<B>;
+  using R = RecC<B>;
   __shared__ double red[kCamWarps][B];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t c = blockIdx.x;
@@ -1589,13 +1743,38 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
 #pragma unroll
   for (int i = 0; i < B; ++i) acc[i] = 0.0;
   const uint32_t qb = cam_off[c], q1 = cam_off[c + 1];
-  if constexpr (sizeof(T) == 4) {
+  if constexpr (sizeof(T) == 4 && R::kSize % 4 == 0) {
+    // one observation per lane, its Jc and Jp (2B + 6 values) in 16-byte
+    // loads straight from its 16-byte aligned record: W y = Jc^T (Jp y).
+    // FP32 products, Kahan-compensated FP32 sums per lane (a camera has
+    // thousands of observations), FP64 from the lane sums on.
+    constexpr int NL = (2 * B + 6 + 3) / 4 * 4;
+    float sa[B], ca[B];
+#pragma unroll
+    for (int i = 0; i < B; ++i) sa[i] = ca[i] = 0.0f;
+    for (uint32_t q = qb + warp * 32 + lane; q < q1; q += kCamWarps * 32) {
+      const uint32_t o = cam_obs[q];
+      float w[NL];
+      ld_vec4<NL>(rec + (int64_t)o * R::kSize, w);
+      const float* yp = yf + 3 * (int64_t)pt[o];
+      const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
+      const float h0 = w[2 * B] * y0 + w[2 * B + 1] * y1 + w[2 * B + 2] * y2;
+      const float h1 = w[2 * B + 3] * y0 + w[2 * B + 4] * y1 + w[2 * B + 5] * y2;
+#pragma unroll
+      for (int i = 0; i < B; ++i) kahan_add(sa[i], ca[i], -(w[i] * h0 + w[B + i] * h1));
+    }
+#pragma unroll
+    for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
+  } else if constexpr (sizeof(T) == 4) {
     // The warp takes its camera's observations 32 at a time, one per lane:
-    // it copies the 32 records' W blocks (3B values each) into shared memory
-    // with coalesced loads, record by record, and each lane then reads its
-    // own.  FP32 products, Kahan-compensated FP32 sums per lane (a camera
-    // has thousands of observations), FP64 from the lane sums on.
-    constexpr int NW = 3 * B, FW = (NW + 31) / 32, kPitch = NW + 1;  // odd pitch: no bank conflicts
+    // it copies the 32 compact records' Jc and Jp (2B + 6 values each) into
+    // shared memory with coalesced loads, record by record, and each lane
+    // then reads its own: W y = Jc^T (Jp y).  FP32 products,
+    // Kahan-compensated FP32 sums per lane (a camera has thousands of
+    // observations), FP64 from the lane sums on.
+    constexpr int NW = 2 * B + 6, FW = (NW + 31) / 32;
+    constexpr int kPitch = NW % 2 == 1 ? NW : NW + 1;  // odd pitch: no bank conflicts
+    static_assert(R::kJc == 0 && R::kJp == 2 * B, "record layout: Jc, Jp first");
     __shared__ float wst[kCamWarps][32 * kPitch];
     float* sw = wst[warp];
     float sa[B], ca[B];
@@ -1608,7 +1787,7 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
       const int nv = (int)min(32u, q1 - q0);
       __syncwarp();
       for (int k = 0; k < nv; ++k) {
-        const T* r = rec + (int64_t)__shfl_sync(0xffffffffu, o, k) * R::kSize + R::kW;
+        const T* r = rec + (int64_t)__shfl_sync(0xffffffffu, o, k) * R::kSize;
 #pragma unroll
         for (int f = 0; f < FW; ++f) {
           const int v = lane + 32 * f;
@@ -1620,8 +1799,10 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
       const float* w = sw + lane * kPitch;
       const float* yp = yf + 3 * (int64_t)pt[o];
       const float y0 = yp[0], y1 = yp[1], y2 = yp[2];
+      const float h0 = w[2 * B] * y0 + w[2 * B + 1] * y1 + w[2 * B + 2] * y2;
+      const float h1 = w[2 * B + 3] * y0 + w[2 * B + 4] * y1 + w[2 * B + 5] * y2;
 #pragma unroll
-      for (int i = 0; i < B; ++i) kahan_add(sa[i], ca[i], -(w[3 * i] * y0 + w[3 * i + 1] * y1 + w[3 * i + 2] * y2));
+      for (int i = 0; i < B; ++i) kahan_add(sa[i], ca[i], -(w[i] * h0 + w[B + i] * h1));
     }
 #pragma unroll
     for (int i = 0; i < B; ++i) acc[i] = (double)sa[i] - (double)ca[i];
@@ -1633,9 +1814,10 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_spmv_camera(
       const T* r = rec + (int64_t)o * R::kSize;
       const double* yp = y + 3 * (int64_t)pt[o];
       const double y0 = yp[0], y1 = yp[1], y2 = yp[2];
+      const double h0 = (double)r[R::kJp] * y0 + (double)r[R::kJp + 1] * y1 + (double)r[R::kJp + 2] * y2;
+      const double h1 = (double)r[R::kJp + 3] * y0 + (double)r[R::kJp + 4] * y1 + (double)r[R::kJp + 5] * y2;
 #pragma unroll
-      for (int i = 0; i < B; ++i)
-        acc[i] -= (double)r[R::kW + 3 * i] * y0 + (double)r[R::kW + 3 * i + 1] * y1 + (double)r[R::kW + 3 * i + 2] * y2;
+      for (int i = 0; i < B; ++i) acc[i] -= (double)r[R::kJc + i] * h0 + (double)r[R::kJc + B + i] * h1;
     }
   }
 #pragma unroll
@@ -1974,7 +2156,7 @@ __global__ void k_cam_groups(const uint32_t* cam, const uint32_t* icam, int64_t 
 // packed group's records are consecutive: the warp copies their Jc, Jp and r
 // (2B + 8 values each) into shared memory with coalesced loads, and each lane
 // reads its own there.
-template <int B, typename T>
+template <int B, typename T, bool kCompact = false>
 __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict__ pt_off, const uint32_t* __restrict__ pt,
                                                      const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                      const uint32_t* __restrict__ cam,
@@ -1983,18 +2165,19 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
                                                      const double* __restrict__ scale_p, const double* __restrict__ pts,
                                                      double* __restrict__ pts_new, double* __restrict__ part_mcc,
                                                      double* __restrict__ part_step, int* __restrict__ flag) {
-  using R = Rec<B>;
-  static_assert(R::kJc == 0 && R::kR == R::kJp + 6 && R::kSize == R::kR + 2, "record layout: Jc first, Jp and r last");
-  constexpr int NV = 2 * B + 8, kPitch = NV + 1;  // staged values; odd pitch: no bank conflicts
+  using R = RecOf<B, kCompact>;
+  // staged values: Jc (2B), Jp (6), r (2)
+  constexpr int NV = 2 * B + 8, kPitch = NV + 1;  // odd pitch: no bank conflicts
   __shared__ T rst[4][32 * kPitch];
   __shared__ double smcc[4], sstep[4];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   double mcc = 0.0, stp = 0.0;
-  // one observation's values: Jc rows, Jp rows (6) and r (2)
+  // one observation's values: Jc rows, Jp rows and r
   struct View {
     const T* jc;
     const T* jp;
+    const T* r;
   };
   // F z of one observation: the camera block's part of J step
   auto fz = [&](const View& v, uint32_t c, T& f0, T& f1) {
@@ -2017,12 +2200,12 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
       f1 += v.jp[3 + j] * y[j];
     }
     const double m0 = -(double)f0, m1 = -(double)f1;
-    const double r0 = (double)v.jp[6], r1 = (double)v.jp[7];
+    const double r0 = (double)v.r[0], r1 = (double)v.r[1];
     return -(m0 * (r0 + m0 / 2.0) + m1 * (r1 + m1 / 2.0));
   };
   auto rec_view = [&](uint32_t o) -> View {
     const T* r = rec + (int64_t)o * R::kSize;
-    return {r + R::kJc, r + R::kJp};
+    return {r + R::kJc, r + R::kJp, r + R::kR};
   };
   // y_p = V^-1 (g_p - E^T F z) and the candidate point
   auto point_step = [&](uint32_t p, const T t[3], T y[3]) {
@@ -2046,7 +2229,9 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
         for (int u = 0; u < 4; ++u) {
           const int e = e0 + 32 * u + lane;
           const int k = e / NV, j = e - k * NV;
-          if (e < total) v[u] = base[(int64_t)k * R::kSize + (j < 2 * B ? R::kJc + j : R::kJp + (j - 2 * B))];
+          if (e < total)
+            v[u] = base[(int64_t)k * R::kSize +
+                        (j < 2 * B ? R::kJc + j : j < 2 * B + 6 ? R::kJp + (j - 2 * B) : R::kR + (j - 2 * B - 6))];
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -2058,7 +2243,7 @@ __global__ void __launch_bounds__(128) k_backsub_rec(const uint32_t* __restrict_
       __syncwarp();
       const uint32_t o = o0 + lane;
       const bool valid = o < o1;
-      const View vw{sr + lane * kPitch, sr + lane * kPitch + 2 * B};
+      const View vw{sr + lane * kPitch, sr + lane * kPitch + 2 * B, sr + lane * kPitch + 2 * B + 6};
       T t[3] = {T(0), T(0), T(0)};
       T f0 = T(0), f1 = T(0);
       uint32_t p = 0;
@@ -2695,7 +2880,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     p1.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
     p1.take<uint32_t>(np + 1);
     p1.take<uint32_t>(np + 1);
-    p1.take<char>((size_t)no * (9 * B + 8) * tsize);
+    p1.take<char>((size_t)no * (s.dense ? 9 * B + 8 : 2 * B + 16) * tsize);
     // PCG vectors (x, r, z, p, q, b), point temporaries, camera blocks
     p1.take<double>(6 * n_pcg);
     p1.take<double>(3 * np);
@@ -2724,7 +2909,7 @@ static void setup_pairs(gbba_handle* h, Solve& s, size_t tsize) {
     uint32_t* chunks = A.take<uint32_t>(ceil_div(std::max(np, nk) + 1, 1024) + 1);
     uint32_t* pcnt = A.take<uint32_t>(np + 1);
     uint32_t* pair_off = A.take<uint32_t>(np + 1);
-    s.rec = A.take<char>((size_t)no * (9 * B + 8) * tsize);
+    s.rec = A.take<char>((size_t)no * (s.dense ? 9 * B + 8 : 2 * B + 16) * tsize);
     s.pcg_x = A.take<double>(n_pcg);
     s.pcg_r = A.take<double>(n_pcg);
     s.pcg_z = A.take<double>(n_pcg);
@@ -3165,14 +3350,24 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
       case 1:
         if (s.np > 0 && s.pair_path) {
           constexpr int B = 6 + Model<M>::K;
+          // the point kernel with or without the FP64 re-inversion, writing
+          // the full record (dense path: camera-pair products) or the
+          // compact one (iterative path)
+          auto point_rec = [&](auto fp64_inverse) {
+            constexpr bool kInv = decltype(fp64_inverse)::value;
+            if (s.dense)
+              k_schur_point_rec<M, T, kInv, false><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
+                  P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
+                  gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+            else
+              k_schur_point_rec<M, T, kInv, true><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
+                  P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
+                  gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+          };
           if (kPose && (o->mixed_flags & GBBA_MIXED_FP64_POINT_INVERSE))
-            k_schur_point_rec<M, T, true><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
-                P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
-                gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+            point_rec(std::true_type());
           else
-            k_schur_point_rec<M, T><<<(unsigned)ceil_div(s.n_pgrp * 32, 128), 128, 0, st>>>(
-                P, s.pt_grp, s.n_pgrp, s.scale_c, s.scale_p, s.diag_p, o->min_lm_diagonal, o->max_lm_diagonal,
-                gshards, s.radius, (T*)s.Vinv, (T*)s.gpv, (T*)s.rec, s.flag);
+            point_rec(std::false_type());
           check_launch(h);
           if (s.dense && s.n_blocks > 0) {
             if (kPose && (o->mixed_flags & GBBA_MIXED_KAHAN_SCHUR))
@@ -3192,10 +3387,14 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
             }
           }
           if (s.nc > 0) {
-            k_rhs_camera<B, T><<<(unsigned)s.nc, kRhsThreads, 0, st>>>(
-                s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs,
-                s.scale_c, s.diag_c, o->min_lm_diagonal, o->max_lm_diagonal, s.radius, s.dense ? S : nullptr,
-                s.n_pad, gshards);
+            auto rhs_cam = [&](auto compact) {
+              k_rhs_camera<B, T, decltype(compact)::value><<<(unsigned)s.nc, kRhsThreads, 0, st>>>(
+                  s.cam_off, s.cam_obs, (const T*)s.rec, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc, rhs,
+                  s.scale_c, s.diag_c, o->min_lm_diagonal, o->max_lm_diagonal, s.radius, s.dense ? S : nullptr,
+                  s.n_pad, gshards);
+            };
+            if (s.dense) rhs_cam(std::false_type());
+            else rhs_cam(std::true_type());
             check_launch(h);
           }
           if (!s.dense && s.nc > 0) {
@@ -3229,9 +3428,13 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
               <<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(s.nc * B, 256), 1024)), 256, 0, st>>>(
                   z, (T*)s.zc, s.ext_col, s.intr_col, s.cam_group, s.k, s.nc);
           check_launch(h);
-          k_backsub_rec<B, T><<<s.nb_pgrp, 128, 0, st>>>(s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, (const T*)s.rec,
-                                                         (const T*)s.zc, (const T*)s.Vinv, (const T*)s.gpv, s.scale_p,
-                                                         s.pts, s.pts2, s.part_mcc, s.part_step_p, s.flag);
+          auto backsub = [&](auto compact) {
+            k_backsub_rec<B, T, decltype(compact)::value><<<s.nb_pgrp, 128, 0, st>>>(
+                s.pt_off, s.pt, s.pt_grp, s.n_pgrp, s.cam, (const T*)s.rec, (const T*)s.zc, (const T*)s.Vinv,
+                (const T*)s.gpv, s.scale_p, s.pts, s.pts2, s.part_mcc, s.part_step_p, s.flag);
+          };
+          if (s.dense) backsub(std::false_type());
+          else backsub(std::true_type());
           check_launch(h);
         } else if (s.np > 0) {
           k_backsub<M, T><<<s.nb_pt, 128, 0, st>>>(P, s.scale_c, s.scale_p, z, (T*)s.Vinv, (T*)s.gpv, s.pts2,
