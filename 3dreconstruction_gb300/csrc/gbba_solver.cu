@@ -559,7 +559,7 @@ __device__ __forceinline__ void gmax_update(unsigned long long* shards, double m
 }
 
 template <int M, typename T, bool kFp64Inverse = false, bool kCompact = false>
-__global__ void __launch_bounds__(128) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 7 : 1) k_schur_point_rec(Prob P, const uint32_t* __restrict__ pt_grp, int64_t n_groups,
                                                          const double* __restrict__ scale_c,
                                                          const double* __restrict__ scale_p,
                                                          double* __restrict__ diag_p, double dmin, double dmax,
@@ -1275,6 +1275,25 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
         acc[i] += j0 * ru[2] + j1 * ru[3];
         nrm[i] += j0 * j0 + j1 * j1;
         grd[i] += j0 * ru[0] + j1 * ru[1];
+      }
+    }
+  } else if constexpr (sizeof(T) == 4 && !kCompact && B % 4 == 0) {
+    // full records, 16-byte aligned fields: thread t reads its
+    // observations' Jc, q and r in 16-byte loads
+    using RF = Rec<B>;
+    static_assert(RF::kQ % 4 == 0 && RF::kR % 4 == 2 && RF::kSize % 4 == 0, "16-byte pieces");
+    for (uint32_t q = cam_off[c] + threadIdx.x; q < cam_off[c + 1]; q += kRhsThreads) {
+      const float* r = rec + (int64_t)cam_obs[q] * RF::kSize;
+      float jc[2 * B], qv[B], tail[4];
+      ld_vec4<2 * B>(r + RF::kJc, jc);
+      ld_vec4<B>(r + RF::kQ, qv);
+      ld_vec4<4>(r + RF::kR - 2, tail);  // Jp[1][1], Jp[1][2], r0, r1
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const T j0 = jc[i], j1 = jc[B + i];
+        acc[i] += qv[i];
+        nrm[i] += j0 * j0 + j1 * j1;
+        grd[i] += j0 * tail[2] + j1 * tail[3];
       }
     }
   } else if constexpr (sizeof(T) == 4) {
