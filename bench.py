@@ -103,7 +103,7 @@ def factor_flops(n_red):
 # phase's four kernels, two executions averaged) of the current kernels on
 # the medium workload: 4.999 GB for 1,999,428 observations; multiplied by the
 # observation count (the phase's traffic grows with the observations).
-SCHUR_TRAFFIC_PER_OBS = 2500.1
+SCHUR_TRAFFIC_PER_OBS = 2480.7
 SCHUR_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of k_schur_point_rec, k_schur_pairs, "
                         "k_pair_merge, k_rhs_camera on the medium workload, per observation, times the observations")
 
