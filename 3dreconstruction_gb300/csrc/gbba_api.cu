@@ -403,9 +403,16 @@ gbba_status gbba_autotune(gbba_handle* h, const gbba_problem* P, const gbba_opti
       out->candidates[c] = cand[c];
       out->schur_time_s[c] = per_iter(sum.schur_kernel_time_s);
       if (best < 0 || out->schur_time_s[c] < out->schur_time_s[best]) best = c;
+      if (iterative) break;  // the iterative path forms no camera-pair products
     }
-    h->pair_chunk = cand[best];
-    out->pair_chunk = cand[best];
+    if (iterative) {
+      h->pair_chunk = keep_chunk;
+      out->num_candidates = 0;
+      out->pair_chunk = keep_chunk;
+    } else {
+      h->pair_chunk = cand[best];
+      out->pair_chunk = cand[best];
+    }
     out->factor_tensor = -1;
     out->camera_warps = 0;
     if (!iterative && t.precision == GBBA_PRECISION_MIXED) {
@@ -421,14 +428,15 @@ gbba_status gbba_autotune(gbba_handle* h, const gbba_problem* P, const gbba_opti
     } else if (iterative) {
       // 3. warps per camera of the PCG camera kernels
       const int warps[3] = {2, 4, 8};
-      int wb = 1;
       for (int w = 0; w < 3; ++w) {
         h->camera_warps = warps[w];
         const gbba_status s = trial();
         if (s != GBBA_SUCCESS) return s;
         out->pcg_time_s[w] = per_iter(sum.linear_solver_time_s + sum.jacobian_time_s);
-        if (out->pcg_time_s[w] < out->pcg_time_s[wb]) wb = w;
       }
+      int wb = 0;  // the fastest, once all three are timed
+      for (int w = 1; w < 3; ++w)
+        if (out->pcg_time_s[w] < out->pcg_time_s[wb]) wb = w;
       h->camera_warps = warps[wb];
       out->camera_warps = warps[wb];
     }

@@ -34,6 +34,7 @@
 #include <type_traits>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <math_constants.h>
 
 #include "gbba_device.cuh"
 #include "gbba_internal.h"
@@ -266,10 +267,97 @@ __device__ __forceinline__ void obs_jacobian(const Prob& P, int64_t o, const dou
 }
 
 // Squared column norms and gradient (unscaled, corrected) at the current x.
+// Column norms and gradient of the first linearisation, summed
+// deterministically in fixed point: k_linearize_max records each column's
+// largest term (ordered bits of a non-negative double under atomicMax),
+// k_linearize_exp turns it into a power-of-two scale per column for which a
+// sum over all observations stays below 2^62, and k_linearize adds the
+// scaled terms as integers (an integer sum does not depend on the order of
+// the adds).  k_linearize_conv converts back.  Each sum keeps about 2^-62 n_o
+// of its largest term (finer than FP64 atomics over the same terms).
+template <int M, typename T>
+__global__ void __launch_bounds__(256) k_linearize_max(Prob P, unsigned long long* __restrict__ mn_c,
+                                                       unsigned long long* __restrict__ mn_p,
+                                                       unsigned long long* __restrict__ mg_c,
+                                                       unsigned long long* __restrict__ mg_p) {
+  constexpr int B = ObsJac<M, T>::B;
+  for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < P.no; o += (int64_t)gridDim.x * blockDim.x) {
+    ObsJac<M, T> J;
+    double cost;
+    obs_jacobian<M, T, false>(P, o, nullptr, nullptr, J, &cost);
+    auto mx = [](unsigned long long* p, double v) {
+      // |v| as ordered bits; a non-finite term keeps the all-ones word (the
+      // sums of its column become NaN)
+      const double a = fabs(v);
+      atomicMax(p, isfinite(a) ? (unsigned long long)__double_as_longlong(a) : ~0ull);
+    };
+#pragma unroll
+    for (int j = 0; j < B; ++j) {
+      if (J.col[j] < 0) continue;
+      const double a = J.Jc[0][j], b = J.Jc[1][j];
+      mx(&mn_c[J.col[j]], a * a + b * b);
+      mx(&mg_c[J.col[j]], a * J.r[0] + b * J.r[1]);
+    }
+    const int64_t p = P.pt[o];
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const double a = J.Jp[0][j], b = J.Jp[1][j];
+      mx(&mn_p[3 * p + j], a * a + b * b);
+      mx(&mg_p[3 * p + j], a * J.r[0] + b * J.r[1]);
+    }
+  }
+}
+
+// Scale exponent for a largest term m (ordered bits) and n terms: the sum's
+// bound m n times 2^e stays within 2^62.  kNonFinite marks a column with a
+// non-finite term.
+constexpr int kFxNonFinite = 4000;
+__device__ __forceinline__ int lin_exp(unsigned long long mbits, double n) {
+  if (mbits == ~0ull) return kFxNonFinite;
+  const double m = __longlong_as_double((long long)mbits);
+  if (!(m > 0.0)) return 0;
+  int e;
+  frexp(m * n, &e);  // m n < 2^e
+  return 62 - e;
+}
+// Per column: the two exponents (norm, gradient) packed into one double of
+// the LM-diagonal array (free until k_scale_diag rewrites it), and the
+// accumulators cleared.
+__global__ void k_linearize_exp(int64_t n, double nobs, unsigned long long* __restrict__ mn,
+                                unsigned long long* __restrict__ mg, double* __restrict__ exps) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int en = lin_exp(mn[i], nobs), eg = lin_exp(mg[i], nobs);
+    exps[i] = (double)(en + 8192) * 16384.0 + (double)(eg + 8192);
+    mn[i] = 0ull;
+    mg[i] = 0ull;
+  }
+}
+__device__ __forceinline__ void lin_unpack(double packed, int& en, int& eg) {
+  const int hi = (int)(packed / 16384.0);
+  en = hi - 8192;
+  eg = (int)(packed - (double)hi * 16384.0) - 8192;
+}
+// v 2^k rounded to an integer with integer operations (|v| 2^k < 2^62 by
+// the choice of k); any rounding rule serves, the sum is exact.
+__device__ __forceinline__ long long lin_fx(double v, int k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)(b >> 52) & 0x7ff;
+  if (ex == 0 || ex == 0x7ff || k >= kFxNonFinite) return 0;
+  const long long m = (long long)((b & 0xfffffffffffffull) | 0x10000000000000ull);
+  const int sh = ex - 1075 + k;  // |v| 2^k = m 2^sh, m < 2^53, sh <= 9
+  const int rs = min(max(-sh, 0), 63);
+  const long long ml = m << max(min(sh, 9), 0);
+  const long long r = rs ? (ml + (1ll << (rs - 1))) >> rs : ml;
+  return (b >> 63) ? -r : r;
+}
 template <int M, typename T>
 __global__ void __launch_bounds__(256) k_linearize(Prob P, double* __restrict__ cn_c, double* __restrict__ cn_p,
-                                                   double* __restrict__ g_c, double* __restrict__ g_p) {
+                                                   double* __restrict__ g_c, double* __restrict__ g_p,
+                                                   const double* __restrict__ exp_c, const double* __restrict__ exp_p) {
   constexpr int B = ObsJac<M, T>::B;
+  auto add = [](double* p, double v, int k) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(p), (unsigned long long)lin_fx(v, k));
+  };
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < P.no; o += (int64_t)gridDim.x * blockDim.x) {
     ObsJac<M, T> J;
     double cost;
@@ -278,16 +366,32 @@ __global__ void __launch_bounds__(256) k_linearize(Prob P, double* __restrict__ 
     for (int j = 0; j < B; ++j) {
       if (J.col[j] < 0) continue;
       const double a = J.Jc[0][j], b = J.Jc[1][j];
-      atomicAdd(&cn_c[J.col[j]], a * a + b * b);
-      atomicAdd(&g_c[J.col[j]], a * J.r[0] + b * J.r[1]);
+      int en, eg;
+      lin_unpack(exp_c[J.col[j]], en, eg);
+      add(&cn_c[J.col[j]], a * a + b * b, en);
+      add(&g_c[J.col[j]], a * J.r[0] + b * J.r[1], eg);
     }
     const int64_t p = P.pt[o];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
       const double a = J.Jp[0][j], b = J.Jp[1][j];
-      atomicAdd(&cn_p[3 * p + j], a * a + b * b);
-      atomicAdd(&g_p[3 * p + j], a * J.r[0] + b * J.r[1]);
+      int en, eg;
+      lin_unpack(exp_p[3 * p + j], en, eg);
+      add(&cn_p[3 * p + j], a * a + b * b, en);
+      add(&g_p[3 * p + j], a * J.r[0] + b * J.r[1], eg);
     }
+  }
+}
+// The fixed-point sums back to floating point (NaN for a column with a
+// non-finite term).
+__global__ void k_linearize_conv(int64_t n, double* __restrict__ cn, double* __restrict__ g,
+                                 const double* __restrict__ exps) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int en, eg;
+    lin_unpack(exps[i], en, eg);
+    const long long vn = __double_as_longlong(cn[i]), vg = __double_as_longlong(g[i]);
+    cn[i] = en >= kFxNonFinite ? CUDART_NAN : ldexp((double)vn, -en);
+    g[i] = eg >= kFxNonFinite ? CUDART_NAN : ldexp((double)vg, -eg);
   }
 }
 
@@ -3240,8 +3344,31 @@ static gbba_status run_lm(Solve& s, const gbba_options* o, gbba_summary* sum) {
     GBBA_CUDA(cudaMemsetAsync(s.cn_p, 0, sizeof(double) * 3 * s.np, st));
     GBBA_CUDA(cudaMemsetAsync(s.g_p, 0, sizeof(double) * 3 * s.np, st));
     GBBA_CUDA(cudaMemsetAsync(s.gmax_bits, 0, sizeof(unsigned long long), st));
-    k_linearize<M, T><<<s.nb_obs, 256, 0, st>>>(P, s.cn_c, s.cn_p, s.g_c, s.g_p);
+    // deterministic sums: largest terms, scales, fixed-point sums, back to FP64
+    auto ull = [](double* p) { return reinterpret_cast<unsigned long long*>(p); };
+    const double nobs = (double)std::max<int64_t>(1, s.no);
+    const unsigned gc = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(s.n_red, 256), 1024));
+    const unsigned gp = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(3 * s.np, 256), 4096));
+    k_linearize_max<M, T><<<s.nb_obs, 256, 0, st>>>(P, ull(s.cn_c), ull(s.cn_p), ull(s.g_c), ull(s.g_p));
     check_launch(h);
+    if (s.n_red > 0) {
+      k_linearize_exp<<<gc, 256, 0, st>>>(s.n_red, nobs, ull(s.cn_c), ull(s.g_c), s.diag_c);
+      check_launch(h);
+    }
+    if (s.np > 0) {
+      k_linearize_exp<<<gp, 256, 0, st>>>(3 * s.np, nobs, ull(s.cn_p), ull(s.g_p), s.diag_p);
+      check_launch(h);
+    }
+    k_linearize<M, T><<<s.nb_obs, 256, 0, st>>>(P, s.cn_c, s.cn_p, s.g_c, s.g_p, s.diag_c, s.diag_p);
+    check_launch(h);
+    if (s.n_red > 0) {
+      k_linearize_conv<<<gc, 256, 0, st>>>(s.n_red, s.cn_c, s.g_c, s.diag_c);
+      check_launch(h);
+    }
+    if (s.np > 0) {
+      k_linearize_conv<<<gp, 256, 0, st>>>(3 * s.np, s.cn_p, s.g_p, s.diag_p);
+      check_launch(h);
+    }
     if (s.n_red > 0) {
       k_scale_diag<<<(unsigned)std::min<int64_t>(ceil_div(s.n_red, 256), 1024), 256, 0, st>>>(
           s.n_red, s.cn_c, s.g_c, s.scale_c, s.diag_c, first ? 1 : 0, o->jacobi_scaling, o->min_lm_diagonal,

@@ -518,7 +518,10 @@ def measure_large(h, abi, max_iters=100):
     iterations) gives C*; the mixed run (FP32 Jacobians and Schur blocks, FP64
     PCG vectors and cost; at most 3 max_iters iterations, as its inexact steps
     descend more slowly per iteration) is traced and its time to
-    (1 + 1e-6) C* is the first traced iteration at or below it.
+    (1 + 1e-6) C* is the first traced iteration at or below it.  The PCG
+    kernels keep the handle's default of 4 warps per camera: the autotuner's
+    2/4/8 differ by less than 2% here, and a choice that follows timing noise
+    would change the order of the camera sums, and with it the trajectory.
     Device-resident inputs; wall times of whole gbba_solve calls, setup
     included."""
     import torch

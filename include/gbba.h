@@ -240,13 +240,13 @@ gbba_status gbba_solve_batched(gbba_handle* handle, const gbba_problem* problems
  *     warp per item of at most `pair_chunk` observation pairs of one
  *     camera-pair block: smaller items spread the long diagonal blocks over
  *     more warps, larger ones read fewer partial sums), by the Schur phase's
- *     time;
+ *     time (skipped on the iterative path, which forms no pair products);
  *   - for the dense FP32 factorisation, the engine of its trailing update:
  *     the tensor cores (tcgen05, 3xTF32) or the FP32 pipes, by the
  *     factorisation's time;
  *   - for the iterative (PCG) path, the warps per camera of its camera-side
- *     kernels (preconditioner blocks, implicit Schur products), by the linear
- *     solver's time.
+ *     kernels (preconditioner blocks, implicit Schur products), by the time of
+ *     the linear solver and the Schur phase together.
  * The problem's parameters are restored after each trial, so the call leaves
  * them unchanged. */
 #define GBBA_TUNE_MAX_CANDIDATES 4
@@ -258,7 +258,7 @@ typedef struct gbba_tuning {
   int32_t factor_tensor;                                 /* chosen: 1 tensor cores, 0 FP32 pipes (-1: not tuned) */
   int32_t camera_warps;                                  /* chosen: 2, 4 or 8 (0: not tuned) */
   double factor_time_s[2];                               /* dense factorisation per LM iteration: FP32 pipes, tensor */
-  double pcg_time_s[3];                                  /* linear solver per LM iteration: 2, 4, 8 warps */
+  double pcg_time_s[3];                                  /* linear solver + Schur phase per LM iteration: 2, 4, 8 warps */
 } gbba_tuning;
 gbba_status gbba_autotune(gbba_handle* handle, const gbba_problem* problem, const gbba_options* options,
                           int32_t iterations, gbba_tuning* tuning);

@@ -299,6 +299,29 @@ def test_autotune_keeps_the_fastest_work_item_size(gb, abi, scenes):
         h.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("solver", ["dense", "pcg"])
+def test_solves_are_bitwise_repeatable(handle, abi, scenes, solver, precision):
+    """Every reduction of the camera-pair path has a fixed order (the first
+    linearisation's column norms and gradient are fixed-point sums, the Schur
+    blocks have one writer, the PCG sums are fixed-order partials), so
+    repeated solves give the same parameters, costs and iteration counts bit
+    for bit."""
+    sc = scenes.medium_scene(num_cameras=40, num_points=3000, seed=141)
+    sc["camera_constant"][1] = 1
+    opts = scenes.ba_options_for(sc, max_num_iterations=12,
+                                 precision=abi.PRECISION_MIXED if precision == "mixed" else abi.PRECISION_FP64)
+    if solver == "pcg":
+        opts.linear_solver = abi.SOLVER_ITERATIVE_SCHUR
+    runs = [solve(handle, abi, sc, opts) for _ in range(3)]
+    s0, p0 = runs[0]
+    assert s0.usable
+    for s1, p1 in runs[1:]:
+        assert s1.final_cost == s0.final_cost and s1.num_iterations == s0.num_iterations
+        for k in ("extrinsics", "intrinsics", "points"):
+            np.testing.assert_array_equal(p1[k], p0[k])
+
+
 @pytest.mark.parametrize("path", ["dense_mixed", "pcg_mixed"])
 def test_autotune_factor_engine_and_camera_warps(gb, abi, scenes, path):
     """In mixed precision the autotuner also times the dense factorisation's
@@ -325,6 +348,7 @@ def test_autotune_factor_engine_and_camera_warps(gb, abi, scenes, path):
             pt = list(tun.pcg_time_s)
             assert all(t > 0 for t in pt) and tun.camera_warps == (2, 4, 8)[pt.index(min(pt))]
             assert tun.factor_tensor == -1
+            assert tun.num_candidates == 0  # no camera-pair products on the iterative path
         s_tuned = h.solve(hp, opts)
         assert s_tuned.usable
         assert abs(s_tuned.final_cost - s_ref.final_cost) <= 1e-6 * s_ref.final_cost
