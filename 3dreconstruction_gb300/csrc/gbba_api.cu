@@ -2,6 +2,7 @@
 // solve entry, and the forward / backward projection contract that replaces
 // ceres::Problem::Evaluate (3rdparty/ceres/include/ceres/problem.h:392-468)
 // for the reference's reprojection functors.
+#include <math_constants.h>
 #include <cstring>
 
 #include "gbba_device.cuh"
@@ -90,7 +91,8 @@ template <int M, typename T>
 __global__ void __launch_bounds__(256) k_backward(const double* ext, const double* intr, const double* pts,
                                                   const double* obs, const uint32_t* cam, const uint32_t* icam,
                                                   const uint32_t* pt, int64_t no, int64_t nc, int64_t ni, int loss_type,
-                                                  double a, double* je, double* jk, double* jx, double* grad) {
+                                                  double a, double* je, double* jk, double* jx, double* grad,
+                                                  const int* gexp, int pass) {
   constexpr int K = Model<M>::K;
   for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < no; o += (int64_t)gridDim.x * blockDim.x) {
     double E[6], Kp[K], X[3], r[2];
@@ -114,27 +116,51 @@ __global__ void __launch_bounds__(256) k_backward(const double* ext, const doubl
     robust<double>(loss_type, a, r[0] * r[0] + r[1] * r[1], &sr1);
     const double rc0 = r[0] * sr1, rc1 = r[1] * sr1;
     const T s = (T)sr1;
+    const bool out = pass == 1;  // the Jacobians are written by the accumulating pass
     for (int i = 0; i < 2; ++i) {
       for (int j = 0; j < 6; ++j) {
         Je[i][j] *= s;
-        if (je) je[(o * 2 + i) * 6 + j] = (double)Je[i][j];
+        if (je && out) je[(o * 2 + i) * 6 + j] = (double)Je[i][j];
       }
       for (int j = 0; j < K; ++j) {
         Jk[i][j] *= s;
-        if (jk) jk[(o * 2 + i) * K + j] = (double)Jk[i][j];
+        if (jk && out) jk[(o * 2 + i) * K + j] = (double)Jk[i][j];
       }
       for (int j = 0; j < 3; ++j) {
         Jx[i][j] *= s;
-        if (jx) jx[(o * 2 + i) * 3 + j] = (double)Jx[i][j];
+        if (jx && out) jx[(o * 2 + i) * 3 + j] = (double)Jx[i][j];
       }
     }
     if (grad) {
-      for (int j = 0; j < 6; ++j) atomicAdd(&grad[6 * (int64_t)c + j], (double)Je[0][j] * rc0 + (double)Je[1][j] * rc1);
-      for (int j = 0; j < K; ++j)
-        atomicAdd(&grad[6 * nc + K * (int64_t)g + j], (double)Jk[0][j] * rc0 + (double)Jk[1][j] * rc1);
+      // deterministic sums (see lin_fx): pass 0 records each entry's
+      // largest |term|, pass 1 adds the terms in fixed point
+      auto put = [&](int64_t idx, double v) {
+        unsigned long long* q = reinterpret_cast<unsigned long long*>(grad + idx);
+        if (pass == 0) atomicMax(q, isfinite(v) ? (unsigned long long)__double_as_longlong(fabs(v)) : ~0ull);
+        else atomicAdd(q, (unsigned long long)lin_fx(v, gexp[idx]));
+      };
+      for (int j = 0; j < 6; ++j) put(6 * (int64_t)c + j, (double)Je[0][j] * rc0 + (double)Je[1][j] * rc1);
+      for (int j = 0; j < K; ++j) put(6 * nc + K * (int64_t)g + j, (double)Jk[0][j] * rc0 + (double)Jk[1][j] * rc1);
       for (int j = 0; j < 3; ++j)
-        atomicAdd(&grad[6 * nc + K * ni + 3 * (int64_t)p + j], (double)Jx[0][j] * rc0 + (double)Jx[1][j] * rc1);
+        put(6 * nc + K * ni + 3 * (int64_t)p + j, (double)Jx[0][j] * rc0 + (double)Jx[1][j] * rc1);
     }
+  }
+}
+
+// Between the gradient's passes: each entry's scale exponent from its largest
+// term, and the entry cleared for the fixed-point sum; after them: back to
+// FP64 (NaN for an entry with a non-finite term).
+__global__ void k_grad_exp(int64_t n, double nobs, double* __restrict__ grad, int* __restrict__ gexp) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long* q = reinterpret_cast<unsigned long long*>(grad + i);
+    gexp[i] = lin_exp(*q, nobs);
+    *q = 0ull;
+  }
+}
+__global__ void k_grad_conv(int64_t n, double* __restrict__ grad, const int* __restrict__ gexp) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const long long v = __double_as_longlong(grad[i]);
+    grad[i] = gexp[i] >= kFxNonFinite ? CUDART_NAN : ldexp((double)v, -gexp[i]);
   }
 }
 
@@ -487,27 +513,44 @@ static gbba_status project_backward(gbba_handle* h, const gbba_problem* P, int32
     const size_t be = jac_extrinsic ? sizeof(double) * no * 12 : 0;
     const size_t bk = jac_intrinsic ? sizeof(double) * no * 2 * k : 0;
     const size_t bx = jac_point ? sizeof(double) * no * 6 : 0;
-    const size_t bg = gradient ? sizeof(double) * (6 * nc + k * ni + 3 * np) : 0;
+    const int64_t ng = 6 * nc + k * ni + 3 * np;
+    const size_t bg = gradient ? sizeof(double) * ng : 0;
+    const size_t bgx = gradient ? sizeof(int) * ng : 0;  // the gradient entries' scale exponents
     auto al = [](size_t b) { return (b + 255) & ~size_t(255); };
     char* extra;
-    Staged s = stage(h, P, al(be) + al(bk) + al(bx) + al(bg), &extra);
+    Staged s = stage(h, P, al(be) + al(bk) + al(bx) + al(bg) + al(bgx), &extra);
     double* dje = be ? (double*)extra : nullptr;
     double* djk = bk ? (double*)(extra + al(be)) : nullptr;
     double* djx = bx ? (double*)(extra + al(be) + al(bk)) : nullptr;
     double* dg = bg ? (double*)(extra + al(be) + al(bk) + al(bx)) : nullptr;
+    int* dgx = bgx ? (int*)(extra + al(be) + al(bk) + al(bx) + al(bg)) : nullptr;
     cudaStream_t st = h->active;
     if (dg) GBBA_CUDA(cudaMemsetAsync(dg, 0, bg, st));
     const int grid = std::max(1, std::min<int>((int)ceil_div(std::max<int64_t>(no, 1), 256), h->sm_count * 8));
+    const unsigned gg = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ng, 256), 4096));
     auto run = [&](auto kern) {
+      // with a gradient: a pass for the largest terms, the exponents, then
+      // the fixed-point sums (and the Jacobians), then back to FP64
+      if (dg) {
+        kern<<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type,
+                                   loss_scale, dje, djk, djx, dg, dgx, 0);
+        check_launch(h);
+        k_grad_exp<<<gg, 256, 0, st>>>(ng, (double)std::max<int64_t>(1, no), dg, dgx);
+        check_launch(h);
+      }
       kern<<<grid, 256, 0, st>>>(s.ext, s.intr, s.pts, s.obs, s.cam, s.icam, s.pt, no, nc, ni, loss_type, loss_scale,
-                                 dje, djk, djx, dg);
+                                 dje, djk, djx, dg, dgx, 1);
+      check_launch(h);
+      if (dg) {
+        k_grad_conv<<<gg, 256, 0, st>>>(ng, dg, dgx);
+        check_launch(h);
+      }
     };
     switch (P->camera_model) {
       case kPinholeF: fp32 ? run(k_backward<kPinholeF, float>) : run(k_backward<kPinholeF, double>); break;
       case kRadialK3: fp32 ? run(k_backward<kRadialK3, float>) : run(k_backward<kRadialK3, double>); break;
       default: fp32 ? run(k_backward<kBrownT2, float>) : run(k_backward<kBrownT2, double>); break;
     }
-    check_launch(h);
     const cudaMemcpyKind kind = P->memory == GBBA_MEMORY_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     if (be) GBBA_CUDA(cudaMemcpyAsync(jac_extrinsic, dje, be, kind, st));
     if (bk) GBBA_CUDA(cudaMemcpyAsync(jac_intrinsic, djk, bk, kind, st));

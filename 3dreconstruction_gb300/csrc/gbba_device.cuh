@@ -242,4 +242,34 @@ __device__ __forceinline__ float warp_sum(float v) {
   return v;
 }
 
+// ---- deterministic fixed-point sums of FP64 terms: a pass records the
+// largest |term| of each sum (ordered bits under atomicMax), lin_exp picks a
+// power-of-two scale for which n such terms stay below 2^62, and lin_fx
+// rounds each scaled term to an integer (integer sums do not depend on the
+// order of the adds).
+// Scale exponent for a largest term m (ordered bits) and n terms: the sum's
+// bound m n times 2^e stays within 2^62.  kNonFinite marks a column with a
+// non-finite term.
+constexpr int kFxNonFinite = 4000;
+__device__ __forceinline__ int lin_exp(unsigned long long mbits, double n) {
+  if (mbits == ~0ull) return kFxNonFinite;
+  const double m = __longlong_as_double((long long)mbits);
+  if (!(m > 0.0)) return 0;
+  int e;
+  frexp(m * n, &e);  // m n < 2^e
+  return 62 - e;
+}
+// v 2^k rounded to an integer with integer operations (|v| 2^k < 2^62 by
+// the choice of k); any rounding rule serves, the sum is exact.
+__device__ __forceinline__ long long lin_fx(double v, int k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int ex = (int)(b >> 52) & 0x7ff;
+  if (ex == 0 || ex == 0x7ff || k >= kFxNonFinite) return 0;
+  const long long m = (long long)((b & 0xfffffffffffffull) | 0x10000000000000ull);
+  const int sh = ex - 1075 + k;  // |v| 2^k = m 2^sh, m < 2^53, sh <= 9
+  const int rs = min(max(-sh, 0), 63);
+  const long long ml = m << max(min(sh, 9), 0);
+  const long long r = rs ? (ml + (1ll << (rs - 1))) >> rs : ml;
+  return (b >> 63) ? -r : r;
+}
 }  // namespace gbba

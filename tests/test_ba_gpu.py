@@ -55,6 +55,18 @@ def test_forward_backward_match_ceres_autodiff(case, handle, abi):
                                atol=1e-9 * np.abs(g["ref_gradient"]).max())
 
 
+def test_backward_gradient_is_bitwise_repeatable(handle, abi, scenes):
+    """The gradient's per-parameter sums are fixed-point integer sums (a pass
+    for each entry's largest term, then the scaled terms), so repeated calls
+    give the same gradient bit for bit, in both precisions."""
+    sc = scenes.medium_scene(num_cameras=30, num_points=4000, seed=151)
+    for mixed in (False, True):
+        runs = [project(handle, abi, sc, abi.LOSS_HUBER, 4.0, mixed=mixed)["gradient"] for _ in range(3)]
+        assert np.all(np.isfinite(runs[0]))
+        for g in runs[1:]:
+            np.testing.assert_array_equal(g, runs[0])
+
+
 # FP32 Jacobian of the mixed path: each entry within 2e-5 of the largest
 # entry of its block type (extrinsic / intrinsic / point), i.e. a few hundred
 # FP32 ulps of the block scale, which covers the rounding of the FP32 adjoint
