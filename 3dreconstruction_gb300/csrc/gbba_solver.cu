@@ -1312,7 +1312,7 @@ __global__ void __launch_bounds__(128) k_pair_merge(const PairMerge* __restrict_
 
 // Stage 3, one block of 256 threads per camera, from the observation records
 // of the camera (camera CSR):
-//   rhs of the camera's columns = sum of q,
+//   rhs of the camera's columns = sum of q (compact records: q = Jc^T u),
 //   column norms of the scaled, corrected Jacobian -> LM diagonal
 //   D_c^2 = clamp(sum Jc^2), stored in diag_c and (dense) added to S's
 //   diagonal as D_c^2 / radius, and the camera gradient's max norm
@@ -1474,8 +1474,9 @@ __global__ void __launch_bounds__(kRhsThreads) k_rhs_camera(const uint32_t* __re
 // blocks of S (ceres SCHUR_JACOBI, internal/ceres/schur_jacobi_preconditioner.cc;
 // implicit products as in internal/ceres/implicit_schur_complement.cc:69-110):
 //   S p = (U + D_c^2) p - sum_o W_o V_p(o)^-1 W_o^T p
-// The operator data (W, V^-1, U) are in the compute type T and the PCG
-// vectors in FP64.  The FP64 path accumulates in FP64; the mixed path forms
+// with W_o = Jc_o^T Jp_o formed where it is used, from the compact
+// observation records (RecC).  The operator data (Jc, Jp, V^-1, U) are in
+// the compute type T and the PCG vectors in FP64.  The FP64 path accumulates in FP64; the mixed path forms
 // the per-observation products and their sums in FP32 (Kahan-compensated
 // where a camera sums thousands of them) and widens the per-camera sums.
 
