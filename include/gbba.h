@@ -74,7 +74,10 @@ typedef enum gbba_loss {
 typedef enum gbba_linear_solver {
   GBBA_SOLVER_AUTO = 0,            /* dense Schur up to options.dense_schur_max_size, else iterative */
   GBBA_SOLVER_DENSE_SCHUR = 1,     /* dense Cholesky of the reduced camera system S */
-  GBBA_SOLVER_ITERATIVE_SCHUR = 2  /* block-Jacobi PCG on S */
+  GBBA_SOLVER_ITERATIVE_SCHUR = 2  /* block-Jacobi PCG on S; every free intrinsic group must belong to one
+                                      camera (else GBBA_ERROR_NOT_SUPPORTED); the dense solver takes any
+                                      grouping (a free group shared by several cameras uses the point-major
+                                      Schur build, whose FP atomics are not bit-repeatable) */
 } gbba_linear_solver;
 
 typedef enum gbba_precision {
