@@ -1556,27 +1556,37 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
     ei[e] = idx < NT ? i : 0;
     ej[e] = idx < NT ? idx - i * (i + 1) / 2 : 0;
   }
+  // Observations in flight: two records in registers (pa, pb, used in
+  // turn) and the index of the next one to load, so that neither the index
+  // load nor the record load waits on the other.
+  constexpr int W = kCamWarps;
   const uint32_t q0 = cam_off[c] + warp, q1 = cam_off[c + 1];
-  T pre[F];
-  auto fetch = [&](uint32_t q) {
-    const T* r = rec + (int64_t)cam_obs[q] * R::kSize;
+  T pa[F], pb[F];
+  auto fetch = [&](uint32_t o, T(&p)[F]) {
+    const T* r = rec + (int64_t)o * R::kSize;
 #pragma unroll
-    for (int f = 0; f < F; ++f) pre[f] = dst[f] >= 0 ? r[lane + 32 * f] : T(0);
+    for (int f = 0; f < F; ++f) p[f] = dst[f] >= 0 ? r[lane + 32 * f] : T(0);
   };
-  if (q0 < q1) fetch(q0);
+  if (q0 < q1) fetch(cam_obs[q0], pa);
+  if (q0 + W < q1) fetch(cam_obs[q0 + W], pb);
+  uint32_t onext = q0 + 2 * W < q1 ? cam_obs[q0 + 2 * W] : 0u;
   // FP32: FP32 products and Kahan-compensated FP32 sums (GB300 runs FP64 at
   // a small fraction of the FP32 rate; a camera sums thousands of terms)
   using A = T;
   A su[E], cu[E], ss[E], cs[E];
 #pragma unroll
   for (int e = 0; e < E; ++e) su[e] = cu[e] = ss[e] = cs[e] = A(0);
-  for (uint32_t q = q0; q < q1; q += kCamWarps) {
+  // observation q from the registers p, which then take observation q + 2W
+  auto step = [&](uint32_t q, T(&p)[F]) {
     __syncwarp();
 #pragma unroll
     for (int f = 0; f < F; ++f)
-      if (dst[f] >= 0) sw[dst[f]] = pre[f];
+      if (dst[f] >= 0) sw[dst[f]] = p[f];
     __syncwarp();
-    if (q + kCamWarps < q1) fetch(q + kCamWarps);
+    if (q + 2 * W < q1) {
+      fetch(onext, p);
+      onext = q + 3 * W < q1 ? cam_obs[q + 3 * W] : 0u;
+    }
     if (lane < 4) {
       const int a = lane >> 1, b = lane & 1;
       const T* jp = sw + kP;
@@ -1605,6 +1615,10 @@ __global__ void __launch_bounds__(kCamWarps * 32) k_cam_blocks(const uint32_t* _
         ss[e] += u - w;
       }
     }
+  };
+  for (uint32_t q = q0; q < q1; q += 2 * W) {
+    step(q, pa);
+    if (q + W < q1) step(q + W, pb);
   }
 #pragma unroll
   for (int e = 0; e < E; ++e) {
